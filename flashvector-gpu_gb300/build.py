@@ -1,0 +1,96 @@
+"""Build recipe for libfvgb300.so (CUDA kernels + C ABI + C++ host engine).
+
+Compiles every translation unit under csrc/ for sm_103a in parallel with
+nvcc and links one shared library next to this file (in-tree, so the
+process that loads it is visibly using it). Re-running is incremental:
+an object is rebuilt only when its source or any header is newer.
+
+    python flashvector-gpu_gb300/build.py [--force] [--jobs N]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+OBJ = PKG / "_build"
+LIB = PKG / "fvgb300" / "libfvgb300.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+              "-Xptxas", "-warn-spills", f"-I{ROOT / 'include'}"]
+CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", f"-I{ROOT / 'include'}", "-I/usr/local/cuda/include"]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _headers() -> list[Path]:
+    return list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
+
+
+def _stale(src: Path, obj: Path, newest_header: float) -> bool:
+    if not obj.exists():
+        return True
+    t = obj.stat().st_mtime
+    return src.stat().st_mtime > t or newest_header > t
+
+
+def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -> Path:
+    OBJ.mkdir(exist_ok=True)
+    nvcc = _nvcc()
+    newest = max((h.stat().st_mtime for h in _headers()), default=0.0)
+    cmds = []
+    objs = []
+    for src in sorted(CSRC.glob("*.cu")):
+        obj = OBJ / (src.stem + ".o")
+        objs.append(obj)
+        if force or _stale(src, obj, newest):
+            cmds.append([nvcc, *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)])
+    for src in sorted(CSRC.glob("*.cpp")):
+        obj = OBJ / (src.stem + ".cpp.o")
+        objs.append(obj)
+        if force or _stale(src, obj, newest):
+            cmds.append(["g++", *CXX_FLAGS, "-c", str(src), "-o", str(obj)])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        if verbose and (r.stderr.strip()):
+            print(r.stderr, flush=True)
+        return r
+
+    if cmds:
+        with ThreadPoolExecutor(max_workers=jobs or min(len(cmds), os.cpu_count() or 4)) as ex:
+            list(ex.map(run, cmds))
+    if force or cmds or not LIB.exists():
+        link = [nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcuda", "-Xcompiler", "-fopenmp"]
+        run(link)
+    return LIB
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("--jobs", type=int, default=None)
+    ap.add_argument("-v", "--verbose", action="store_true")
+    a = ap.parse_args()
+    print(build(force=a.force, jobs=a.jobs, verbose=a.verbose))
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,230 @@
+// bridge.cu -- the C ABI of libfvgb300: device / memory / stream plumbing,
+// argument validation and clamps of the drop-in search entry points, the
+// per-stream scratch arena, the device status word and the launch counter.
+//
+// Plumbing functions replace hnsw_traverse.cu:525-637 one for one (same
+// CUDA calls, same null/zero-size handling); the search entry points keep
+// the reference's validation order and clamps (sparse_hybrid.cu:96-101,
+// 517-518).
+#include <atomic>
+#include <mutex>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/fv_bridge.h"
+#include "common.cuh"
+#include "kernels.h"
+
+namespace fv {
+
+namespace {
+std::atomic<uint64_t> g_launches{0};
+
+struct Arena {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  bool owned = true;
+};
+std::mutex g_arena_mu;
+// keyed by (device, stream)
+std::unordered_map<uint64_t, Arena> g_arenas;
+
+uint64_t arena_key(cudaStream_t s) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  return (uint64_t)(uintptr_t)s * 64u + (uint64_t)dev;
+}
+
+std::mutex g_dev_mu;
+std::vector<int> g_sm_counts;
+std::vector<uint32_t*> g_status;
+}  // namespace
+
+void note_launch(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int device_sm_count() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  if ((int)g_sm_counts.size() <= dev) g_sm_counts.resize(dev + 1, 0);
+  if (g_sm_counts[dev] == 0) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    g_sm_counts[dev] = n > 0 ? n : 1;
+  }
+  return g_sm_counts[dev];
+}
+
+uint32_t* status_word() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  if ((int)g_status.size() <= dev) g_status.resize(dev + 1, nullptr);
+  if (!g_status[dev]) {
+    uint32_t* p = nullptr;
+    if (cudaMalloc(&p, sizeof(uint32_t)) != cudaSuccess) return nullptr;
+    cudaMemset(p, 0, sizeof(uint32_t));
+    g_status[dev] = p;
+  }
+  return g_status[dev];
+}
+
+void* scratch_get(cudaStream_t stream, size_t bytes) {
+  if (bytes == 0) bytes = 256;
+  bytes = (bytes + 255) & ~(size_t)255;
+  std::lock_guard<std::mutex> lk(g_arena_mu);
+  Arena& a = g_arenas[arena_key(stream)];
+  if (a.bytes >= bytes) return a.ptr;
+  if (!a.owned) return nullptr;  // caller-provided arena too small: refuse
+  if (a.ptr) cudaFreeAsync(a.ptr, stream);
+  a.ptr = nullptr;
+  a.bytes = 0;
+  size_t grow = bytes + bytes / 4;
+  if (cudaMallocAsync(&a.ptr, grow, stream) != cudaSuccess) {
+    cudaGetLastError();
+    a.ptr = nullptr;
+    return nullptr;
+  }
+  a.bytes = grow;
+  return a.ptr;
+}
+
+}  // namespace fv
+
+using fv::note_launch;
+
+extern "C" {
+
+// ---------------------------------------------------------------- plumbing
+int cuda_init_device(int device_id) {
+  cudaError_t e = cudaSetDevice(device_id);
+  if (e != cudaSuccess) return (int)e;
+  return (int)cudaFree(0);
+}
+int cuda_set_device(int device_id) { return (int)cudaSetDevice(device_id); }
+int cuda_get_device_count(int* count) {
+  if (!count) return FV_ERR_NULL;
+  return (int)cudaGetDeviceCount(count);
+}
+int cuda_get_device_memory(size_t* free_bytes, size_t* total_bytes) {
+  if (!free_bytes || !total_bytes) return FV_ERR_NULL;
+  return (int)cudaMemGetInfo(free_bytes, total_bytes);
+}
+int cuda_device_synchronize(void) { return (int)cudaDeviceSynchronize(); }
+int cuda_malloc_device(void** ptr, size_t bytes) {
+  if (!ptr || bytes == 0) return FV_ERR_NULL;
+  return (int)cudaMalloc(ptr, bytes);
+}
+int cuda_free_device(void* ptr) { return ptr ? (int)cudaFree(ptr) : 0; }
+int cuda_malloc_host(void** ptr, size_t bytes) {
+  if (!ptr || bytes == 0) return FV_ERR_NULL;
+  return (int)cudaHostAlloc(ptr, bytes, cudaHostAllocMapped);
+}
+int cuda_free_host(void* ptr) { return ptr ? (int)cudaFreeHost(ptr) : 0; }
+int cuda_memcpy_h2d_async(void* dst, const void* src, size_t bytes, void* stream) {
+  if (!dst || !src) return FV_ERR_NULL;
+  if (bytes == 0) return 0;
+  return (int)cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream);
+}
+int cuda_memcpy_d2h_async(void* dst, const void* src, size_t bytes, void* stream) {
+  if (!dst || !src) return FV_ERR_NULL;
+  if (bytes == 0) return 0;
+  return (int)cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+}
+int cuda_memset_device_async(void* dst, int value, size_t bytes, void* stream) {
+  if (!dst) return FV_ERR_NULL;
+  if (bytes == 0) return 0;
+  return (int)cudaMemsetAsync(dst, value, bytes, (cudaStream_t)stream);
+}
+int cuda_host_get_device_pointer(void** dev_ptr, void* host_ptr) {
+  if (!dev_ptr || !host_ptr) return FV_ERR_NULL;
+  return (int)cudaHostGetDevicePointer(dev_ptr, host_ptr, 0);
+}
+int cuda_create_stream(void** stream) {
+  if (!stream) return FV_ERR_NULL;
+  return (int)cudaStreamCreateWithFlags((cudaStream_t*)stream, cudaStreamNonBlocking);
+}
+int cuda_destroy_stream(void* stream) {
+  if (!stream) return 0;
+  {
+    std::lock_guard<std::mutex> lk(fv::g_arena_mu);
+    auto it = fv::g_arenas.find(fv::arena_key((cudaStream_t)stream));
+    if (it != fv::g_arenas.end()) {
+      if (it->second.owned && it->second.ptr) cudaFreeAsync(it->second.ptr, (cudaStream_t)stream);
+      fv::g_arenas.erase(it);
+    }
+  }
+  return (int)cudaStreamDestroy((cudaStream_t)stream);
+}
+int cuda_sync_stream(void* stream) {
+  if (!stream) return (int)cudaDeviceSynchronize();
+  return (int)cudaStreamSynchronize((cudaStream_t)stream);
+}
+
+// ------------------------------------------------------------ flat scan
+int cuda_flat_scan_batch(const float* d_vectors, const uint32_t* d_vec_ids, uint32_t num_vectors, uint32_t dim,
+                         const float* d_queries, uint32_t num_queries, uint32_t top_k, MetricType metric,
+                         const uint32_t* d_valid_mask, GpuSearchResult* d_out_results, void* stream) {
+  if (!d_queries || !d_out_results) return FV_ERR_NULL;
+  if (num_vectors > 0 && !d_vectors) return FV_ERR_NULL;
+  if (num_queries == 0 || top_k == 0) return 0;
+  if (top_k > (uint32_t)fv::kMaxTopK) top_k = fv::kMaxTopK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (num_vectors == 0) {
+    // the reference fills the outputs with 0xFF bytes here (ids 0xFFFFFFFF,
+    // distance bits 0xFFFFFFFF), not with the 1e30 sentinel
+    return (int)cudaMemsetAsync(d_out_results, 0xFF, (size_t)num_queries * top_k * sizeof(GpuSearchResult), s);
+  }
+  if (dim == 0) return FV_ERR_ARG;
+  return fv::launch_flat_f32(d_vectors, d_vec_ids, num_vectors, dim, d_queries, num_queries, top_k, metric,
+                             d_valid_mask, d_out_results, 0, s);
+}
+
+// ------------------------------------------------------------- fixtures
+int cuda_compute_distances_warp(const float* d_queries, const float* d_dataset, uint32_t num_queries,
+                                uint32_t num_vectors, uint32_t dim, MetricType metric, float* d_out_distances,
+                                void* stream) {
+  if (!d_queries || !d_dataset || !d_out_distances) return FV_ERR_NULL;
+  return fv::launch_distance_matrix(d_queries, d_dataset, num_queries, num_vectors, dim, metric, d_out_distances,
+                                    (cudaStream_t)stream);
+}
+
+int cuda_bitonic_sort_test(const float* d_keys_in, const uint32_t* d_vals_in, float* d_keys_out, uint32_t* d_vals_out,
+                           uint32_t n, void* stream) {
+  if (!d_keys_in || !d_vals_in || !d_keys_out || !d_vals_out) return FV_ERR_NULL;
+  return fv::launch_bitonic_test(d_keys_in, d_vals_in, d_keys_out, d_vals_out, n, (cudaStream_t)stream);
+}
+
+// ----------------------------------------------------------- extensions
+const char* fv_version(void) { return "fvgb300 0.1 sm_103a"; }
+
+int fv_read_device_status(uint32_t* status) {
+  if (!status) return FV_ERR_NULL;
+  uint32_t* w = fv::status_word();
+  if (!w) return (int)cudaErrorMemoryAllocation;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return (int)e;
+  e = cudaMemcpy(status, w, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return (int)e;
+  return (int)cudaMemset(w, 0, sizeof(uint32_t));
+}
+
+uint64_t fv_launch_count(void) { return fv::g_launches.load(std::memory_order_relaxed); }
+
+int fv_set_stream_scratch(void* stream, void* d_ptr, size_t bytes) {
+  std::lock_guard<std::mutex> lk(fv::g_arena_mu);
+  fv::Arena& a = fv::g_arenas[fv::arena_key((cudaStream_t)stream)];
+  if (a.owned && a.ptr) cudaFreeAsync(a.ptr, (cudaStream_t)stream);
+  if (d_ptr) {
+    a.ptr = d_ptr;
+    a.bytes = bytes;
+    a.owned = false;
+  } else {
+    a = fv::Arena{};
+  }
+  return 0;
+}
+
+int fv_release_stream_scratch(void* stream) { return fv_set_stream_scratch(stream, nullptr, 0); }
+
+}  // extern "C"

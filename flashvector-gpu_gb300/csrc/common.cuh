@@ -1,0 +1,133 @@
+// common.cuh -- device helpers shared by every kernel of libfvgb300.
+//
+// Ordering convention used by all top-k code here: a candidate is the
+// 64-bit key (order(dist) << 32) | slot, where order() maps an IEEE float
+// to an unsigned integer with the same ordering. Comparing keys therefore
+// compares (distance, slot) lexicographically, which is the reference's
+// tie rule for the exact scans (strict `<` while scanning slots in
+// ascending order keeps the lower slot: sparse_hybrid.cu:42-72,
+// ivf_quant_lookup.cu:1010-1019).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/fv_types.h"
+
+namespace fv {
+
+constexpr uint32_t kInvalidId = 0xFFFFFFFFu;
+constexpr float kSentinelDist = 1e30f;  // unfilled result slot distance
+constexpr int kMaxTopK = 256;           // reference clamp (streams.rs:14)
+
+// Device status word: bounded waits and bounds checks set bits here
+// instead of trapping, so the context stays usable and the host can read
+// the cause with fv_read_device_status().
+enum : uint32_t {
+  kStatusMbarTimeout = 1u << 0,
+  kStatusBounds = 1u << 1,
+  kStatusOverflow = 1u << 2,
+};
+// The word lives in device memory owned by the bridge (status_word());
+// kernels receive its address as an argument.
+__device__ __forceinline__ void set_status(uint32_t* status, uint32_t bits) {
+  if (status) atomicOr(status, bits);
+}
+
+// Order-preserving float -> uint32 map. -0.0 is folded onto +0.0 first so
+// that the two zeros compare equal, as they do under float `<`.
+__host__ __device__ __forceinline__ uint32_t float_order(float f) {
+  f = f + 0.0f;
+#ifdef __CUDA_ARCH__
+  uint32_t u = __float_as_uint(f);
+#else
+  uint32_t u;
+  __builtin_memcpy(&u, &f, 4);
+#endif
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__host__ __device__ __forceinline__ float order_float(uint32_t o) {
+  uint32_t u = (o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o;
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float f;
+  __builtin_memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+
+__host__ __device__ __forceinline__ uint64_t make_key(float dist, uint32_t slot) {
+  return ((uint64_t)float_order(dist) << 32) | slot;
+}
+__host__ __device__ __forceinline__ float key_dist(uint64_t k) { return order_float((uint32_t)(k >> 32)); }
+__host__ __device__ __forceinline__ uint32_t key_slot(uint64_t k) { return (uint32_t)k; }
+
+// Key of an empty slot: larger than the key of every admissible candidate
+// (admissible = distance < 1e30, which also rejects NaN).
+constexpr uint64_t kSentinelKey = 0xFFFFFFFFFFFFFFFFull;
+
+// Packed LSB-first validity bit of slot `i` (nullptr = everything valid).
+// Same bit convention as the reference (distance_metrics.cuh:17-20,
+// filter.rs:364-371).
+__device__ __forceinline__ bool mask_allows(const uint32_t* __restrict__ mask, uint32_t i) {
+  return mask == nullptr || ((__ldg(mask + (i >> 5)) >> (i & 31u)) & 1u);
+}
+
+__device__ __forceinline__ GpuSearchResult key_to_result(uint64_t key, const uint32_t* __restrict__ vec_ids) {
+  GpuSearchResult r;
+  if (key == kSentinelKey) {
+    r.id = kInvalidId;
+    r.distance = kSentinelDist;
+  } else {
+    uint32_t slot = key_slot(key);
+    r.id = vec_ids ? __ldg(vec_ids + slot) : slot;
+    r.distance = key_dist(key);
+  }
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// The reference's warp-cooperative fp32 distance, restated: lane l sums the
+// dimensions l, l+32, ... with fmaf; the 32 partials are reduced with the
+// shuffle-down tree 16, 8, 4, 2, 1 and lane 0's value is returned to every
+// lane (distance_metrics.cuh:53-138). Using the same order makes the rerank
+// distances of the IVF paths bit-identical to the reference's.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float warp_tree_sum(float v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  return __shfl_sync(0xffffffffu, v, 0);
+}
+
+__device__ __forceinline__ float warp_metric_distance(const float* __restrict__ q, const float* __restrict__ x,
+                                                      uint32_t dim, int lane, MetricType metric) {
+  if (metric == METRIC_INNER_PRODUCT) {
+    float dot = 0.f;
+    for (uint32_t d = lane; d < dim; d += 32) dot = fmaf(q[d], __ldg(x + d), dot);
+    return -warp_tree_sum(dot);
+  }
+  if (metric == METRIC_COSINE) {
+    float dot = 0.f, nq = 0.f, nx = 0.f;
+    for (uint32_t d = lane; d < dim; d += 32) {
+      float a = q[d], b = __ldg(x + d);
+      dot = fmaf(a, b, dot);
+      nq = fmaf(a, a, nq);
+      nx = fmaf(b, b, nx);
+    }
+    dot = warp_tree_sum(dot);
+    nq = warp_tree_sum(nq);
+    nx = warp_tree_sum(nx);
+    float denom = __fadd_rn(__fmul_rn(sqrtf(nq), sqrtf(nx)), 1e-8f);
+    return __fsub_rn(1.0f, __fdiv_rn(dot, denom));
+  }
+  float acc = 0.f;
+  for (uint32_t d = lane; d < dim; d += 32) {
+    float diff = q[d] - __ldg(x + d);
+    acc = fmaf(diff, diff, acc);
+  }
+  return warp_tree_sum(acc);
+}
+
+}  // namespace fv

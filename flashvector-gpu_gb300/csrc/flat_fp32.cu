@@ -1,0 +1,338 @@
+// flat_fp32.cu -- exact fp32 flat scan fused with top-k.
+//
+// Replaces the reference's flat_scan_kernel / launch_flat_scan
+// (sparse_hybrid.cu:13-107). Same contract, different machine mapping:
+//
+//  * a CTA owns 64 queries and a contiguous range of base tiles (128 rows);
+//    every base tile is staged once in shared memory and scored against all
+//    64 queries (the reference re-streams the whole base set per query);
+//  * each thread accumulates a 4 x 8 block of (query, row) distances,
+//    walking the dimensions in ascending order with separately rounded
+//    subtract / multiply / add -- the order of the reference's own exact
+//    search RecallEvaluator::exact_knn (metrics.rs:103-135), so distances
+//    are bit-identical to it;
+//  * per query a max-heap of (distance, slot) keys in shared memory keeps
+//    the running top-k (ties -> lower slot, as the reference's strict `<`
+//    insertion in slot order);
+//  * when the base range is split over several CTAs the per-split heaps go
+//    to scratch and a second kernel merges them.
+#include "common.cuh"
+#include "kernels.h"
+#include "topk.cuh"
+
+namespace fv {
+
+namespace {
+
+constexpr int QT = 64;    // queries per CTA
+constexpr int VT = 128;   // base rows per tile
+constexpr int DK = 32;    // dimensions per staged chunk
+constexpr int NT = 256;   // threads per CTA
+constexpr int QS = QT + 1;  // padded row strides (bank-conflict free)
+constexpr int VS = VT + 1;
+
+struct FlatArgs {
+  const float* vectors;
+  const uint32_t* vec_ids;
+  uint32_t n, dim;
+  const float* queries;
+  uint32_t nq, k;
+  const uint32_t* mask;
+  GpuSearchResult* out;   // written directly when splits == 1
+  uint64_t* partial;      // [nq][splits][k] heap dumps when splits > 1
+  uint32_t splits, tiles_per_split;
+};
+
+__device__ __forceinline__ void heap_replace_root(uint64_t* heap, int k, int lane_stride, uint64_t key) {
+  // max-heap stored interleaved: element i of this query at heap[i * lane_stride]
+  int i = 0;
+  while (true) {
+    int l = 2 * i + 1;
+    if (l >= k) break;
+    uint64_t cv = heap[l * lane_stride];
+    int c = l;
+    if (l + 1 < k) {
+      uint64_t rv = heap[(l + 1) * lane_stride];
+      if (rv > cv) { cv = rv; c = l + 1; }
+    }
+    if (cv <= key) break;
+    heap[i * lane_stride] = cv;
+    i = c;
+  }
+  heap[i * lane_stride] = key;
+}
+
+// In-place heapsort of a max-heap (ascending result).
+__device__ void heap_sort_ascending(uint64_t* heap, int k, int s) {
+  for (int end = k - 1; end > 0; --end) {
+    uint64_t top = heap[0];
+    uint64_t last = heap[end * s];
+    heap[end * s] = top;
+    // sift `last` down from the root within [0, end)
+    int i = 0;
+    while (true) {
+      int l = 2 * i + 1;
+      if (l >= end) break;
+      uint64_t cv = heap[l * s];
+      int c = l;
+      if (l + 1 < end) {
+        uint64_t rv = heap[(l + 1) * s];
+        if (rv > cv) { cv = rv; c = l + 1; }
+      }
+      if (cv <= last) break;
+      heap[i * s] = cv;
+      i = c;
+    }
+    heap[i * s] = last;
+  }
+}
+
+template <int METRIC, bool VEC4>
+__global__ void __launch_bounds__(NT) flat_f32_scan_kernel(FlatArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* qs = reinterpret_cast<float*>(smem_raw);  // [DK][QS]
+  float* xs = qs + DK * QS;                          // [DK][VS]
+  float* ds = xs + DK * VS;                          // [QT][VS] distances of a tile
+  float* qn = ds + QT * VS;                          // [QT]
+  float* xn = qn + QT;                               // [VT]
+  uint64_t* heap = reinterpret_cast<uint64_t*>(xn + VT);  // [k][QT], 8B aligned (see smem size)
+
+  const int tid = threadIdx.x;
+  const int ty = tid >> 4, tx = tid & 15;
+  const uint32_t q0 = blockIdx.x * QT;
+  const uint32_t k = a.k;
+  const uint32_t ntiles = (a.n + VT - 1) / VT;
+  const uint32_t t_begin = blockIdx.y * a.tiles_per_split;
+  const uint32_t t_end = min(t_begin + a.tiles_per_split, ntiles);
+
+  for (uint32_t i = tid; i < k * QT; i += NT) heap[i] = kSentinelKey;
+  if (METRIC == METRIC_COSINE && tid < QT) {
+    float s = 0.f;
+    if (q0 + tid < a.nq) {
+      const float* q = a.queries + (size_t)(q0 + tid) * a.dim;
+      for (uint32_t d = 0; d < a.dim; ++d) s = __fadd_rn(s, __fmul_rn(q[d], q[d]));
+    }
+    qn[tid] = s;
+  }
+  __syncthreads();
+
+  uint64_t worst = kSentinelKey;  // cached heap root of query `tid` (tid < QT)
+
+  for (uint32_t t = t_begin; t < t_end; ++t) {
+    const uint32_t v0 = t * VT;
+    float acc[4][8];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+    float xnorm = 0.f;
+
+    for (uint32_t d0 = 0; d0 < a.dim; d0 += DK) {
+      const uint32_t dk = min((uint32_t)DK, a.dim - d0);
+      __syncthreads();  // previous chunk fully consumed
+      if (VEC4) {
+        // 64 queries x 32 dims = 512 float4; 128 rows x 32 dims = 1024 float4
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          int e = tid + NT * r;
+          int qi = e >> 3, dd = (e & 7) * 4;
+          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (q0 + qi < a.nq && d0 + dd < a.dim)
+            v = __ldg(reinterpret_cast<const float4*>(a.queries + (size_t)(q0 + qi) * a.dim + d0 + dd));
+          qs[(dd + 0) * QS + qi] = v.x;
+          qs[(dd + 1) * QS + qi] = v.y;
+          qs[(dd + 2) * QS + qi] = v.z;
+          qs[(dd + 3) * QS + qi] = v.w;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          int e = tid + NT * r;
+          int vi = e >> 3, dd = (e & 7) * 4;
+          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (v0 + vi < a.n && d0 + dd < a.dim)
+            v = __ldg(reinterpret_cast<const float4*>(a.vectors + (size_t)(v0 + vi) * a.dim + d0 + dd));
+          xs[(dd + 0) * VS + vi] = v.x;
+          xs[(dd + 1) * VS + vi] = v.y;
+          xs[(dd + 2) * VS + vi] = v.z;
+          xs[(dd + 3) * VS + vi] = v.w;
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < (QT * DK) / NT; ++r) {
+          int e = tid + NT * r;
+          int qi = e / DK, dd = e % DK;
+          float v = 0.f;
+          if (q0 + qi < a.nq && d0 + dd < a.dim) v = __ldg(a.queries + (size_t)(q0 + qi) * a.dim + d0 + dd);
+          qs[dd * QS + qi] = v;
+        }
+#pragma unroll
+        for (int r = 0; r < (VT * DK) / NT; ++r) {
+          int e = tid + NT * r;
+          int vi = e / DK, dd = e % DK;
+          float v = 0.f;
+          if (v0 + vi < a.n && d0 + dd < a.dim) v = __ldg(a.vectors + (size_t)(v0 + vi) * a.dim + d0 + dd);
+          xs[dd * VS + vi] = v;
+        }
+      }
+      __syncthreads();
+
+      if (METRIC == METRIC_COSINE && tid < VT) {
+        for (uint32_t dd = 0; dd < dk; ++dd) {
+          float x = xs[dd * VS + tid];
+          xnorm = __fadd_rn(xnorm, __fmul_rn(x, x));
+        }
+      }
+
+      auto step = [&](int dd) {
+        float qv[4], xv[8];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) qv[i] = qs[dd * QS + ty * 4 + i];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) xv[j] = xs[dd * VS + tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            if (METRIC == METRIC_L2) {
+              float diff = __fsub_rn(qv[i], xv[j]);
+              acc[i][j] = __fadd_rn(acc[i][j], __fmul_rn(diff, diff));
+            } else {
+              acc[i][j] = __fadd_rn(acc[i][j], __fmul_rn(qv[i], xv[j]));
+            }
+          }
+      };
+      if (dk == DK) {
+#pragma unroll 8
+        for (int dd = 0; dd < DK; ++dd) step(dd);
+      } else {
+        for (uint32_t dd = 0; dd < dk; ++dd) step((int)dd);
+      }
+    }
+
+    if (METRIC == METRIC_COSINE && tid < VT) xn[tid] = xnorm;
+    __syncthreads();  // xn visible; previous selection finished reading ds
+
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int qi = ty * 4 + i;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int vi = tx + 16 * j;
+        float dist;
+        if (METRIC == METRIC_L2) {
+          dist = acc[i][j];
+        } else if (METRIC == METRIC_INNER_PRODUCT) {
+          dist = -acc[i][j];
+        } else {
+          float denom = __fadd_rn(__fmul_rn(sqrtf(qn[qi]), sqrtf(xn[vi])), 1e-8f);
+          dist = __fsub_rn(1.0f, __fdiv_rn(acc[i][j], denom));
+        }
+        const uint32_t slot = v0 + vi;
+        bool ok = slot < a.n && mask_allows(a.mask, slot);
+        ds[qi * VS + vi] = ok ? dist : __int_as_float(0x7fc00000);  // NaN never passes `<`
+      }
+    }
+    __syncthreads();
+
+    if (tid < QT && q0 + tid < a.nq) {
+      uint64_t* h = heap + tid;
+      for (int vi = 0; vi < VT; ++vi) {
+        float dist = ds[tid * VS + vi];
+        if (dist < kSentinelDist) {
+          uint64_t key = make_key(dist, v0 + vi);
+          if (key < worst) {
+            heap_replace_root(h, (int)k, QT, key);
+            worst = h[0];
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  if (tid < QT && q0 + tid < a.nq) {
+    uint64_t* h = heap + tid;
+    const uint32_t q = q0 + tid;
+    if (a.splits == 1) {
+      heap_sort_ascending(h, (int)k, QT);
+      for (uint32_t r = 0; r < k; ++r) a.out[(size_t)q * k + r] = key_to_result(h[r * QT], a.vec_ids);
+    } else {
+      uint64_t* dst = a.partial + ((size_t)q * a.splits + blockIdx.y) * k;
+      for (uint32_t r = 0; r < k; ++r) dst[r] = h[r * QT];
+    }
+  }
+}
+
+}  // namespace
+
+// Merges `lists` unsorted candidate lists of `k` keys per query into the
+// ascending top-k; one CTA per query, bitonic sort in shared memory.
+__global__ void __launch_bounds__(256) merge_partial_topk_kernel(const uint64_t* __restrict__ partial, uint32_t lists,
+                                                                 uint32_t k, uint32_t pow2, const uint32_t* vec_ids,
+                                                                 GpuSearchResult* __restrict__ out, uint32_t out_k) {
+  extern __shared__ uint64_t keys[];
+  const uint32_t q = blockIdx.x;
+  const uint32_t total = lists * k;
+  const uint64_t* src = partial + (size_t)q * total;
+  for (uint32_t i = threadIdx.x; i < pow2; i += blockDim.x) keys[i] = i < total ? src[i] : kSentinelKey;
+  __syncthreads();
+  block_bitonic_sort(keys, pow2);
+  for (uint32_t r = threadIdx.x; r < out_k; r += blockDim.x) out[(size_t)q * out_k + r] = key_to_result(keys[r], vec_ids);
+}
+
+size_t flat_f32_smem_bytes(uint32_t k) {
+  size_t floats = (size_t)DK * QS + (size_t)DK * VS + (size_t)QT * VS + QT + VT;
+  size_t bytes = floats * 4;
+  bytes = (bytes + 7) & ~(size_t)7;
+  return bytes + (size_t)k * QT * 8;
+}
+
+int launch_flat_f32(const float* vectors, const uint32_t* vec_ids, uint32_t n, uint32_t dim, const float* queries,
+                    uint32_t nq, uint32_t k, MetricType metric, const uint32_t* mask, GpuSearchResult* out,
+                    uint32_t forced_splits, cudaStream_t stream) {
+  const uint32_t nqb = (nq + QT - 1) / QT;
+  const uint32_t ntiles = (n + VT - 1) / VT;
+  int sms = device_sm_count();
+  uint32_t splits = forced_splits ? forced_splits : (uint32_t)((2 * sms + nqb - 1) / nqb);
+  const uint32_t pow2k = next_pow2(k);
+  splits = std::max(1u, std::min(splits, std::min(ntiles, 8192u / pow2k)));
+  uint32_t tps = (ntiles + splits - 1) / splits;
+  splits = (ntiles + tps - 1) / tps;
+
+  FlatArgs a{vectors, vec_ids, n, dim, queries, nq, k, mask, out, nullptr, splits, tps};
+  const size_t total_keys = (size_t)nq * splits * k;
+  if (splits > 1) {
+    a.partial = static_cast<uint64_t*>(scratch_get(stream, total_keys * 8));
+    if (!a.partial) return (int)cudaErrorMemoryAllocation;
+  }
+
+  const size_t smem = flat_f32_smem_bytes(k);
+  const bool vec4 = (dim % 4 == 0) && ((uintptr_t)vectors % 16 == 0) && ((uintptr_t)queries % 16 == 0);
+  dim3 grid(nqb, splits);
+  auto go = [&](auto kern) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<grid, NT, smem, stream>>>(a);
+  };
+  switch (metric) {
+    case METRIC_INNER_PRODUCT:
+      vec4 ? go(flat_f32_scan_kernel<METRIC_INNER_PRODUCT, true>) : go(flat_f32_scan_kernel<METRIC_INNER_PRODUCT, false>);
+      break;
+    case METRIC_COSINE:
+      vec4 ? go(flat_f32_scan_kernel<METRIC_COSINE, true>) : go(flat_f32_scan_kernel<METRIC_COSINE, false>);
+      break;
+    default:
+      vec4 ? go(flat_f32_scan_kernel<METRIC_L2, true>) : go(flat_f32_scan_kernel<METRIC_L2, false>);
+      break;
+  }
+  note_launch();
+  if (splits > 1) {
+    const uint32_t pow2 = next_pow2(splits * k);
+    const size_t msmem = (size_t)pow2 * 8;
+    cudaFuncSetAttribute(merge_partial_topk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msmem);
+    merge_partial_topk_kernel<<<nq, 256, msmem, stream>>>(a.partial, splits, k, pow2, vec_ids, out, k);
+    note_launch();
+  }
+  return (int)cudaGetLastError();
+}
+
+}  // namespace fv

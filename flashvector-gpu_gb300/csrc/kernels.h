@@ -1,0 +1,53 @@
+// kernels.h -- internal (C++) interface between the C-ABI bridge and the
+// kernel translation units. Nothing here crosses the library boundary.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "../../include/fv_types.h"
+
+namespace fv {
+
+inline uint32_t next_pow2(uint32_t v) {
+  if (v <= 1) return 1;
+  --v;
+  v |= v >> 1;
+  v |= v >> 2;
+  v |= v >> 4;
+  v |= v >> 8;
+  v |= v >> 16;
+  return v + 1;
+}
+
+// Streaming-multiprocessor count of the current device (cached per device).
+int device_sm_count();
+
+// Device address of the status word of the current device (see
+// fv_read_device_status); allocated on first use.
+uint32_t* status_word();
+
+// Host-side launch counter (fv_launch_count).
+void note_launch(uint32_t n = 1);
+
+// Per-stream scratch arena: returns a device buffer of at least `bytes`
+// bytes that stays valid for work enqueued on `stream` until the next call
+// for the same stream with a larger size. Grows with stream-ordered
+// allocation; returns nullptr on failure. A caller-provided arena installed
+// with fv_set_stream_scratch() takes precedence.
+void* scratch_get(cudaStream_t stream, size_t bytes);
+
+// exact fp32 flat scan (flat_fp32.cu)
+int launch_flat_f32(const float* vectors, const uint32_t* vec_ids, uint32_t n, uint32_t dim, const float* queries,
+                    uint32_t nq, uint32_t k, MetricType metric, const uint32_t* mask, GpuSearchResult* out,
+                    uint32_t forced_splits, cudaStream_t stream);
+
+// test fixtures (fixtures.cu)
+int launch_distance_matrix(const float* queries, const float* base, uint32_t nq, uint32_t n, uint32_t dim,
+                           MetricType metric, float* out, cudaStream_t stream);
+int launch_bitonic_test(const float* keys_in, const uint32_t* vals_in, float* keys_out, uint32_t* vals_out,
+                        uint32_t n, cudaStream_t stream);
+
+}  // namespace fv

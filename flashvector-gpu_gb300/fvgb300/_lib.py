@@ -1,0 +1,113 @@
+"""ctypes binding of libfvgb300.so (the C ABI declared in include/fv_bridge.h).
+
+The library is loaded from this package directory (built in-tree by
+flashvector-gpu_gb300/build.py). There is no fallback: if the shared library
+is missing or fails to load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libfvgb300.so"
+
+P = C.c_void_p
+U32 = C.c_uint32
+I32 = C.c_int
+SZ = C.c_size_t
+F32 = C.c_float
+
+
+class GpuSearchResult(C.Structure):
+    _fields_ = [("id", C.c_uint32), ("distance", C.c_float)]
+    _pack_ = 8
+
+
+class IvfPqGpuTables(C.Structure):
+    _fields_ = [("d_centroids", P), ("d_pq_codebooks", P), ("d_pq_codes", P), ("d_ivf_offsets", P),
+                ("d_ivf_vec_ids", P), ("d_vectors", P), ("num_vectors", U32), ("dim", U32), ("nlist", U32),
+                ("m_pq", U32), ("sub_dim", U32)]
+
+
+class IvfSqGpuTables(C.Structure):
+    _fields_ = [("d_centroids", P), ("d_sq_mins", P), ("d_sq_scales", P), ("d_sq_codes", P), ("d_ivf_offsets", P),
+                ("d_ivf_vec_ids", P), ("d_vectors", P), ("num_vectors", U32), ("dim", U32), ("nlist", U32)]
+
+
+class Fp16GpuTables(C.Structure):
+    _fields_ = [("d_vectors_fp16", P), ("d_vec_norms_sq", P), ("d_vectors", P), ("num_vectors", U32), ("dim", U32),
+                ("padded_dim", U32)]
+
+
+class FvFp8GpuTables(C.Structure):
+    _fields_ = [("d_vectors_fp8", P), ("d_scales", P), ("d_vec_norms_sq", P), ("d_vectors", P),
+                ("num_vectors", U32), ("dim", U32), ("padded_dim", U32)]
+
+
+class FvScanOptions(C.Structure):
+    _fields_ = [("overfetch", U32), ("boundary_fp64", U32), ("boundary_eps", F32), ("splits", U32)]
+
+
+# name -> (restype, argtypes); every function declared in include/fv_bridge.h
+SIGNATURES = {
+    "cuda_init_device": (I32, [I32]),
+    "cuda_set_device": (I32, [I32]),
+    "cuda_get_device_count": (I32, [P]),
+    "cuda_get_device_memory": (I32, [P, P]),
+    "cuda_device_synchronize": (I32, []),
+    "cuda_malloc_device": (I32, [P, SZ]),
+    "cuda_free_device": (I32, [P]),
+    "cuda_malloc_host": (I32, [P, SZ]),
+    "cuda_free_host": (I32, [P]),
+    "cuda_memcpy_h2d_async": (I32, [P, P, SZ, P]),
+    "cuda_memcpy_d2h_async": (I32, [P, P, SZ, P]),
+    "cuda_memset_device_async": (I32, [P, I32, SZ, P]),
+    "cuda_host_get_device_pointer": (I32, [P, P]),
+    "cuda_create_stream": (I32, [P]),
+    "cuda_destroy_stream": (I32, [P]),
+    "cuda_sync_stream": (I32, [P]),
+    "cuda_flat_scan_batch": (I32, [P, P, U32, U32, P, U32, U32, I32, P, P, P]),
+    "cuda_compute_distances_warp": (I32, [P, P, U32, U32, U32, I32, P, P]),
+    "cuda_bitonic_sort_test": (I32, [P, P, P, P, U32, P]),
+    "fv_version": (C.c_char_p, []),
+    "fv_read_device_status": (I32, [P]),
+    "fv_launch_count": (C.c_uint64, []),
+    "fv_set_stream_scratch": (I32, [P, P, SZ]),
+    "fv_release_stream_scratch": (I32, [P]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with flashvector-gpu_gb300/build.py "
+                               "(there is no CPU fallback)")
+        handle = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = handle
+    return _lib
+
+
+class FvError(RuntimeError):
+    def __init__(self, fn: str, code: int):
+        super().__init__(f"{fn} failed with code {code}")
+        self.code = code
+
+
+def check(fn: str, code: int) -> None:
+    if code != 0:
+        raise FvError(fn, code)
+
+
+def call(name: str, *args) -> int:
+    """Calls `name` and raises FvError on a non-zero return."""
+    code = getattr(lib(), name)(*args)
+    check(name, code)
+    return code

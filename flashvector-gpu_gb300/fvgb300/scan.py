@@ -1,0 +1,79 @@
+"""Thin torch-facing wrappers over the C-ABI search entry points.
+
+Each wrapper takes CUDA tensors, calls the exported C function with their
+device pointers on the current torch stream, and returns the (Q, k)
+results as a structured pair of tensors (ids uint32-as-int32 view, float32
+distances). These are the calls the parity tests and the benchmark make;
+they add no computation of their own.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _lib
+from ._lib import call
+
+METRIC = {"l2": 0, "cosine": 1, "ip": 2}
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _stream(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _metric(m):
+    return METRIC[m] if isinstance(m, str) else int(m)
+
+
+def split_results(res: torch.Tensor):
+    """(Q, k, 2) int32 storage of GpuSearchResult -> (ids int64, distances f32)."""
+    ids = res[..., 0].to(torch.int64) & 0xFFFFFFFF
+    dist = res[..., 1].view(torch.float32)
+    return ids, dist
+
+
+def empty_results(nq: int, k: int, device="cuda") -> torch.Tensor:
+    return torch.empty((nq, k, 2), dtype=torch.int32, device=device)
+
+
+def flat_scan(vectors, queries, k, metric="l2", mask=None, vec_ids=None, out=None, stream=None):
+    """cuda_flat_scan_batch: exact fp32 scan + top-k (k clamped to 256)."""
+    n = vectors.shape[0] if vectors is not None else 0
+    dim = queries.shape[1]
+    nq = queries.shape[0]
+    kk = min(k, 256)
+    if out is None:
+        out = empty_results(nq, kk, queries.device)
+    call("cuda_flat_scan_batch", _ptr(vectors) if n else None, _ptr(vec_ids), n, dim, _ptr(queries), nq, k,
+         _metric(metric), _ptr(mask), _ptr(out), _stream(stream))
+    return out
+
+
+def distance_matrix(queries, base, metric="l2", stream=None):
+    out = torch.empty((queries.shape[0], base.shape[0]), dtype=torch.float32, device=queries.device)
+    call("cuda_compute_distances_warp", _ptr(queries), _ptr(base), queries.shape[0], base.shape[0],
+         queries.shape[1], _metric(metric), _ptr(out), _stream(stream))
+    return out
+
+
+def bitonic_sort(keys, vals, stream=None):
+    ko = torch.empty_like(keys)
+    vo = torch.empty_like(vals)
+    call("cuda_bitonic_sort_test", _ptr(keys), _ptr(vals), _ptr(ko), _ptr(vo), keys.shape[0], _stream(stream))
+    return ko, vo
+
+
+def device_status() -> int:
+    v = C.c_uint32(0)
+    call("fv_read_device_status", C.byref(v))
+    return v.value
+
+
+def launch_count() -> int:
+    return int(_lib.lib().fv_launch_count())

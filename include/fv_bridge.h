@@ -1,0 +1,101 @@
+/*
+ * fv_bridge.h -- C ABI of libfvgb300 (sm_103a).
+ *
+ * The `cuda_*` entry points are drop-ins for the functions of the same
+ * name in the reference's kernels/include/cuda_bridge.h: same name, same
+ * argument order and meaning, same return convention, so the extern block
+ * of crates/engine/src/ffi.rs:234-455 binds them unchanged.
+ *
+ * Return convention (reference: sparse_hybrid.cu:517-524,
+ * ivf_pq_lookup.cu:462-472): 0 on success; -1 when a required pointer is
+ * null; otherwise the cudaError_t of the failing CUDA call. Empty work
+ * (zero queries or top_k == 0) is a successful no-op. All launches are
+ * asynchronous on `stream` (a cudaStream_t passed as void*, NULL = legacy
+ * default stream); the caller synchronises.
+ *
+ * `fv_*` entry points are extensions with no reference counterpart.
+ */
+#ifndef FV_BRIDGE_H
+#define FV_BRIDGE_H
+
+#include "fv_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Additional return codes of the fv extensions (and of the drop-ins where
+ * the reference would have silently failed). */
+#define FV_OK 0
+#define FV_ERR_NULL (-1)
+#define FV_ERR_ARG (-2)        /* argument outside the supported range        */
+#define FV_ERR_TIMEOUT (-3)    /* a bounded device wait gave up               */
+#define FV_ERR_NOMEM (-4)      /* scratch admission refused                   */
+#define FV_ERR_ARCH (-5)       /* device is not sm_103 / sm_100 class         */
+
+/* ---- device, memory and stream plumbing -------------------------------
+ * Replace cuda_bridge.h:11-31 (hnsw_traverse.cu:525-637). */
+int cuda_init_device(int device_id);
+int cuda_set_device(int device_id);
+int cuda_get_device_count(int* count);
+int cuda_get_device_memory(size_t* free_bytes, size_t* total_bytes);
+int cuda_device_synchronize(void);
+int cuda_malloc_device(void** ptr, size_t bytes);
+int cuda_free_device(void* ptr);
+int cuda_malloc_host(void** ptr, size_t bytes);
+int cuda_free_host(void* ptr);
+int cuda_memcpy_h2d_async(void* dst, const void* src, size_t bytes, void* stream);
+int cuda_memcpy_d2h_async(void* dst, const void* src, size_t bytes, void* stream);
+int cuda_memset_device_async(void* dst, int value, size_t bytes, void* stream);
+int cuda_host_get_device_pointer(void** dev_ptr, void* host_ptr);
+int cuda_create_stream(void** stream);
+int cuda_destroy_stream(void* stream);
+int cuda_sync_stream(void* stream);
+
+/* ---- exact flat scan ---------------------------------------------------
+ * Replaces cuda_bridge.h:150-162 (sparse_hybrid.cu:504-525).
+ * Per query: the top_k (clamped to 256) rows of d_vectors by distance,
+ * ascending; ties go to the lower slot index. d_vec_ids (optional) maps
+ * slot -> reported id; d_valid_mask (optional) is a packed LSB-first bit
+ * per slot. num_vectors == 0 fills d_out_results with 0xFF bytes. */
+int cuda_flat_scan_batch(const float* d_vectors, const uint32_t* d_vec_ids,
+                         uint32_t num_vectors, uint32_t dim,
+                         const float* d_queries, uint32_t num_queries,
+                         uint32_t top_k, MetricType metric,
+                         const uint32_t* d_valid_mask,
+                         GpuSearchResult* d_out_results, void* stream);
+
+/* ---- test fixtures -----------------------------------------------------
+ * Replace cuda_bridge.h:195-213 (hnsw_traverse.cu:387-437, 694-735). */
+int cuda_compute_distances_warp(const float* d_queries, const float* d_dataset,
+                                uint32_t num_queries, uint32_t num_vectors,
+                                uint32_t dim, MetricType metric,
+                                float* d_out_distances, void* stream);
+int cuda_bitonic_sort_test(const float* d_keys_in, const uint32_t* d_vals_in,
+                           float* d_keys_out, uint32_t* d_vals_out, uint32_t n,
+                           void* stream);
+
+/* ---- extensions --------------------------------------------------------*/
+/* Library version string, e.g. "fvgb300 0.1 sm_103a". */
+const char* fv_version(void);
+/* Reads and clears the device status word that bounded waits and bounds
+ * checks of the kernels set (0 = clean). Synchronises the device. */
+int fv_read_device_status(uint32_t* status);
+/* Number of this library's kernel launches issued since load (all
+ * devices, all streams); used to count launches inside timed regions. */
+uint64_t fv_launch_count(void);
+/* Installs a caller-owned device buffer as the scratch arena of `stream`
+ * (kernels that need scratch then never allocate on that stream; a call
+ * needing more than `bytes` fails with cudaErrorMemoryAllocation).
+ * d_ptr == NULL removes the caller buffer and returns to library-managed
+ * stream-ordered allocation. Replaces the reference's per-call
+ * cudaMallocAsync in ivf_pq_lookup.cu:397-401. */
+int fv_set_stream_scratch(void* stream, void* d_ptr, size_t bytes);
+/* Frees the library-managed scratch arena of `stream`. */
+int fv_release_stream_scratch(void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FV_BRIDGE_H */

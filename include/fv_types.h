@@ -1,0 +1,114 @@
+/*
+ * fv_types.h -- plain-old-data types that cross the C ABI of libfvgb300.
+ *
+ * Layout contract: every struct below that has a counterpart in the
+ * reference (FlashVector-GPU kernels/include/types.h) keeps that
+ * counterpart's field order, field types and alignment, so that a caller
+ * built against the reference header (the Rust `#[repr(C)]` mirrors in
+ * crates/engine/src/ffi.rs:20-232) can pass its structs unchanged.
+ * New structs (FP8 tables, list-major IVF layouts, status words) carry an
+ * `Fv` prefix and have no reference counterpart.
+ */
+#ifndef FV_TYPES_H
+#define FV_TYPES_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define FV_ALIGN8 alignas(8)
+extern "C" {
+#else
+#define FV_ALIGN8 _Alignas(8)
+#endif
+
+/* Distance metric. Values as kernels/include/types.h:15-19 (L2=0, Cosine=1,
+ * InnerProduct=2). L2 is the squared Euclidean distance, inner product is
+ * reported as -dot so that smaller is always better, cosine as 1-cos. */
+typedef enum {
+    METRIC_L2 = 0,
+    METRIC_COSINE = 1,
+    METRIC_INNER_PRODUCT = 2
+} MetricType;
+
+/* One (id, distance) hit; 8 bytes, 8-byte aligned (types.h:39-42).
+ * Unfilled slots are {0xFFFFFFFF, 1e30f}. */
+typedef struct FV_ALIGN8 {
+    uint32_t id;
+    float distance;
+} GpuSearchResult;
+
+/* IVF-PQ tables, field order as types.h:85-97. All pointers are device (or
+ * mapped-host for d_vectors) pointers owned by the caller. d_pq_codes is
+ * indexed by vector id: row v holds the m_pq one-byte codes of vector v. */
+typedef struct {
+    const float* d_centroids;      /* [nlist * dim] coarse centroids            */
+    const float* d_pq_codebooks;   /* [m_pq * 256 * sub_dim] sub-space codewords */
+    const uint8_t* d_pq_codes;     /* [num_vectors * m_pq]                       */
+    const uint32_t* d_ivf_offsets; /* [nlist + 1] posting-list prefix offsets    */
+    const uint32_t* d_ivf_vec_ids; /* [num_vectors] vector ids in list order     */
+    const float* d_vectors;        /* [num_vectors * dim] fp32 rows for rerank   */
+    uint32_t num_vectors;
+    uint32_t dim;
+    uint32_t nlist;
+    uint32_t m_pq;
+    uint32_t sub_dim;
+} IvfPqGpuTables;
+
+/* IVF-SQ8 tables, field order as types.h:100-111. */
+typedef struct {
+    const float* d_centroids;      /* [nlist * dim]                              */
+    const float* d_sq_mins;        /* [dim] per-dimension residual minimum       */
+    const float* d_sq_scales;      /* [dim] per-dimension step (range / 255)     */
+    const uint8_t* d_sq_codes;     /* [num_vectors * dim] indexed by vector id   */
+    const uint32_t* d_ivf_offsets; /* [nlist + 1]                                */
+    const uint32_t* d_ivf_vec_ids; /* [num_vectors]                              */
+    const float* d_vectors;        /* [num_vectors * dim] fp32 rows for rerank   */
+    uint32_t num_vectors;
+    uint32_t dim;
+    uint32_t nlist;
+} IvfSqGpuTables;
+
+/* FP16 flat tables, field order as types.h:131-138. padded_dim is a
+ * multiple of 16; columns dim..padded_dim-1 of each fp16 row are zero.
+ * When d_vectors (fp32 copy, row stride dim) is non-null the scan is
+ * followed by an exact fp32 rescore of an over-fetched shortlist. */
+typedef struct {
+    const uint16_t* d_vectors_fp16; /* [num_vectors * padded_dim] IEEE binary16 */
+    const float* d_vec_norms_sq;    /* [num_vectors] ||x||^2 of the fp32 row     */
+    const float* d_vectors;         /* optional [num_vectors * dim] fp32 rows    */
+    uint32_t num_vectors;
+    uint32_t dim;
+    uint32_t padded_dim;
+} Fp16GpuTables;
+
+/* FP8 (E4M3) flat tables; no reference counterpart. Row v of d_vectors_fp8
+ * holds round_e4m3(x_v[d] / d_scales[v]) for d < dim and zero padding up to
+ * padded_dim (a multiple of 32). d_scales[v] = max|x_v| / 448 (1 for a zero
+ * row). d_vec_norms_sq holds ||x_v||^2 of the fp32 row. */
+typedef struct {
+    const uint8_t* d_vectors_fp8;   /* [num_vectors * padded_dim] E4M3 bytes     */
+    const float* d_scales;          /* [num_vectors] per-vector dequant scale    */
+    const float* d_vec_norms_sq;    /* [num_vectors] ||x||^2 of the fp32 row     */
+    const float* d_vectors;         /* optional [num_vectors * dim] fp32 rows    */
+    uint32_t num_vectors;
+    uint32_t dim;
+    uint32_t padded_dim;
+} FvFp8GpuTables;
+
+/* Tuning knobs of the reduced-precision flat scans; no reference
+ * counterpart. Zero in any field selects the default. */
+typedef struct {
+    uint32_t overfetch;      /* shortlist = overfetch * top_k (default 4)      */
+    uint32_t boundary_fp64;  /* 1 = fp64 re-rank of ties at the k-th boundary  */
+    float boundary_eps;      /* relative band around the k-th distance (fp64)  */
+    uint32_t splits;         /* base-range splits per query block (0 = auto)   */
+} FvScanOptions;
+
+#undef FV_ALIGN8
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FV_TYPES_H */

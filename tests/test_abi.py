@@ -1,0 +1,53 @@
+"""The C-ABI library loads and exports every function include/*.h declares
+(CPU only: no compute calls)."""
+from __future__ import annotations
+
+import ctypes
+import re
+
+from conftest import ROOT
+
+DECL = re.compile(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\*?\s*\b((?:cuda|fv)_[A-Za-z0-9_]+)\s*\(", re.M)
+
+
+def declared_functions():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names.update(DECL.findall(text))
+    return sorted(names)
+
+
+def test_headers_declare_the_drop_in_entry_points():
+    names = declared_functions()
+    for required in ("cuda_flat_scan_batch", "cuda_init_device", "cuda_sync_stream"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    lib = ctypes.CDLL(str(built_lib))
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, f"declared but not exported: {missing}"
+
+
+def test_python_binding_covers_every_declared_symbol(built_lib):
+    from fvgb300 import _lib
+
+    missing = [n for n in declared_functions() if n not in _lib.SIGNATURES]
+    assert not missing, f"no ctypes signature for: {missing}"
+    lib = _lib.lib()
+    assert lib.fv_version().startswith(b"fvgb300")
+
+
+def test_struct_layouts_match_reference():
+    """GpuSearchResult is 8 bytes, align 8 (types.h:39-42); table structs keep
+    the reference field order (types.h:85-111, 131-138)."""
+    from fvgb300 import _lib
+
+    assert ctypes.sizeof(_lib.GpuSearchResult) == 8
+    assert ctypes.alignment(_lib.GpuSearchResult) in (4, 8)
+    assert ctypes.sizeof(_lib.IvfPqGpuTables) == 6 * 8 + 5 * 4 + 4  # padded to 8
+    assert ctypes.sizeof(_lib.IvfSqGpuTables) == 7 * 8 + 3 * 4 + 4
+    assert ctypes.sizeof(_lib.Fp16GpuTables) == 3 * 8 + 3 * 4 + 4
+    assert [f[0] for f in _lib.IvfPqGpuTables._fields_][:6] == [
+        "d_centroids", "d_pq_codebooks", "d_pq_codes", "d_ivf_offsets", "d_ivf_vec_ids", "d_vectors"]
