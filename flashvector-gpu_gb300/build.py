@@ -78,7 +78,7 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
         with ThreadPoolExecutor(max_workers=jobs or min(len(cmds), os.cpu_count() or 4)) as ex:
             list(ex.map(run, cmds))
     if force or cmds or not LIB.exists():
-        link = [nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcuda", "-Xcompiler", "-fopenmp"]
+        link = [nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-Xcompiler", "-fopenmp"]
         run(link)
     return LIB
 

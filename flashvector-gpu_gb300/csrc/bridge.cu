@@ -180,6 +180,72 @@ int cuda_flat_scan_batch(const float* d_vectors, const uint32_t* d_vec_ids, uint
                              d_valid_mask, d_out_results, 0, s);
 }
 
+// -------------------------------------------------- tensor-core scans
+namespace {
+int tc_common(const fv::TcTables& t, const float* q, uint32_t nq, uint32_t top_k, MetricType metric,
+              const uint32_t* mask, const FvScanOptions* opt, GpuSearchResult* out, void* stream) {
+  if (nq == 0 || top_k == 0) return 0;
+  if (top_k > (uint32_t)fv::kMaxTopK) top_k = fv::kMaxTopK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (t.n == 0) {
+    // no rows: every slot is the {0xFFFFFFFF, 1e30} sentinel
+    return fv::launch_fill_sentinel(out, (size_t)nq * top_k, s);
+  }
+  if (!t.base) return FV_ERR_NULL;
+  if (t.dim == 0 || t.padded_dim < t.dim || t.padded_dim % 16 != 0) return FV_ERR_ARG;
+  if ((uintptr_t)t.base % 16 != 0) return FV_ERR_ARG;
+  if (metric != METRIC_INNER_PRODUCT && !t.norms) return FV_ERR_NULL;
+  if (t.fp8 && !t.scales) return FV_ERR_NULL;
+  FvScanOptions o{};
+  if (opt) o = *opt;
+  else o.boundary_fp64 = 1;
+  return fv::launch_tc_scan(t, q, nq, top_k, metric, mask, out, o, s);
+}
+}  // namespace
+
+int cuda_fp16_tc_search_batch(const Fp16GpuTables* tables, const float* d_queries, uint32_t num_queries,
+                              uint32_t top_k, MetricType metric, const uint32_t* d_valid_mask,
+                              GpuSearchResult* d_out_results, void* stream) {
+  if (!tables || !d_queries || !d_out_results) return FV_ERR_NULL;
+  fv::TcTables t{false, tables->d_vectors_fp16, tables->d_vec_norms_sq, nullptr, tables->d_vectors,
+                 tables->num_vectors, tables->dim, tables->padded_dim};
+  return tc_common(t, d_queries, num_queries, top_k, metric, d_valid_mask, nullptr, d_out_results, stream);
+}
+
+int fv_fp16_search_batch_ex(const Fp16GpuTables* tables, const float* d_queries, uint32_t num_queries,
+                            uint32_t top_k, MetricType metric, const uint32_t* d_valid_mask,
+                            const FvScanOptions* options, GpuSearchResult* d_out_results, void* stream) {
+  if (!tables || !d_queries || !d_out_results) return FV_ERR_NULL;
+  fv::TcTables t{false, tables->d_vectors_fp16, tables->d_vec_norms_sq, nullptr, tables->d_vectors,
+                 tables->num_vectors, tables->dim, tables->padded_dim};
+  return tc_common(t, d_queries, num_queries, top_k, metric, d_valid_mask, options, d_out_results, stream);
+}
+
+int fv_fp8_search_batch(const FvFp8GpuTables* tables, const float* d_queries, uint32_t num_queries, uint32_t top_k,
+                        MetricType metric, const uint32_t* d_valid_mask, const FvScanOptions* options,
+                        GpuSearchResult* d_out_results, void* stream) {
+  if (!tables || !d_queries || !d_out_results) return FV_ERR_NULL;
+  fv::TcTables t{true, tables->d_vectors_fp8, tables->d_vec_norms_sq, tables->d_scales, tables->d_vectors,
+                 tables->num_vectors, tables->dim, tables->padded_dim};
+  return tc_common(t, d_queries, num_queries, top_k, metric, d_valid_mask, options, d_out_results, stream);
+}
+
+int fv_encode_fp16_padded(const float* d_vectors, uint32_t num_vectors, uint32_t dim, uint32_t padded_dim,
+                          uint16_t* d_out_fp16, float* d_out_norms_sq, void* stream) {
+  if (num_vectors && (!d_vectors || !d_out_fp16)) return FV_ERR_NULL;
+  if (padded_dim < dim || padded_dim % 16) return FV_ERR_ARG;
+  return fv::launch_encode_fp16(d_vectors, num_vectors, dim, padded_dim, d_out_fp16, d_out_norms_sq,
+                                (cudaStream_t)stream);
+}
+
+int fv_encode_fp8(const float* d_vectors, uint32_t num_vectors, uint32_t dim, uint32_t padded_dim,
+                  uint8_t* d_out_fp8, float* d_out_scales, float* d_out_norms_sq, void* stream) {
+  if (num_vectors && (!d_vectors || !d_out_fp8 || !d_out_scales)) return FV_ERR_NULL;
+  if (padded_dim < dim || padded_dim % 16) return FV_ERR_ARG;
+  return fv::launch_encode_fp8(d_vectors, num_vectors, dim, padded_dim, d_out_fp8, d_out_scales, d_out_norms_sq,
+                               (cudaStream_t)stream);
+}
+
 // ------------------------------------------------------------- fixtures
 int cuda_compute_distances_warp(const float* d_queries, const float* d_dataset, uint32_t num_queries,
                                 uint32_t num_vectors, uint32_t dim, MetricType metric, float* d_out_distances,

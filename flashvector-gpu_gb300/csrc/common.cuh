@@ -68,6 +68,17 @@ __host__ __device__ __forceinline__ uint32_t key_slot(uint64_t k) { return (uint
 // (admissible = distance < 1e30, which also rejects NaN).
 constexpr uint64_t kSentinelKey = 0xFFFFFFFFFFFFFFFFull;
 
+__host__ __device__ __forceinline__ uint32_t next_pow2_dev(uint32_t v) {
+  if (v <= 1) return 1;
+  --v;
+  v |= v >> 1;
+  v |= v >> 2;
+  v |= v >> 4;
+  v |= v >> 8;
+  v |= v >> 16;
+  return v + 1;
+}
+
 // Packed LSB-first validity bit of slot `i` (nullptr = everything valid).
 // Same bit convention as the reference (distance_metrics.cuh:17-20,
 // filter.rs:364-371).

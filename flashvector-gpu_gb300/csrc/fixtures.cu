@@ -39,7 +39,20 @@ __global__ void __launch_bounds__(256) bitonic_test_kernel(const float* __restri
   }
 }
 
+__global__ void fill_sentinel_kernel(GpuSearchResult* out, size_t count) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = GpuSearchResult{kInvalidId, kSentinelDist};
+}
+
 }  // namespace
+
+int launch_fill_sentinel(GpuSearchResult* out, size_t count, cudaStream_t stream) {
+  if (count == 0) return 0;
+  const size_t blocks = std::min<size_t>((count + 255) / 256, 4096);
+  fill_sentinel_kernel<<<(unsigned)blocks, 256, 0, stream>>>(out, count);
+  note_launch();
+  return (int)cudaGetLastError();
+}
 
 int launch_distance_matrix(const float* queries, const float* base, uint32_t nq, uint32_t n, uint32_t dim,
                            MetricType metric, float* out, cudaStream_t stream) {

@@ -39,10 +39,31 @@ void note_launch(uint32_t n = 1);
 // with fv_set_stream_scratch() takes precedence.
 void* scratch_get(cudaStream_t stream, size_t bytes);
 
+// Writes `count` {0xFFFFFFFF, 1e30} results (fixtures.cu).
+int launch_fill_sentinel(GpuSearchResult* out, size_t count, cudaStream_t stream);
+
 // exact fp32 flat scan (flat_fp32.cu)
 int launch_flat_f32(const float* vectors, const uint32_t* vec_ids, uint32_t n, uint32_t dim, const float* queries,
                     uint32_t nq, uint32_t k, MetricType metric, const uint32_t* mask, GpuSearchResult* out,
                     uint32_t forced_splits, cudaStream_t stream);
+
+// tensor-core flat scans (tc_scan.cu)
+struct TcTables {
+  bool fp8;              // false: fp16 rows, true: e4m3 rows with per-row scales
+  const void* base;      // [n][padded_dim] fp16 or e4m3
+  const float* norms;    // [n] ||x||^2 (may be null for inner product)
+  const float* scales;   // [n] per-row dequantisation scale (fp8 only)
+  const float* vectors;  // [n][dim] fp32 rows for the rescore (optional)
+  uint32_t n, dim, padded_dim;
+};
+int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
+                   const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream);
+
+// reduced-precision table encoders (encode.cu)
+int launch_encode_fp16(const float* x, uint32_t n, uint32_t dim, uint32_t pd, uint16_t* out, float* norms,
+                       cudaStream_t stream);
+int launch_encode_fp8(const float* x, uint32_t n, uint32_t dim, uint32_t pd, uint8_t* out, float* scales,
+                      float* norms, cudaStream_t stream);
 
 // test fixtures (fixtures.cu)
 int launch_distance_matrix(const float* queries, const float* base, uint32_t nq, uint32_t n, uint32_t dim,

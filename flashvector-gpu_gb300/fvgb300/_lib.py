@@ -69,6 +69,11 @@ SIGNATURES = {
     "cuda_flat_scan_batch": (I32, [P, P, U32, U32, P, U32, U32, I32, P, P, P]),
     "cuda_compute_distances_warp": (I32, [P, P, U32, U32, U32, I32, P, P]),
     "cuda_bitonic_sort_test": (I32, [P, P, P, P, U32, P]),
+    "cuda_fp16_tc_search_batch": (I32, [P, P, U32, U32, I32, P, P, P]),
+    "fv_fp16_search_batch_ex": (I32, [P, P, U32, U32, I32, P, P, P, P]),
+    "fv_fp8_search_batch": (I32, [P, P, U32, U32, I32, P, P, P, P]),
+    "fv_encode_fp16_padded": (I32, [P, U32, U32, U32, P, P, P]),
+    "fv_encode_fp8": (I32, [P, U32, U32, U32, P, P, P, P]),
     "fv_version": (C.c_char_p, []),
     "fv_read_device_status": (I32, [P]),
     "fv_launch_count": (C.c_uint64, []),

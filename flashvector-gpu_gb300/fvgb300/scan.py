@@ -77,3 +77,81 @@ def device_status() -> int:
 
 def launch_count() -> int:
     return int(_lib.lib().fv_launch_count())
+
+
+# ----------------------------------------------------------- reduced precision
+def padded_dim(dim: int, multiple: int = 16) -> int:
+    return (dim + multiple - 1) // multiple * multiple
+
+
+def encode_fp16(vectors, pd=None, stream=None):
+    """fv_encode_fp16_padded: fp16 rows (reference rounding) + ||x||^2."""
+    n, dim = vectors.shape
+    pd = pd or padded_dim(dim)
+    out = torch.empty((n, pd), dtype=torch.int16, device=vectors.device)
+    norms = torch.empty((n,), dtype=torch.float32, device=vectors.device)
+    call("fv_encode_fp16_padded", _ptr(vectors), n, dim, pd, _ptr(out), _ptr(norms), _stream(stream))
+    return out, norms
+
+
+def encode_fp8(vectors, pd=None, stream=None):
+    """fv_encode_fp8: e4m3 rows with per-row scales + compensated ||x||^2."""
+    n, dim = vectors.shape
+    pd = pd or padded_dim(dim)
+    out = torch.empty((n, pd), dtype=torch.uint8, device=vectors.device)
+    scales = torch.empty((n,), dtype=torch.float32, device=vectors.device)
+    norms = torch.empty((n,), dtype=torch.float32, device=vectors.device)
+    call("fv_encode_fp8", _ptr(vectors), n, dim, pd, _ptr(out), _ptr(scales), _ptr(norms), _stream(stream))
+    return out, scales, norms
+
+
+class Fp16Table:
+    """Device-resident fp16 flat table (+ optional fp32 copy for rescoring)."""
+
+    def __init__(self, vectors, keep_fp32=True, stream=None):
+        self.n, self.dim = vectors.shape
+        self.pd = padded_dim(self.dim)
+        self.fp16, self.norms = encode_fp16(vectors, self.pd, stream)
+        self.fp32 = vectors if keep_fp32 else None
+        self.struct = _lib.Fp16GpuTables(self.fp16.data_ptr(), self.norms.data_ptr(),
+                                         self.fp32.data_ptr() if self.fp32 is not None else None,
+                                         self.n, self.dim, self.pd)
+
+
+class Fp8Table:
+    def __init__(self, vectors, keep_fp32=True, stream=None):
+        self.n, self.dim = vectors.shape
+        self.pd = padded_dim(self.dim)
+        self.fp8, self.scales, self.norms = encode_fp8(vectors, self.pd, stream)
+        self.fp32 = vectors if keep_fp32 else None
+        self.struct = _lib.FvFp8GpuTables(self.fp8.data_ptr(), self.scales.data_ptr(), self.norms.data_ptr(),
+                                          self.fp32.data_ptr() if self.fp32 is not None else None,
+                                          self.n, self.dim, self.pd)
+
+
+def options(overfetch=0, boundary_fp64=1, boundary_eps=0.0, splits=0):
+    return _lib.FvScanOptions(overfetch, boundary_fp64, boundary_eps, splits)
+
+
+def fp16_search(table, queries, k, metric="ip", mask=None, opts=None, out=None, stream=None, dropin=False):
+    nq = queries.shape[0]
+    if out is None:
+        out = empty_results(nq, min(k, 256), queries.device)
+    if dropin:
+        call("cuda_fp16_tc_search_batch", C.byref(table.struct), _ptr(queries), nq, k, _metric(metric), _ptr(mask),
+             _ptr(out), _stream(stream))
+    else:
+        o = opts if opts is not None else options()
+        call("fv_fp16_search_batch_ex", C.byref(table.struct), _ptr(queries), nq, k, _metric(metric), _ptr(mask),
+             C.byref(o), _ptr(out), _stream(stream))
+    return out
+
+
+def fp8_search(table, queries, k, metric="l2", mask=None, opts=None, out=None, stream=None):
+    nq = queries.shape[0]
+    if out is None:
+        out = empty_results(nq, min(k, 256), queries.device)
+    o = opts if opts is not None else options()
+    call("fv_fp8_search_batch", C.byref(table.struct), _ptr(queries), nq, k, _metric(metric), _ptr(mask),
+         C.byref(o), _ptr(out), _stream(stream))
+    return out

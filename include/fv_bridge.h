@@ -65,6 +65,47 @@ int cuda_flat_scan_batch(const float* d_vectors, const uint32_t* d_vec_ids,
                          const uint32_t* d_valid_mask,
                          GpuSearchResult* d_out_results, void* stream);
 
+/* ---- tensor-core flat scans --------------------------------------------
+ * Replaces cuda_bridge.h:138-147 (ivf_quant_lookup.cu:1106-1123). Per
+ * query the top_k (<= 256) rows by the fp16 tensor-core distance
+ * (IP: -dot, L2: max(0, |q|^2 + |x|^2 - 2 dot), cosine: 1 - dot /
+ * (sqrt(|q|^2 |x|^2) + 1e-8)), ties to the lower slot. When
+ * tables->d_vectors is non-null (the reference documents it as the fp32
+ * copy for exact rerank, types.h:134) a shortlist of 4 * top_k is rescored
+ * in fp32 and the band around the k-th distance re-ranked in fp64; the
+ * reported distances are then the fp32 (fp64 in the band) values. Ids are
+ * slot indices; d_valid_mask filters slots. */
+int cuda_fp16_tc_search_batch(const Fp16GpuTables* tables, const float* d_queries,
+                              uint32_t num_queries, uint32_t top_k, MetricType metric,
+                              const uint32_t* d_valid_mask, GpuSearchResult* d_out_results,
+                              void* stream);
+
+/* Same as cuda_fp16_tc_search_batch with explicit options (over-fetch,
+ * fp64 boundary band, base-range splits); options may be NULL. */
+int fv_fp16_search_batch_ex(const Fp16GpuTables* tables, const float* d_queries,
+                            uint32_t num_queries, uint32_t top_k, MetricType metric,
+                            const uint32_t* d_valid_mask, const FvScanOptions* options,
+                            GpuSearchResult* d_out_results, void* stream);
+
+/* FP8 (E4M3, per-row scale) tensor-core flat scan; same contract as the
+ * fp16 scan, the per-query scale is amax(|q|)/448. No reference
+ * counterpart (the reference has no fp8 path). */
+int fv_fp8_search_batch(const FvFp8GpuTables* tables, const float* d_queries,
+                        uint32_t num_queries, uint32_t top_k, MetricType metric,
+                        const uint32_t* d_valid_mask, const FvScanOptions* options,
+                        GpuSearchResult* d_out_results, void* stream);
+
+/* Device-side table encoders. fv_encode_fp16_padded restates the
+ * reference's host encoder encode_fp16_padded (quant.rs:306-327, rounding
+ * of quant.rs:239-274). fv_encode_fp8 has no counterpart. padded_dim must
+ * be a multiple of 16 and >= dim. */
+int fv_encode_fp16_padded(const float* d_vectors, uint32_t num_vectors, uint32_t dim,
+                          uint32_t padded_dim, uint16_t* d_out_fp16, float* d_out_norms_sq,
+                          void* stream);
+int fv_encode_fp8(const float* d_vectors, uint32_t num_vectors, uint32_t dim,
+                  uint32_t padded_dim, uint8_t* d_out_fp8, float* d_out_scales,
+                  float* d_out_norms_sq, void* stream);
+
 /* ---- test fixtures -----------------------------------------------------
  * Replace cuda_bridge.h:195-213 (hnsw_traverse.cu:387-437, 694-735). */
 int cuda_compute_distances_warp(const float* d_queries, const float* d_dataset,

@@ -1,0 +1,256 @@
+"""Tensor-core flat scans (fp16 / fp8) through the C ABI.
+
+Reduced-precision forms are judged the way the scan path's contract states
+them: the candidate ranking must agree with an fp64 evaluation of the same
+quantised products, the fp32-rescored results must reach recall@k >= 0.99
+against the fp64 oracle, and every reported distance must be the fp32
+rescore value (bit-identical to the oracle's restatement of the reference's
+warp-order distance) or, inside the k-th boundary band, the fp64 value
+rounded to fp32."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def unit_mixture(n, dim, comps, sigma, seed):
+    rng = np.random.default_rng(seed)
+    c = rng.standard_normal((comps, dim)).astype(np.float32)
+    c /= np.linalg.norm(c, axis=1, keepdims=True)
+    x = c[rng.integers(0, comps, n)] + np.float32(sigma) * rng.standard_normal((n, dim), dtype=np.float32)
+    x /= np.linalg.norm(x, axis=1, keepdims=True)
+    return x.astype(np.float32)
+
+
+def res_np(res):
+    r = res.cpu().numpy()
+    return r[..., 0].view(np.uint32), r[..., 1].view(np.float32)
+
+
+def check_rescored(oracle_mod, base, queries, ids, dist, metric, k):
+    """recall vs fp64 and exactness of every reported distance."""
+    truth, _ = oracle_mod.bruteforce_f64(base, queries, k, metric)
+    rec = oracle_mod.recall(ids, truth)
+    bad = 0
+    for qi in range(queries.shape[0]):
+        for r in range(k):
+            i = ids[qi, r]
+            if i == 0xFFFFFFFF:
+                continue
+            w = np.float32(oracle_mod.warp_distance(queries[qi], base[i], metric))
+            if dist[qi, r] != w:
+                x = base[i].astype(np.float64)
+                q = queries[qi].astype(np.float64)
+                if metric == "l2":
+                    d64 = np.sum((q - x) ** 2)
+                elif metric == "ip":
+                    d64 = -np.dot(q, x)
+                else:
+                    d64 = 1 - np.dot(q, x) / (np.linalg.norm(q) * np.linalg.norm(x))
+                if abs(np.float32(d64) - dist[qi, r]) > 1e-6 * max(1.0, abs(d64)):
+                    bad += 1
+    assert bad == 0, f"{bad} reported distances are neither the fp32 rescore nor the fp64 band value"
+    # sorted ascending per query
+    assert np.all(dist[:, :-1] <= dist[:, 1:])
+    return rec
+
+
+def test_encode_fp16_matches_oracle(cuda, oracle_mod):
+    from fvgb300 import scan
+
+    torch = cuda
+    rng = np.random.default_rng(0)
+    x = (rng.standard_normal((777, 70)) * np.logspace(-6, 4, 70)).astype(np.float32)
+    x[0, :5] = [1.0 + 2 ** -11, 65519.0, 70000.0, 1e-9, -0.0]
+    codes, norms = scan.encode_fp16(torch.from_numpy(x).cuda())
+    ref_codes, ref_norms = oracle_mod.encode_fp16_padded(x)
+    assert np.array_equal(codes.cpu().numpy().view(np.uint16), ref_codes)
+    assert np.array_equal(norms.cpu().numpy().view(np.uint32), ref_norms.view(np.uint32))
+
+
+def test_encode_fp8(cuda):
+    from fvgb300 import scan
+
+    torch = cuda
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((500, 96)).astype(np.float32)
+    x[3] = 0.0
+    codes, scales, norms = scan.encode_fp8(torch.from_numpy(x).cuda())
+    amax = np.abs(x).max(axis=1)
+    exp_scale = np.where(amax > 0, amax / np.float32(448.0), 1.0).astype(np.float32)
+    assert np.array_equal(scales.cpu().numpy(), exp_scale)
+    ref = (torch.from_numpy(x).cuda() / scales[:, None]).to(torch.float8_e4m3fn).view(torch.uint8)
+    assert torch.equal(codes[:, :96], ref)
+    assert np.allclose(norms.cpu().numpy(), (x.astype(np.float64) ** 2).sum(1), rtol=1e-6)
+
+
+@pytest.mark.parametrize("metric", ["ip", "l2", "cosine"])
+@pytest.mark.parametrize("n,dim,nq,k", [(30000, 768, 200, 10), (5003, 70, 129, 16), (1000, 128, 1, 5),
+                                        (257, 64, 64, 10)])
+def test_fp16_scan_ranking_without_rescore(cuda, metric, n, dim, nq, k):
+    """No fp32 copy: results are the top-k of the fp16 tensor-core distance.
+    Checked against an fp64 evaluation of the same fp16 products."""
+    from fvgb300 import scan
+
+    torch = cuda
+    base = unit_mixture(n, dim, 64, 0.4, n + dim)
+    queries = unit_mixture(nq, dim, 64, 0.4, 7 + nq)
+    bt = torch.from_numpy(base).cuda()
+    table = scan.Fp16Table(bt, keep_fp32=False)
+    res = scan.fp16_search(table, torch.from_numpy(queries).cuda(), k, metric, opts=scan.options(boundary_fp64=0))
+    torch.cuda.synchronize()
+    ids, dist = res_np(res)
+    x16 = table.fp16.cpu().numpy().view(np.float16).astype(np.float64)[:, :dim]
+    q16 = queries.astype(np.float16).astype(np.float64)
+    dots = q16 @ x16.T
+    xn = table.norms.cpu().numpy().astype(np.float64)
+    qn = (queries.astype(np.float64) ** 2).sum(1)
+    if metric == "ip":
+        d64 = -dots
+    elif metric == "l2":
+        d64 = np.maximum(0, qn[:, None] + xn[None, :] - 2 * dots)
+    else:
+        d64 = 1 - dots / (np.sqrt(qn[:, None] * xn[None, :]) + 1e-8)
+    order = np.argsort(d64, axis=1, kind="stable")[:, :k]
+    hit = np.mean([len(set(ids[i]) & set(order[i])) / k for i in range(nq)])
+    assert hit >= 0.995, hit
+    got = np.take_along_axis(d64, ids.astype(np.int64), axis=1)
+    assert np.allclose(dist, got, rtol=2e-5, atol=2e-5)
+    assert np.all(dist[:, :-1] <= dist[:, 1:])
+    assert scan.device_status() == 0
+
+
+@pytest.mark.parametrize("metric", ["ip", "l2"])
+@pytest.mark.parametrize("k", [10, 100])
+def test_fp16_rescored_recall(cuda, oracle_mod, metric, k):
+    from fvgb300 import scan
+
+    torch = cuda
+    base = unit_mixture(40000, 768, 256, 0.3, 11)
+    queries = unit_mixture(64, 768, 256, 0.3, 12)
+    table = scan.Fp16Table(torch.from_numpy(base).cuda())
+    res = scan.fp16_search(table, torch.from_numpy(queries).cuda(), k, metric)
+    torch.cuda.synchronize()
+    ids, dist = res_np(res)
+    rec = check_rescored(oracle_mod, base, queries, ids, dist, metric, k)
+    assert rec >= 0.99, rec
+    assert scan.device_status() == 0
+
+
+def test_fp16_masked_and_dropin(cuda, oracle_mod):
+    """Bernoulli(0.5) slot mask; no masked id comes back; the drop-in entry
+    point gives the same answer as the extension with default options."""
+    from fvgb300 import scan
+    from fvgb300.datasets import bernoulli_mask_words, unpack_words
+
+    torch = cuda
+    base = unit_mixture(20000, 256, 128, 0.3, 21)
+    queries = unit_mixture(100, 256, 128, 0.3, 22)
+    words = bernoulli_mask_words(base.shape[0], 0.5, 1)
+    allowed = unpack_words(words, base.shape[0])
+    table = scan.Fp16Table(torch.from_numpy(base).cuda())
+    m = torch.from_numpy(words.view(np.int32)).cuda()
+    q = torch.from_numpy(queries).cuda()
+    a = scan.fp16_search(table, q, 10, "ip", mask=m)
+    b = scan.fp16_search(table, q, 10, "ip", mask=m, dropin=True)
+    torch.cuda.synchronize()
+    ids, dist = res_np(a)
+    assert torch.equal(a, b)
+    assert np.all(allowed[ids])
+    truth, _ = oracle_mod.bruteforce_f64(base, queries, 10, "ip", mask=words)
+    assert oracle_mod.recall(ids, truth) >= 0.99
+
+
+@pytest.mark.parametrize("splits", [1, 2, 7, 0])
+def test_fp16_split_invariance(cuda, splits):
+    """The answer does not depend on how the base range is split over CTAs."""
+    from fvgb300 import scan
+
+    torch = cuda
+    base = unit_mixture(9000, 128, 32, 0.3, 31)
+    queries = unit_mixture(300, 128, 32, 0.3, 32)
+    table = scan.Fp16Table(torch.from_numpy(base).cuda())
+    q = torch.from_numpy(queries).cuda()
+    ref = scan.fp16_search(table, q, 16, "l2", opts=scan.options(splits=1))
+    got = scan.fp16_search(table, q, 16, "l2", opts=scan.options(splits=splits))
+    torch.cuda.synchronize()
+    assert torch.equal(ref, got)
+
+
+def gen_clustered(n, dim, clusters, seed):
+    rng = np.random.default_rng(seed)
+    centers = rng.uniform(-1, 1, size=(clusters, dim)).astype(np.float32)
+    return (centers[np.arange(n) % clusters] + np.float32(0.18) * rng.standard_normal((n, dim))).astype(np.float32)
+
+
+@pytest.mark.parametrize("metric", ["l2", "cosine"])
+def test_fp16_self_query(cuda, metric):
+    """e2e_search_test.rs:291-319: gen_clustered(512, 64, 8, 303), the first
+    4 rows as queries; the nearest neighbour of row 0 is row 0."""
+    from fvgb300 import scan
+
+    torch = cuda
+    x = gen_clustered(512, 64, 8, 303)
+    if metric == "cosine":  # the engine normalises for cosine (index.rs:338-345)
+        x /= np.linalg.norm(x, axis=1, keepdims=True)
+    table = scan.Fp16Table(torch.from_numpy(x).cuda())
+    res = scan.fp16_search(table, torch.from_numpy(x[:4]).cuda(), 10, metric, dropin=True)
+    ids, _ = res_np(res)
+    assert ids[0, 0] == 0
+    assert np.array_equal(ids[:, 0], [0, 1, 2, 3])
+
+
+def test_fp16_filter_window(cuda):
+    """python/tests/test_bindings.py:142-169: mask = ids in [10, 200); every
+    returned id lies in the window."""
+    from fvgb300 import scan
+    from fvgb300.datasets import pack_bools
+
+    torch = cuda
+    rng = np.random.default_rng(7)
+    data = rng.standard_normal((400, 64)).astype(np.float32)
+    mask = np.zeros(400, dtype=bool)
+    mask[10:200] = True
+    table = scan.Fp16Table(torch.from_numpy(data).cuda())
+    m = torch.from_numpy(pack_bools(mask).view(np.int32)).cuda()
+    res = scan.fp16_search(table, torch.from_numpy(data[:2]).cuda(), 5, "l2", mask=m, dropin=True)
+    ids, _ = res_np(res)
+    valid = ids[ids != 0xFFFFFFFF]
+    assert valid.size > 0 and np.all((valid >= 10) & (valid < 200))
+
+
+def test_fp16_tiny_and_empty(cuda):
+    from fvgb300 import scan
+
+    torch = cuda
+    x = torch.randn(3, 32, device="cuda")
+    table = scan.Fp16Table(x)
+    res = scan.fp16_search(table, x[:2].contiguous(), 8, "l2")
+    ids, dist = res_np(res)
+    assert np.all(ids[:, 3:] == 0xFFFFFFFF) and np.all(dist[:, 3:] == np.float32(1e30))
+    assert sorted(ids[0, :3].tolist()) == [0, 1, 2]
+    empty = scan.Fp16Table(torch.zeros((0, 32), device="cuda"))
+    ids, dist = res_np(scan.fp16_search(empty, x[:2].contiguous(), 4, "ip"))
+    assert np.all(ids == 0xFFFFFFFF)
+    assert scan.device_status() == 0
+
+
+@pytest.mark.parametrize("k", [10, 100])
+def test_fp8_rescored_recall(cuda, oracle_mod, k):
+    """fp8 E4M3 with per-row scales, fp32 rescore, fp64 boundary band, on
+    data shaped like the 10M x 96 workload (N(0,1) component means, sigma
+    0.5), scaled down."""
+    from fvgb300 import datasets, scan
+
+    torch = cuda
+    base = datasets.sample_np(datasets.FP8_L2, 60000, seed=2, stream=0)
+    queries = datasets.sample_np(datasets.FP8_L2, 96, seed=2, stream=1)
+    table = scan.Fp8Table(torch.from_numpy(base).cuda())
+    res = scan.fp8_search(table, torch.from_numpy(queries).cuda(), k, "l2")
+    torch.cuda.synchronize()
+    ids, dist = res_np(res)
+    rec = check_rescored(oracle_mod, base, queries, ids, dist, "l2", k)
+    assert rec >= 0.99, rec
+    assert scan.device_status() == 0
