@@ -7,9 +7,13 @@
 // the reference's validation order and clamps (sparse_hybrid.cu:96-101,
 // 517-518).
 #include <atomic>
+#include <map>
 #include <mutex>
+#include <string>
 #include <unordered_map>
 #include <vector>
+#include <cstdio>
+#include <cstring>
 
 #include "../../include/fv_bridge.h"
 #include "common.cuh"
@@ -41,6 +45,36 @@ std::vector<uint32_t*> g_status;
 }  // namespace
 
 void note_launch(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+namespace {
+std::atomic<bool> g_prof_on{false};
+std::mutex g_prof_mu;
+std::vector<cudaEvent_t> g_prof_free;
+struct ProfRec {
+  std::string name;
+  cudaEvent_t a, b;
+};
+std::vector<ProfRec> g_prof_pending;
+}  // namespace
+
+bool profiling_enabled() { return g_prof_on.load(std::memory_order_relaxed); }
+
+cudaEvent_t profile_event() {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  if (!g_prof_free.empty()) {
+    cudaEvent_t e = g_prof_free.back();
+    g_prof_free.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void profile_record(const char* name, cudaEvent_t a, cudaEvent_t b) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof_pending.push_back({name, a, b});
+}
 
 int device_sm_count() {
   int dev = 0;
@@ -276,6 +310,47 @@ int fv_read_device_status(uint32_t* status) {
 }
 
 uint64_t fv_launch_count(void) { return fv::g_launches.load(std::memory_order_relaxed); }
+
+int fv_profile_enable(int on) {
+  fv::g_prof_on.store(on != 0);
+  return 0;
+}
+
+int fv_profile_summary(char* buf, size_t len) {
+  if (!buf || len == 0) return FV_ERR_NULL;
+  std::vector<fv::ProfRec> recs;
+  {
+    std::lock_guard<std::mutex> lk(fv::g_prof_mu);
+    recs.swap(fv::g_prof_pending);
+  }
+  std::map<std::string, std::pair<uint64_t, double>> agg;
+  int rc = 0;
+  for (auto& r : recs) {
+    float ms = 0.f;
+    cudaError_t e = cudaEventSynchronize(r.b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, r.a, r.b);
+    if (e != cudaSuccess) rc = (int)e;
+    auto& slot = agg[r.name];
+    slot.first += 1;
+    slot.second += ms;
+    std::lock_guard<std::mutex> lk(fv::g_prof_mu);
+    fv::g_prof_free.push_back(r.a);
+    fv::g_prof_free.push_back(r.b);
+  }
+  std::string out = "{";
+  bool first = true;
+  for (auto& kv : agg) {
+    char item[256];
+    snprintf(item, sizeof(item), "%s\"%s\": {\"launches\": %llu, \"ms\": %.6f}", first ? "" : ", ", kv.first.c_str(),
+             (unsigned long long)kv.second.first, kv.second.second);
+    out += item;
+    first = false;
+  }
+  out += "}";
+  if (out.size() + 1 > len) return FV_ERR_ARG;
+  memcpy(buf, out.c_str(), out.size() + 1);
+  return rc;
+}
 
 int fv_set_stream_scratch(void* stream, void* d_ptr, size_t bytes) {
   std::lock_guard<std::mutex> lk(fv::g_arena_mu);

@@ -313,6 +313,7 @@ int launch_flat_f32(const float* vectors, const uint32_t* vec_ids, uint32_t n, u
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<grid, NT, smem, stream>>>(a);
   };
+  ProfScope ps("flat_f32_scan", stream);
   switch (metric) {
     case METRIC_INNER_PRODUCT:
       vec4 ? go(flat_f32_scan_kernel<METRIC_INNER_PRODUCT, true>) : go(flat_f32_scan_kernel<METRIC_INNER_PRODUCT, false>);

@@ -32,6 +32,30 @@ uint32_t* status_word();
 // Host-side launch counter (fv_launch_count).
 void note_launch(uint32_t n = 1);
 
+// Optional per-kernel timing (fv_profile_enable): when on, ProfScope
+// records a CUDA event pair around the launches in its scope on `stream`.
+bool profiling_enabled();
+void profile_record(const char* name, cudaEvent_t start, cudaEvent_t stop);
+cudaEvent_t profile_event();
+struct ProfScope {
+  const char* name;
+  cudaStream_t stream;
+  cudaEvent_t start = nullptr;
+  ProfScope(const char* n, cudaStream_t s) : name(n), stream(s) {
+    if (profiling_enabled()) {
+      start = profile_event();
+      cudaEventRecord(start, stream);
+    }
+  }
+  ~ProfScope() {
+    if (start) {
+      cudaEvent_t stop = profile_event();
+      cudaEventRecord(stop, stream);
+      profile_record(name, start, stop);
+    }
+  }
+};
+
 // Per-stream scratch arena: returns a device buffer of at least `bytes`
 // bytes that stays valid for work enqueued on `stream` until the next call
 // for the same stream with a larger size. Grows with stream-ordered

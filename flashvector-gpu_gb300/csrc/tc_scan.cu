@@ -563,6 +563,7 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   uint64_t* partial = reinterpret_cast<uint64_t*>(scratch + q_bytes + 2 * qn_bytes);
 
   {
+    ProfScope ps(fp8 ? "tc_prep_queries_fp8" : "tc_prep_queries_fp16", stream);
     const uint32_t blocks = (nq * 32 + 255) / 256;
     if (fp8)
       tc_prep_queries_kernel<true><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm, qscale);
@@ -578,8 +579,12 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
 
   TcScanArgs a{t.n, nq, kblocks, nqb, splits, tps, (int)metric, t.norms, t.scales, qnorm, qscale, mask, partial,
                status_word()};
-  cudaError_t e = fp8 ? dispatch_scan<true>((int)kl, ta, tb, a, nqb * splits, stream)
-                      : dispatch_scan<false>((int)kl, ta, tb, a, nqb * splits, stream);
+  cudaError_t e;
+  {
+    ProfScope ps(fp8 ? "tc_scan_fp8" : "tc_scan_fp16", stream);
+    e = fp8 ? dispatch_scan<true>((int)kl, ta, tb, a, nqb * splits, stream)
+            : dispatch_scan<false>((int)kl, ta, tb, a, nqb * splits, stream);
+  }
   if (e != cudaSuccess) return (int)e;
 
   SelectArgs s{partial, splits, kl, next_pow2(splits * kl), shortlist, k, queries, t.vectors, t.dim, (int)metric,
@@ -588,8 +593,11 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   const size_t sel_smem = (size_t)std::max(s.pow2, next_pow2(shortlist)) * 8;
   e = cudaFuncSetAttribute(tc_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sel_smem);
   if (e != cudaSuccess) return (int)e;
-  tc_select_kernel<<<nq, SEL_THREADS, sel_smem, stream>>>(s);
-  note_launch();
+  {
+    ProfScope ps("tc_select_rescore", stream);
+    tc_select_kernel<<<nq, SEL_THREADS, sel_smem, stream>>>(s);
+    note_launch();
+  }
   return (int)cudaGetLastError();
 }
 

@@ -77,6 +77,8 @@ SIGNATURES = {
     "fv_version": (C.c_char_p, []),
     "fv_read_device_status": (I32, [P]),
     "fv_launch_count": (C.c_uint64, []),
+    "fv_profile_enable": (I32, [I32]),
+    "fv_profile_summary": (I32, [C.c_char_p, SZ]),
     "fv_set_stream_scratch": (I32, [P, P, SZ]),
     "fv_release_stream_scratch": (I32, [P]),
 }

@@ -155,3 +155,16 @@ def fp8_search(table, queries, k, metric="l2", mask=None, opts=None, out=None, s
     call("fv_fp8_search_batch", C.byref(table.struct), _ptr(queries), nq, k, _metric(metric), _ptr(mask),
          C.byref(o), _ptr(out), _stream(stream))
     return out
+
+
+def profile_enable(on: bool = True) -> None:
+    call("fv_profile_enable", 1 if on else 0)
+
+
+def profile_summary() -> dict:
+    """Per-kernel {name: {"launches": n, "ms": total}} since the last call."""
+    import json
+
+    buf = C.create_string_buffer(1 << 16)
+    call("fv_profile_summary", buf, len(buf))
+    return json.loads(buf.value.decode())

@@ -125,6 +125,12 @@ int fv_read_device_status(uint32_t* status);
 /* Number of this library's kernel launches issued since load (all
  * devices, all streams); used to count launches inside timed regions. */
 uint64_t fv_launch_count(void);
+/* Per-kernel timing: while enabled, each kernel launch of the library is
+ * bracketed by a CUDA event pair on its stream. fv_profile_summary waits
+ * for the recorded events, writes {"kernel": {"launches": n, "ms": t}, ...}
+ * (JSON, NUL-terminated) into buf and clears the record. */
+int fv_profile_enable(int on);
+int fv_profile_summary(char* buf, size_t len);
 /* Installs a caller-owned device buffer as the scratch arena of `stream`
  * (kernels that need scratch then never allocate on that stream; a call
  * needing more than `bytes` fails with cudaErrorMemoryAllocation).
