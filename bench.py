@@ -19,6 +19,7 @@ from pinned host memory, search, and copy the results back. The base set
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -174,8 +175,9 @@ def run_reference(a, world, rank):
     from fvgb300 import datasets
 
     threads = os.cpu_count() or 1
-    base = datasets.sample_np(datasets.FP16_IP_UNIT, a.n, seed=1, stream=0)
-    queries = datasets.sample_np(datasets.FP16_IP_UNIT, a.batch, seed=1, stream=1)
+    mix = dataclasses.replace(datasets.FP16_IP_UNIT, dim=a.dim)
+    base = datasets.sample_np(mix, a.n, seed=1, stream=0)
+    queries = datasets.sample_np(mix, a.batch, seed=1, stream=1)
     words = datasets.bernoulli_mask_words(a.n, 0.5, seed=1)
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
@@ -223,9 +225,10 @@ def run_ours(a, world, rank, local):
         dist.init_process_group("nccl", device_id=dev)
     stream = torch.cuda.current_stream()
 
-    base = datasets.sample_torch(datasets.FP16_IP_UNIT, a.n, seed=1, stream=0, device=dev)
+    mix = dataclasses.replace(datasets.FP16_IP_UNIT, dim=a.dim)
+    base = datasets.sample_torch(mix, a.n, seed=1, stream=0, device=dev)
     nbatches = 4
-    qpool = datasets.sample_torch(datasets.FP16_IP_UNIT, a.batch * nbatches, seed=1, stream=1, device=dev)
+    qpool = datasets.sample_torch(mix, a.batch * nbatches, seed=1, stream=1, device=dev)
     batches = [qpool[i * a.batch:(i + 1) * a.batch].contiguous() for i in range(nbatches)]
     words = datasets.bernoulli_mask_words(a.n, 0.5, seed=1)
     mask = torch.from_numpy(words.view(np.int32)).to(dev)
