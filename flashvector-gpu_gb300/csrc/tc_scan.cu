@@ -249,18 +249,21 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
 
       const uint32_t t_row = tmem + ((uint32_t)(quad * 32) << 16) + buf * TC_N;
 #pragma unroll 1
-      for (int c0 = 0; c0 < TC_N; c0 += 32) {
-        float v[32];
-        tc::tmem_ld32(t_row + c0, v);
-        const uint32_t mw = qvalid ? cm[c0 >> 5] : 0u;
-        if (mw == 0u) continue;
-        // distances of the 32 columns, and a prefilter against the current
-        // worst kept distance (it only shrinks while inserting, so a column
-        // that fails here can never enter the heap)
-        uint32_t pass = 0;
+      for (int c0 = 0; c0 < TC_N; c0 += 64) {
+        uint32_t ra[32], rb[32];
+        tc::tmem_ld32_async(t_row + c0, ra);
+        tc::tmem_ld32_async(t_row + c0 + 32, rb);
+        tc::tmem_wait_ld(ra);
+        tc::reg_fence(rb);
+        const uint64_t mw = qvalid ? ((uint64_t)cm[(c0 >> 5) + 1] << 32 | cm[c0 >> 5]) : 0ull;
+        if (mw == 0ull) continue;
+        // exact per-column distances (the same expressions the insertion
+        // test uses), reduced to their minimum: a 64-column batch whose
+        // minimum cannot beat the worst kept distance is skipped whole
+        float v[64];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          float dot = v[j];
+        for (int j = 0; j < 64; ++j) {
+          float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
           if (FP8) dot = dot * (qs * cb[TC_N + c0 + j]);
           float dist;
           if (metric == METRIC_INNER_PRODUCT) {
@@ -271,17 +274,19 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
             dist = fmaxf(0.f, fmaf(-2.0f, dot, qn + cb[c0 + j]));
           }
           v[j] = dist;
-          pass |= (dist < worst ? 1u : 0u) << j;
         }
-        pass &= mw;
-        while (pass) {
-          const int j = __ffs(pass) - 1;
-          pass &= pass - 1;
-          float dist = v[0];
+        float m[32];
 #pragma unroll
-          for (int u = 1; u < 32; ++u) dist = (j == u) ? v[u] : dist;
-          if (dist < worst) {
-            heap_sift(h, KL, make_key(dist, v0 + c0 + j));
+        for (int j = 0; j < 32; ++j) m[j] = fminf(v[j], v[j + 32]);
+#pragma unroll
+        for (int w = 16; w > 0; w >>= 1)
+#pragma unroll
+          for (int j = 0; j < w; ++j) m[j] = fminf(m[j], m[j + w]);
+        if (!(m[0] < worst)) continue;
+#pragma unroll
+        for (int j = 0; j < 64; ++j) {
+          if (((mw >> j) & 1ull) && v[j] < worst) {
+            heap_sift(h, KL, make_key(v[j], v0 + c0 + j));
             const uint64_t root = h[0];
             worst = root == kSentinelKey ? kSentinelDist : key_dist(root);
           }
