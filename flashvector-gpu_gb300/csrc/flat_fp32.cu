@@ -16,6 +16,8 @@
 //    insertion in slot order);
 //  * when the base range is split over several CTAs the per-split heaps go
 //    to scratch and a second kernel merges them.
+#include <mutex>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "topk.cuh"
@@ -336,4 +338,122 @@ int launch_flat_f32(const float* vectors, const uint32_t* vec_ids, uint32_t n, u
   return (int)cudaGetLastError();
 }
 
+
+// ===========================================================================
+// Allocation-free variant of the exact flat scan.
+//
+// Some callers of this library cannot call cudaMalloc: code that runs while
+// another thread is capturing a CUDA graph in global capture mode (where an
+// allocation is an illegal call), latency-critical serving threads that
+// must not take the allocator's locks or risk its implicit device
+// synchronisation, and hosts that hand all device memory to one pool of
+// their own. For them fv_flat_scan_batch_noalloc keeps the per-split heaps
+// of the scan in the fixed array below instead of the per-stream arena.
+//
+// The array is a file-scope device variable: every GPU that loads this
+// library holds its kNoAllocScratchBytes until the process exits. In host
+// code its name is only a host-side stand-in, not a device address, so the
+// address handed to the kernels is looked up once per device with
+// cudaGetSymbolAddress (with that device current) on the first call made
+// on the device; make that first call before any stream capture begins.
+// All calls share the one array and it keeps whatever the last call wrote;
+// the scan writes every slot it later reads, so nothing needs clearing, but
+// calls whose work overlaps on the GPU (different streams, or host threads
+// racing on one device) overwrite each other's heaps -- serialise them.
+// ===========================================================================
+namespace {
+constexpr size_t kNoAllocScratchBytes = 8u << 20;  // 8 MiB per device
+static __device__ __align__(256) uint64_t g_flat_noalloc_scratch[kNoAllocScratchBytes / 8];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+uint64_t* g_noalloc_addr[kMaxDevices] = {};
+
+cudaError_t noalloc_scratch_address(uint64_t** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_flat_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_addr[dev] = static_cast<uint64_t*>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return cudaSuccess;
+}
+}  // namespace
+
+// Same work split and kernels as launch_flat_f32, with the per-split heaps
+// in the fixed array; refuses (FV_ERR_SCRATCH_LIMIT) a call whose heaps
+// would not fit instead of allocating.
+int launch_flat_f32_noalloc(const float* vectors, const uint32_t* vec_ids, uint32_t n, uint32_t dim,
+                            const float* queries, uint32_t nq, uint32_t k, MetricType metric, const uint32_t* mask,
+                            GpuSearchResult* out, cudaStream_t stream) {
+  const uint32_t nqb = (nq + QT - 1) / QT;
+  const uint32_t ntiles = (n + VT - 1) / VT;
+  int sms = device_sm_count();
+  uint32_t splits = (uint32_t)((2 * sms + nqb - 1) / nqb);
+  const uint32_t pow2k = next_pow2(k);
+  splits = std::max(1u, std::min(splits, std::min(ntiles, 8192u / pow2k)));
+  uint32_t tps = (ntiles + splits - 1) / splits;
+  splits = (ntiles + tps - 1) / tps;
+
+  FlatArgs a{vectors, vec_ids, n, dim, queries, nq, k, mask, out, nullptr, splits, tps};
+  if (splits > 1) {
+    const size_t need = (size_t)nq * splits * k * 8;
+    if (need > kNoAllocScratchBytes) return -6;  // FV_ERR_SCRATCH_LIMIT
+    uint64_t* p = nullptr;
+    cudaError_t e = noalloc_scratch_address(&p);
+    if (e != cudaSuccess) return (int)e;
+    a.partial = p;
+  }
+  const size_t smem = flat_f32_smem_bytes(k);
+  const bool vec4 = (dim % 4 == 0) && ((uintptr_t)vectors % 16 == 0) && ((uintptr_t)queries % 16 == 0);
+  dim3 grid(nqb, splits);
+  auto go = [&](auto kern) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<grid, NT, smem, stream>>>(a);
+  };
+  switch (metric) {
+    case METRIC_INNER_PRODUCT:
+      vec4 ? go(flat_f32_scan_kernel<METRIC_INNER_PRODUCT, true>) : go(flat_f32_scan_kernel<METRIC_INNER_PRODUCT, false>);
+      break;
+    case METRIC_COSINE:
+      vec4 ? go(flat_f32_scan_kernel<METRIC_COSINE, true>) : go(flat_f32_scan_kernel<METRIC_COSINE, false>);
+      break;
+    default:
+      vec4 ? go(flat_f32_scan_kernel<METRIC_L2, true>) : go(flat_f32_scan_kernel<METRIC_L2, false>);
+      break;
+  }
+  note_launch();
+  if (splits > 1) {
+    const uint32_t pow2 = next_pow2(splits * k);
+    const size_t msmem = (size_t)pow2 * 8;
+    cudaFuncSetAttribute(merge_partial_topk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msmem);
+    merge_partial_topk_kernel<<<nq, 256, msmem, stream>>>(a.partial, splits, k, pow2, vec_ids, out, k);
+    note_launch();
+  }
+  return (int)cudaGetLastError();
+}
+
 }  // namespace fv
+
+extern "C" int fv_flat_scan_batch_noalloc(const float* d_vectors, const uint32_t* d_vec_ids, uint32_t num_vectors,
+                                          uint32_t dim, const float* d_queries, uint32_t num_queries, uint32_t top_k,
+                                          MetricType metric, const uint32_t* d_valid_mask,
+                                          GpuSearchResult* d_out_results, void* stream) {
+  if (!d_queries || !d_out_results) return -1;
+  if (num_vectors > 0 && !d_vectors) return -1;
+  if (num_queries == 0 || top_k == 0) return 0;
+  if (top_k > (uint32_t)fv::kMaxTopK) top_k = fv::kMaxTopK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (num_vectors == 0)
+    return (int)cudaMemsetAsync(d_out_results, 0xFF, (size_t)num_queries * top_k * sizeof(GpuSearchResult), s);
+  if (dim == 0) return -2;
+  return fv::launch_flat_f32_noalloc(d_vectors, d_vec_ids, num_vectors, dim, d_queries, num_queries, top_k, metric,
+                                     d_valid_mask, d_out_results, s);
+}
+

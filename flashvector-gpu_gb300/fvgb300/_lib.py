@@ -67,6 +67,7 @@ SIGNATURES = {
     "cuda_destroy_stream": (I32, [P]),
     "cuda_sync_stream": (I32, [P]),
     "cuda_flat_scan_batch": (I32, [P, P, U32, U32, P, U32, U32, I32, P, P, P]),
+    "fv_flat_scan_batch_noalloc": (I32, [P, P, U32, U32, P, U32, U32, I32, P, P, P]),
     "cuda_compute_distances_warp": (I32, [P, P, U32, U32, U32, I32, P, P]),
     "cuda_bitonic_sort_test": (I32, [P, P, P, P, U32, P]),
     "cuda_fp16_tc_search_batch": (I32, [P, P, U32, U32, I32, P, P, P]),

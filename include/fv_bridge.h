@@ -32,6 +32,7 @@ extern "C" {
 #define FV_ERR_TIMEOUT (-3)    /* a bounded device wait gave up               */
 #define FV_ERR_NOMEM (-4)      /* scratch admission refused                   */
 #define FV_ERR_ARCH (-5)       /* device is not sm_103 / sm_100 class         */
+#define FV_ERR_SCRATCH_LIMIT (-6) /* work exceeds a fixed scratch area's size  */
 
 /* ---- device, memory and stream plumbing -------------------------------
  * Replace cuda_bridge.h:11-31 (hnsw_traverse.cu:525-637). */
@@ -64,6 +65,30 @@ int cuda_flat_scan_batch(const float* d_vectors, const uint32_t* d_vec_ids,
                          uint32_t top_k, MetricType metric,
                          const uint32_t* d_valid_mask,
                          GpuSearchResult* d_out_results, void* stream);
+
+/* Allocation-free exact flat scan. No counterpart in the reference: it is
+ * cuda_flat_scan_batch for callers that may not allocate device memory --
+ * threads running while a CUDA graph is captured in global mode (where
+ * cudaMalloc is an illegal call), latency-critical serving threads that
+ * must not take the allocator's locks or its implicit synchronisation, and
+ * hosts that give all device memory to a pool of their own. Same arguments,
+ * results (bit-identical) and return codes as cuda_flat_scan_batch; the
+ * per-split heaps that cuda_flat_scan_batch keeps in a per-stream arena
+ * live instead in one fixed 8 MiB device array that the library holds on
+ * every GPU that loads it, until exit. The caller still passes inputs and
+ * outputs. A call whose heaps (num_queries x splits x top_k x 8 bytes)
+ * would exceed the array is refused with FV_ERR_SCRATCH_LIMIT and
+ * launches nothing. The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) and caches it: make that first call
+ * before any stream capture. All calls share the array, which keeps the
+ * last call's contents; calls whose GPU work overlaps (other streams, other
+ * host threads on the same device) race on it and must be serialised. */
+int fv_flat_scan_batch_noalloc(const float* d_vectors, const uint32_t* d_vec_ids,
+                               uint32_t num_vectors, uint32_t dim,
+                               const float* d_queries, uint32_t num_queries,
+                               uint32_t top_k, MetricType metric,
+                               const uint32_t* d_valid_mask,
+                               GpuSearchResult* d_out_results, void* stream);
 
 /* ---- tensor-core flat scans --------------------------------------------
  * Replaces cuda_bridge.h:138-147 (ivf_quant_lookup.cu:1106-1123). Per
