@@ -49,6 +49,9 @@ struct TcScanArgs {
   const float* qscale;   // [nq] per-query fp8 scale (FP8 only)
   const uint32_t* mask;
   uint64_t* partial;     // [nq][splits][KL]
+  uint32_t* tau;         // [nq] shared bound on each query's kl-th distance (float_order)
+  uint32_t kl;           // heap entries used (<= KL); == shortlist when shared bounds are on
+  uint32_t share_tau;    // 1: CTAs of one query publish / read tau (kl == shortlist)
   uint32_t* status;
 };
 
@@ -82,6 +85,22 @@ __device__ __noinline__ void heap_sift(uint64_t* h, int kl, uint64_t key) {
     i = c;
   }
   h[i * TC_M] = key;
+}
+
+// v[j] for a lane-varying j without local memory: a 6-level select tree.
+__device__ __forceinline__ float select64(const float (&v)[64], int j) {
+  float t[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) t[i] = (j & 1) ? v[2 * i + 1] : v[2 * i];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) t[i] = (j & 2) ? t[2 * i + 1] : t[2 * i];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) t[i] = (j & 4) ? t[2 * i + 1] : t[2 * i];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) t[i] = (j & 8) ? t[2 * i + 1] : t[2 * i];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) t[i] = (j & 16) ? t[2 * i + 1] : t[2 * i];
+  return (j & 32) ? t[1] : t[0];
 }
 
 template <bool FP8, int KL, int STAGES>
@@ -212,7 +231,15 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
     const uint32_t q = qb * TC_M + row;
     const bool qvalid = q < a.nq;
     uint64_t* h = heap + row;
-    for (int i = 0; i < KL; ++i) h[i * TC_M] = kSentinelKey;
+    const int kl = (int)a.kl;
+    for (int i = 0; i < kl; ++i) h[i * TC_M] = kSentinelKey;
+    // Shared bound: every CTA scanning query q publishes the distance of its
+    // kl-th best key once its heap is full; the minimum over CTAs bounds the
+    // query's global kl-th best distance from above, so any row farther
+    // than it cannot be in the shortlist and is skipped by every CTA.
+    float tau_d = kSentinelDist;
+    float published = kSentinelDist;
+    uint32_t* tau_ptr = (a.share_tau && qvalid) ? a.tau + q : nullptr;
     const float qn = qvalid ? __ldg(a.qnorm + q) : 0.f;
     const float qs = (FP8 && qvalid) ? __ldg(a.qscale + q) : 1.f;
     float worst = kSentinelDist;
@@ -244,8 +271,10 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
         cm[lane] = w;
       }
       __syncwarp();
+      const uint32_t tau_raw = tau_ptr ? __ldcg(tau_ptr) : 0u;
       if (!tc::mbar_wait(&acc_full[buf], use & 1, abort_flag, a.status)) break;
       tc::tc_fence_after();
+      if (tau_ptr) tau_d = fminf(tau_d, order_float(tau_raw));
 
       const uint32_t t_row = tmem + ((uint32_t)(quad * 32) << 16) + buf * TC_N;
 #pragma unroll 1
@@ -282,23 +311,36 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
         for (int w = 16; w > 0; w >>= 1)
 #pragma unroll
           for (int j = 0; j < w; ++j) m[j] = fminf(m[j], m[j + w]);
-        if (!(m[0] < worst)) continue;
+        if (!(m[0] < worst && m[0] <= tau_d)) continue;
+        // columns that may enter: the warp walks them lane-parallel, one
+        // per lane per round, fetching v[j] with a depth-6 select tree
+        uint64_t pass = 0;
 #pragma unroll
-        for (int j = 0; j < 64; ++j) {
-          if (((mw >> j) & 1ull) && v[j] < worst) {
-            heap_sift(h, KL, make_key(v[j], v0 + c0 + j));
+        for (int j = 0; j < 64; ++j) pass |= (uint64_t)(v[j] < worst && v[j] <= tau_d) << j;
+        pass &= mw;
+        while (pass) {
+          const int j = __ffsll((long long)pass) - 1;
+          pass &= pass - 1;
+          const float dist = select64(v, j);
+          if (dist < worst && dist <= tau_d) {
+            heap_sift(h, kl, make_key(dist, v0 + c0 + j));
             const uint64_t root = h[0];
             worst = root == kSentinelKey ? kSentinelDist : key_dist(root);
           }
         }
+      }
+      if (tau_ptr && worst < published) {
+        // heap full (worst < 1e30 only then): publish its kl-th distance
+        atomicMin(tau_ptr, float_order(worst));
+        published = worst;
       }
       tc::tc_fence_before();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&acc_empty[buf]);
     }
     if (qvalid) {
-      uint64_t* dst = a.partial + ((size_t)q * a.splits + split) * KL;
-      for (int i = 0; i < KL; ++i) dst[i] = h[i * TC_M];
+      uint64_t* dst = a.partial + ((size_t)q * a.splits + split) * kl;
+      for (int i = 0; i < kl; ++i) dst[i] = h[i * TC_M];
     }
   }
 
@@ -323,12 +365,14 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
 template <bool FP8>
 __global__ void __launch_bounds__(256) tc_prep_queries_kernel(const float* __restrict__ q, uint32_t nq, uint32_t dim,
                                                               uint32_t pd, void* __restrict__ out,
-                                                              float* __restrict__ qnorm, float* __restrict__ qscale) {
+                                                              float* __restrict__ qnorm, float* __restrict__ qscale,
+                                                              uint32_t* __restrict__ tau) {
   const uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (qi >= nq) return;
   const float* src = q + (size_t)qi * dim;
   if (lane == 0) {
+    tau[qi] = float_order(kSentinelDist);
     float s = 0.f;
     for (uint32_t d = 0; d < dim; ++d) s = fmaf(src[d], src[d], s);
     qnorm[qi] = s;
@@ -545,7 +589,8 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   const uint32_t kblocks = (t.padded_dim + kb_elems - 1) / kb_elems;
   const uint32_t overfetch = opt.overfetch ? opt.overfetch : 4;
   const uint32_t shortlist = t.vectors ? std::min<uint32_t>(std::max(k, overfetch * k), 4096u) : k;
-  const uint32_t kl = std::min<uint32_t>(64u, (shortlist + 15) / 16 * 16);
+  const uint32_t kl = std::min<uint32_t>(64u, shortlist);            // heap entries per (query, range)
+  const uint32_t kl_tmpl = std::min<uint32_t>(64u, (kl + 15) / 16 * 16);  // heap capacity (template)
   const uint32_t nqb = (nq + TC_M - 1) / TC_M;
   const uint32_t ntiles = (t.n + TC_N - 1) / TC_N;
   const int sms = device_sm_count();
@@ -559,21 +604,24 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   // scratch: prepared queries | ||q||^2 | q scales | partial heaps
   const size_t q_bytes = align_up((size_t)nq * t.padded_dim * elem, 1024);
   const size_t qn_bytes = align_up((size_t)nq * 4, 256);
-  const size_t part_bytes = (size_t)nq * splits * kl * 8;
-  uint8_t* scratch = static_cast<uint8_t*>(scratch_get(stream, q_bytes + 2 * qn_bytes + part_bytes));
+  const size_t part_bytes = align_up((size_t)nq * splits * kl * 8, 256);
+  uint8_t* scratch = static_cast<uint8_t*>(scratch_get(stream, q_bytes + 3 * qn_bytes + part_bytes));
   if (!scratch) return (int)cudaErrorMemoryAllocation;
   void* qprep = scratch;
   float* qnorm = reinterpret_cast<float*>(scratch + q_bytes);
   float* qscale = reinterpret_cast<float*>(scratch + q_bytes + qn_bytes);
   uint64_t* partial = reinterpret_cast<uint64_t*>(scratch + q_bytes + 2 * qn_bytes);
+  uint32_t* tau = reinterpret_cast<uint32_t*>(scratch + q_bytes + 2 * qn_bytes + part_bytes);
 
   {
     ProfScope ps(fp8 ? "tc_prep_queries_fp8" : "tc_prep_queries_fp16", stream);
     const uint32_t blocks = (nq * 32 + 255) / 256;
     if (fp8)
-      tc_prep_queries_kernel<true><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm, qscale);
+      tc_prep_queries_kernel<true><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm, qscale,
+                                                               tau);
     else
-      tc_prep_queries_kernel<false><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm, qscale);
+      tc_prep_queries_kernel<false><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm,
+                                                                qscale, tau);
     note_launch();
   }
 
@@ -582,13 +630,13 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
       !encode_tmap(&tb, t.base, fp8, t.padded_dim, t.n, (uint64_t)t.padded_dim * elem, TC_N))
     return FV_ERR_ARG;
 
-  TcScanArgs a{t.n, nq, kblocks, nqb, splits, tps, (int)metric, t.norms, t.scales, qnorm, qscale, mask, partial,
-               status_word()};
+  TcScanArgs a{t.n,   nq,      kblocks, nqb, splits, tps, (int)metric, t.norms, t.scales, qnorm, qscale, mask, partial,
+               tau, kl,     kl == shortlist ? 1u : 0u, status_word()};
   cudaError_t e;
   {
     ProfScope ps(fp8 ? "tc_scan_fp8" : "tc_scan_fp16", stream);
-    e = fp8 ? dispatch_scan<true>((int)kl, ta, tb, a, nqb * splits, stream)
-            : dispatch_scan<false>((int)kl, ta, tb, a, nqb * splits, stream);
+    e = fp8 ? dispatch_scan<true>((int)kl_tmpl, ta, tb, a, nqb * splits, stream)
+            : dispatch_scan<false>((int)kl_tmpl, ta, tb, a, nqb * splits, stream);
   }
   if (e != cudaSuccess) return (int)e;
 
