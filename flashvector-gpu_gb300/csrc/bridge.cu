@@ -280,6 +280,66 @@ int fv_encode_fp8(const float* d_vectors, uint32_t num_vectors, uint32_t dim, ui
                                (cudaStream_t)stream);
 }
 
+// ------------------------------------------------------------------ IVF
+namespace {
+int ivf_pq(const IvfPqGpuTables* t, const FvIvfOptions* o, const float* q, uint32_t nq, uint32_t top_k,
+           uint32_t nprobe, uint32_t rerank_k, MetricType metric, const uint32_t* mask, GpuSearchResult* out,
+           void* stream) {
+  if (!t || !q || !out) return FV_ERR_NULL;
+  if (nq == 0 || top_k == 0 || t->m_pq == 0 || t->nlist == 0) return 0;
+  if (!t->d_centroids || !t->d_pq_codebooks || !t->d_pq_codes || !t->d_ivf_offsets || !t->d_ivf_vec_ids)
+    return FV_ERR_NULL;
+  fv::IvfLaunch L{t->d_centroids, t->d_pq_codebooks, nullptr, nullptr, t->d_pq_codes, t->d_ivf_offsets,
+                  t->d_ivf_vec_ids, t->d_vectors, t->num_vectors, t->dim, t->nlist, t->m_pq, t->sub_dim,
+                  o && o->codes_list_major, q, nq, top_k, nprobe, rerank_k, metric, mask, out};
+  return fv::launch_ivf_search(0, L, (cudaStream_t)stream);
+}
+int ivf_sq(const IvfSqGpuTables* t, const FvIvfOptions* o, const float* q, uint32_t nq, uint32_t top_k,
+           uint32_t nprobe, uint32_t rerank_k, MetricType metric, const uint32_t* mask, GpuSearchResult* out,
+           void* stream) {
+  if (!t || !q || !out) return FV_ERR_NULL;
+  if (nq == 0 || top_k == 0 || t->nlist == 0 || t->dim == 0) return 0;
+  if (!t->d_centroids || !t->d_sq_mins || !t->d_sq_scales || !t->d_sq_codes || !t->d_ivf_offsets ||
+      !t->d_ivf_vec_ids)
+    return FV_ERR_NULL;
+  fv::IvfLaunch L{t->d_centroids, nullptr, t->d_sq_mins, t->d_sq_scales, t->d_sq_codes, t->d_ivf_offsets,
+                  t->d_ivf_vec_ids, t->d_vectors, t->num_vectors, t->dim, t->nlist, 0, 0,
+                  o && o->codes_list_major, q, nq, top_k, nprobe, rerank_k, metric, mask, out};
+  return fv::launch_ivf_search(1, L, (cudaStream_t)stream);
+}
+}  // namespace
+
+int cuda_ivf_pq_search_batch(const IvfPqGpuTables* tables, const float* d_queries, uint32_t num_queries,
+                             uint32_t top_k, uint32_t nprobe, uint32_t rerank_k, MetricType metric,
+                             const uint32_t* d_valid_mask, GpuSearchResult* d_out_results, void* stream) {
+  return ivf_pq(tables, nullptr, d_queries, num_queries, top_k, nprobe, rerank_k, metric, d_valid_mask,
+                d_out_results, stream);
+}
+int cuda_ivf_sq_search_batch(const IvfSqGpuTables* tables, const float* d_queries, uint32_t num_queries,
+                             uint32_t top_k, uint32_t nprobe, uint32_t rerank_k, MetricType metric,
+                             const uint32_t* d_valid_mask, GpuSearchResult* d_out_results, void* stream) {
+  return ivf_sq(tables, nullptr, d_queries, num_queries, top_k, nprobe, rerank_k, metric, d_valid_mask,
+                d_out_results, stream);
+}
+int fv_ivf_pq_search_ex(const IvfPqGpuTables* tables, const FvIvfOptions* options, const float* d_queries,
+                        uint32_t num_queries, uint32_t top_k, uint32_t nprobe, uint32_t rerank_k, MetricType metric,
+                        const uint32_t* d_valid_mask, GpuSearchResult* d_out_results, void* stream) {
+  return ivf_pq(tables, options, d_queries, num_queries, top_k, nprobe, rerank_k, metric, d_valid_mask,
+                d_out_results, stream);
+}
+int fv_ivf_sq_search_ex(const IvfSqGpuTables* tables, const FvIvfOptions* options, const float* d_queries,
+                        uint32_t num_queries, uint32_t top_k, uint32_t nprobe, uint32_t rerank_k, MetricType metric,
+                        const uint32_t* d_valid_mask, GpuSearchResult* d_out_results, void* stream) {
+  return ivf_sq(tables, options, d_queries, num_queries, top_k, nprobe, rerank_k, metric, d_valid_mask,
+                d_out_results, stream);
+}
+int fv_ivf_relayout_codes(const uint8_t* d_codes_by_id, const uint32_t* d_ivf_vec_ids, uint32_t num_vectors,
+                          uint32_t row_bytes, uint8_t* d_out_by_list, void* stream) {
+  if (num_vectors && (!d_codes_by_id || !d_ivf_vec_ids || !d_out_by_list)) return FV_ERR_NULL;
+  return fv::launch_relayout_codes(d_codes_by_id, d_ivf_vec_ids, num_vectors, row_bytes, d_out_by_list,
+                                   (cudaStream_t)stream);
+}
+
 // ------------------------------------------------------------- fixtures
 int cuda_compute_distances_warp(const float* d_queries, const float* d_dataset, uint32_t num_queries,
                                 uint32_t num_vectors, uint32_t dim, MetricType metric, float* d_out_distances,

@@ -89,7 +89,10 @@ __device__ void heap_sort_ascending(uint64_t* heap, int k, int s) {
   }
 }
 
-template <int METRIC, bool VEC4>
+// FUSED = false: separately rounded sub/mul/add in dimension order (the
+// reference's exact search). FUSED = true: fmaf(diff, diff, acc) in
+// dimension order (the reference's coarse quantizer, ivf_rerank.cuh:80-84).
+template <int METRIC, bool VEC4, bool FUSED = false>
 __global__ void __launch_bounds__(NT) flat_f32_scan_kernel(FlatArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* qs = reinterpret_cast<float*>(smem_raw);  // [DK][QS]
@@ -195,7 +198,10 @@ __global__ void __launch_bounds__(NT) flat_f32_scan_kernel(FlatArgs a) {
         for (int i = 0; i < 4; ++i)
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
-            if (METRIC == METRIC_L2) {
+            if (METRIC == METRIC_L2 && FUSED) {
+              float diff = __fsub_rn(qv[i], xv[j]);
+              acc[i][j] = fmaf(diff, diff, acc[i][j]);
+            } else if (METRIC == METRIC_L2) {
               float diff = __fsub_rn(qv[i], xv[j]);
               acc[i][j] = __fadd_rn(acc[i][j], __fmul_rn(diff, diff));
             } else {
@@ -289,9 +295,7 @@ size_t flat_f32_smem_bytes(uint32_t k) {
   return bytes + (size_t)k * QT * 8;
 }
 
-int launch_flat_f32(const float* vectors, const uint32_t* vec_ids, uint32_t n, uint32_t dim, const float* queries,
-                    uint32_t nq, uint32_t k, MetricType metric, const uint32_t* mask, GpuSearchResult* out,
-                    uint32_t forced_splits, cudaStream_t stream) {
+FlatPlan plan_flat_f32(uint32_t n, uint32_t nq, uint32_t k, uint32_t forced_splits) {
   const uint32_t nqb = (nq + QT - 1) / QT;
   const uint32_t ntiles = (n + VT - 1) / VT;
   int sms = device_sm_count();
@@ -300,13 +304,34 @@ int launch_flat_f32(const float* vectors, const uint32_t* vec_ids, uint32_t n, u
   splits = std::max(1u, std::min(splits, std::min(ntiles, 8192u / pow2k)));
   uint32_t tps = (ntiles + splits - 1) / splits;
   splits = (ntiles + tps - 1) / tps;
+  FlatPlan p;
+  p.splits = splits;
+  p.tiles_per_split = tps;
+  p.scratch_bytes = splits > 1 ? (size_t)nq * splits * k * 8 : 0;
+  return p;
+}
 
-  FlatArgs a{vectors, vec_ids, n, dim, queries, nq, k, mask, out, nullptr, splits, tps};
-  const size_t total_keys = (size_t)nq * splits * k;
-  if (splits > 1) {
-    a.partial = static_cast<uint64_t*>(scratch_get(stream, total_keys * 8));
-    if (!a.partial) return (int)cudaErrorMemoryAllocation;
+int launch_flat_f32(const float* vectors, const uint32_t* vec_ids, uint32_t n, uint32_t dim, const float* queries,
+                    uint32_t nq, uint32_t k, MetricType metric, const uint32_t* mask, GpuSearchResult* out,
+                    uint32_t forced_splits, cudaStream_t stream) {
+  const FlatPlan p = plan_flat_f32(n, nq, k, forced_splits);
+  void* scratch = nullptr;
+  if (p.scratch_bytes) {
+    scratch = scratch_get(stream, p.scratch_bytes);
+    if (!scratch) return (int)cudaErrorMemoryAllocation;
   }
+  return launch_flat_f32_planned(p, vectors, vec_ids, n, dim, queries, nq, k, metric, mask, out, false, scratch,
+                                 stream);
+}
+
+int launch_flat_f32_planned(const FlatPlan& p, const float* vectors, const uint32_t* vec_ids, uint32_t n,
+                            uint32_t dim, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
+                            const uint32_t* mask, GpuSearchResult* out, bool fused, void* scratch,
+                            cudaStream_t stream) {
+  const uint32_t nqb = (nq + QT - 1) / QT;
+  const uint32_t splits = p.splits, tps = p.tiles_per_split;
+  FlatArgs a{vectors, vec_ids, n, dim, queries, nq, k, mask, out, static_cast<uint64_t*>(scratch), splits, tps};
+  if (splits > 1 && !a.partial) return (int)cudaErrorMemoryAllocation;
 
   const size_t smem = flat_f32_smem_bytes(k);
   const bool vec4 = (dim % 4 == 0) && ((uintptr_t)vectors % 16 == 0) && ((uintptr_t)queries % 16 == 0);
@@ -315,17 +340,22 @@ int launch_flat_f32(const float* vectors, const uint32_t* vec_ids, uint32_t n, u
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<grid, NT, smem, stream>>>(a);
   };
-  ProfScope ps("flat_f32_scan", stream);
-  switch (metric) {
-    case METRIC_INNER_PRODUCT:
-      vec4 ? go(flat_f32_scan_kernel<METRIC_INNER_PRODUCT, true>) : go(flat_f32_scan_kernel<METRIC_INNER_PRODUCT, false>);
-      break;
-    case METRIC_COSINE:
-      vec4 ? go(flat_f32_scan_kernel<METRIC_COSINE, true>) : go(flat_f32_scan_kernel<METRIC_COSINE, false>);
-      break;
-    default:
-      vec4 ? go(flat_f32_scan_kernel<METRIC_L2, true>) : go(flat_f32_scan_kernel<METRIC_L2, false>);
-      break;
+  ProfScope ps(fused ? "coarse_f32_scan" : "flat_f32_scan", stream);
+  if (fused) {
+    vec4 ? go(flat_f32_scan_kernel<METRIC_L2, true, true>) : go(flat_f32_scan_kernel<METRIC_L2, false, true>);
+  } else {
+    switch (metric) {
+      case METRIC_INNER_PRODUCT:
+        vec4 ? go(flat_f32_scan_kernel<METRIC_INNER_PRODUCT, true>)
+             : go(flat_f32_scan_kernel<METRIC_INNER_PRODUCT, false>);
+        break;
+      case METRIC_COSINE:
+        vec4 ? go(flat_f32_scan_kernel<METRIC_COSINE, true>) : go(flat_f32_scan_kernel<METRIC_COSINE, false>);
+        break;
+      default:
+        vec4 ? go(flat_f32_scan_kernel<METRIC_L2, true>) : go(flat_f32_scan_kernel<METRIC_L2, false>);
+        break;
+    }
   }
   note_launch();
   if (splits > 1) {

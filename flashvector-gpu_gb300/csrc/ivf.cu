@@ -1,0 +1,341 @@
+// ivf.cu -- IVF-PQ and IVF-SQ8 inverted-list scans.
+//
+// Replaces launch_ivf_pq_search / launch_ivf_sq_search and their kernels
+// (ivf_pq_lookup.cu:14-444, ivf_quant_lookup.cu:18-327, ivf_rerank.cuh:49-160)
+// with the same inputs, clamps and result semantics:
+//   * top_k <= 256; nprobe clamped to [1, nlist];
+//     shortlist = rerank_k ? rerank_k : top_k, >= top_k, <= 10240;
+//     exact rerank when rerank_k != 1 and fp32 rows are present;
+//   * coarse probe: the nprobe nearest centroids by squared L2 accumulated
+//     with fmaf in dimension order (ivf_rerank.cuh:78-84) -- exact here, by
+//     (distance, list id);
+//   * PQ: residual LUT[m][c] = sum_sd fmaf(((q - centroid) - codeword)^2)
+//     per (query, list) in shared memory (ivf_pq_lookup.cu:150-162), ADC =
+//     the LUT entries of a row's codes added in sub-space order (:176-178);
+//     SQ8: sum_d fmaf over (q - centroid) - fmaf(code, scale, min)
+//     (ivf_quant_lookup.cu:83-87), L2 whatever the metric;
+//   * shortlist = the best `shortlist` (approx distance, id) keys; rerank
+//     with the reference's warp-order fp32 distance; the first top_k by
+//     (distance, id) are returned.
+// Because every distance is evaluated in the reference's operation order,
+// the results are bit-identical to the oracle's restatement.
+//
+// Machine mapping. The coarse probe is the exact flat scan kernel in its
+// fused-FMA mode (a Q x nlist tiled scan with a fused top-nprobe). The list
+// scan is one persistent launch: CTAs pull queries from a device work
+// counter and drain that query's (query, list) pairs: per pair the LUT (or
+// the query residual) is built in shared memory, the posting list is
+// streamed with 16-byte code loads (contiguous rows when the codes are laid
+// out list-major, gathered by id in the reference's layout), and a running
+// shortlist is kept in shared memory: rows whose key cannot beat the
+// current shortlist's worst key are dropped, the rest are appended to a
+// buffer that is bitonic-merged into the shortlist when it fills.
+#include "../../include/fv_bridge.h"
+#include "common.cuh"
+#include "kernels.h"
+#include "topk.cuh"
+
+namespace fv {
+
+namespace {
+
+constexpr int IVF_THREADS = 256;
+constexpr uint32_t IVF_BUF = 1024;         // candidate buffer entries
+constexpr uint32_t MAX_SHORTLIST = 10240;  // reference clamp (ivf_rerank.cuh:12)
+
+enum IvfMode { IVF_PQ = 0, IVF_SQ8 = 1 };
+
+struct IvfArgs {
+  const float* centroids;   // [nlist][dim]
+  const float* codebooks;   // PQ: [m][256][sub]
+  const float* sq_mins;     // SQ8: [dim]
+  const float* sq_scales;   // SQ8: [dim]
+  const uint8_t* codes;     // [N][code_bytes] by id, or by list position when list_major
+  const uint32_t* offsets;  // [nlist + 1]
+  const uint32_t* vec_ids;  // [N] ids in list order
+  const float* vectors;     // fp32 rows (rerank) or null
+  uint32_t num_vectors, dim, nlist, m_pq, sub_dim, code_bytes;
+  const float* queries;
+  uint32_t nq, top_k, nprobe, shortlist, list_major, do_rerank;
+  int metric;
+  const uint32_t* mask;
+  const GpuSearchResult* probes;  // [nq][nprobe] coarse result (id = list)
+  uint32_t* work;                 // work counter (zeroed before the launch)
+  GpuSearchResult* out;
+  uint32_t* status;
+  uint32_t keys_pow2;             // pow2(shortlist + IVF_BUF)
+};
+
+struct IvfSmem {
+  // [keys_pow2] u64 keys | LUT (PQ: m*256 f32) or residual+mins+scales (SQ8: 3*dim f32) | query (dim f32)
+  static size_t bytes(int mode, uint32_t keys_pow2, uint32_t dim, uint32_t m_pq) {
+    size_t b = (size_t)keys_pow2 * 8;
+    b += mode == IVF_PQ ? (size_t)m_pq * 256 * 4 : (size_t)3 * dim * 4;
+    b += (size_t)dim * 4;
+    return b + 64;
+  }
+};
+
+// PQ: ADC of one row from its code bytes; LUT rows of 256 floats.
+__device__ __forceinline__ float adc_row(const float* __restrict__ lut, const uint8_t* __restrict__ row, uint32_t m_pq,
+                                         bool vec16) {
+  float s = 0.f;
+  if (vec16) {
+    for (uint32_t m0 = 0; m0 < m_pq; m0 += 16) {
+      const uint4 w = __ldg(reinterpret_cast<const uint4*>(row + m0));
+      const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+      for (int b = 0; b < 16; ++b) {
+        const uint32_t c = (ws[b >> 2] >> ((b & 3) * 8)) & 0xFFu;
+        s = __fadd_rn(s, lut[(m0 + b) * 256 + c]);
+      }
+    }
+  } else {
+    for (uint32_t m = 0; m < m_pq; ++m) s = __fadd_rn(s, lut[m * 256 + __ldg(row + m)]);
+  }
+  return s;
+}
+
+// SQ8: squared L2 between the query residual and the decoded row.
+__device__ __forceinline__ float sq8_row(const float* __restrict__ qres, const float* __restrict__ mins,
+                                         const float* __restrict__ scales, const uint8_t* __restrict__ row,
+                                         uint32_t dim, bool vec16) {
+  float s = 0.f;
+  uint32_t d = 0;
+  if (vec16) {
+    for (; d + 16 <= dim; d += 16) {
+      const uint4 w = __ldg(reinterpret_cast<const uint4*>(row + d));
+      const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+      for (int b = 0; b < 16; ++b) {
+        const float c = (float)((ws[b >> 2] >> ((b & 3) * 8)) & 0xFFu);
+        const float rec = fmaf(c, scales[d + b], mins[d + b]);
+        const float t = qres[d + b] - rec;
+        s = fmaf(t, t, s);
+      }
+    }
+  }
+  for (; d < dim; ++d) {
+    const float rec = fmaf((float)__ldg(row + d), scales[d], mins[d]);
+    const float t = qres[d] - rec;
+    s = fmaf(t, t, s);
+  }
+  return s;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  uint64_t* keys = reinterpret_cast<uint64_t*>(smem);
+  float* tab = reinterpret_cast<float*>(smem + (size_t)a.keys_pow2 * 8);
+  float* qs = tab + (MODE == IVF_PQ ? (size_t)a.m_pq * 256 : (size_t)3 * a.dim);
+  __shared__ uint32_t s_q, s_cnt;
+  __shared__ uint64_t s_tau;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t S = a.shortlist;
+  const bool vec16 = (a.code_bytes % 16u) == 0 && ((uintptr_t)a.codes % 16u) == 0;
+  float* mins = tab + a.dim;      // SQ8 only
+  float* scales = tab + 2 * a.dim;
+
+  if (MODE == IVF_SQ8) {
+    for (uint32_t d = tid; d < a.dim; d += IVF_THREADS) {
+      mins[d] = __ldg(a.sq_mins + d);
+      scales[d] = __ldg(a.sq_scales + d);
+    }
+  }
+
+  while (true) {
+    __syncthreads();
+    if (tid == 0) s_q = atomicAdd(a.work, 1u);
+    __syncthreads();
+    const uint32_t q = s_q;
+    if (q >= a.nq) break;
+
+    const float* qv = a.queries + (size_t)q * a.dim;
+    for (uint32_t d = tid; d < a.dim; d += IVF_THREADS) qs[d] = __ldg(qv + d);
+    for (uint32_t i = tid; i < S; i += IVF_THREADS) keys[i] = kSentinelKey;
+    if (tid == 0) {
+      s_cnt = 0;
+      s_tau = kSentinelKey;
+    }
+    __syncthreads();
+
+    auto flush = [&]() {
+      // keys[0, S) sorted shortlist, keys[S, S + cnt) new candidates
+      const uint32_t cnt = s_cnt;
+      for (uint32_t i = S + cnt + tid; i < a.keys_pow2; i += IVF_THREADS) keys[i] = kSentinelKey;
+      __syncthreads();
+      block_bitonic_sort(keys, a.keys_pow2);
+      if (tid == 0) {
+        s_cnt = 0;
+        s_tau = keys[S - 1];
+      }
+      __syncthreads();
+    };
+
+    for (uint32_t p = 0; p < a.nprobe; ++p) {
+      const uint32_t l = a.probes[(size_t)q * a.nprobe + p].id;
+      if (l >= a.nlist) continue;  // uniform over the block
+      const float* cent = a.centroids + (size_t)l * a.dim;
+      if (MODE == IVF_PQ) {
+        const uint32_t entries = a.m_pq * 256;
+        for (uint32_t e = tid; e < entries; e += IVF_THREADS) {
+          const uint32_t m = e >> 8, c = e & 255u;
+          const float* cb = a.codebooks + ((size_t)m * 256 + c) * a.sub_dim;
+          float s = 0.f;
+          for (uint32_t sd = 0; sd < a.sub_dim; ++sd) {
+            const uint32_t d = m * a.sub_dim + sd;
+            const float t = (qs[d] - __ldg(cent + d)) - __ldg(cb + sd);
+            s = fmaf(t, t, s);
+          }
+          tab[e] = s;
+        }
+      } else {
+        for (uint32_t d = tid; d < a.dim; d += IVF_THREADS) tab[d] = qs[d] - __ldg(cent + d);
+      }
+      __syncthreads();
+
+      const uint32_t beg = __ldg(a.offsets + l), end = __ldg(a.offsets + l + 1);
+      for (uint32_t base = beg; base < end; base += IVF_THREADS) {
+        const uint32_t i = base + tid;
+        if (i < end) {
+          const uint32_t vid = __ldg(a.vec_ids + i);
+          if (mask_allows(a.mask, vid)) {
+            const uint8_t* row = a.codes + (size_t)(a.list_major ? i : vid) * a.code_bytes;
+            const float d = MODE == IVF_PQ ? adc_row(tab, row, a.m_pq, vec16)
+                                           : sq8_row(tab, mins, scales, row, a.dim, vec16);
+            if (d < kSentinelDist) {
+              const uint64_t key = make_key(d, vid);
+              if (key < s_tau) {
+                const uint32_t pos = atomicAdd(&s_cnt, 1u);
+                keys[S + pos] = key;
+              }
+            }
+          }
+        }
+        __syncthreads();
+        if (s_cnt > IVF_BUF - IVF_THREADS) flush();
+      }
+      __syncthreads();  // the table is rebuilt for the next list
+    }
+    flush();
+
+    if (a.do_rerank) {
+      for (uint32_t c = warp; c < S; c += IVF_THREADS / 32) {
+        const uint64_t key = keys[c];
+        if (key == kSentinelKey) continue;
+        const uint32_t vid = key_slot(key);
+        if (vid >= a.num_vectors) continue;
+        const float d = warp_metric_distance(qv, a.vectors + (size_t)vid * a.dim, a.dim, lane, (MetricType)a.metric);
+        if (lane == 0) keys[c] = make_key(d, vid);
+      }
+      const uint32_t p2 = next_pow2_dev(S);
+      for (uint32_t i = S + tid; i < p2; i += IVF_THREADS) keys[i] = kSentinelKey;
+      __syncthreads();
+      block_bitonic_sort(keys, p2);
+    }
+    for (uint32_t r = tid; r < a.top_k; r += IVF_THREADS)
+      a.out[(size_t)q * a.top_k + r] = key_to_result(r < S ? keys[r] : kSentinelKey, nullptr);
+  }
+}
+
+__global__ void relayout_codes_kernel(const uint8_t* __restrict__ by_id, const uint32_t* __restrict__ vec_ids,
+                                      uint32_t n, uint32_t row_bytes, uint8_t* __restrict__ by_list) {
+  const uint64_t total = (uint64_t)n * row_bytes;
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t pos = e / row_bytes, b = e % row_bytes;
+    by_list[e] = by_id[(uint64_t)__ldg(vec_ids + pos) * row_bytes + b];
+  }
+}
+
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+}  // namespace
+
+int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
+  if (L.nq == 0 || L.top_k == 0 || L.nlist == 0) return 0;
+  if (mode == IVF_PQ && L.m_pq == 0) return 0;
+  if (L.dim == 0) return 0;
+  const uint32_t top_k = std::min(L.top_k, (uint32_t)kMaxTopK);
+  uint32_t nprobe = L.nprobe == 0 ? 1u : L.nprobe;
+  nprobe = std::min(nprobe, L.nlist);
+  if (nprobe > (uint32_t)kMaxTopK) return FV_ERR_ARG;  // coarse selection keeps <= 256 lists
+  uint32_t shortlist = L.rerank_k == 0 ? top_k : L.rerank_k;
+  shortlist = std::max(shortlist, top_k);
+  shortlist = std::min(shortlist, MAX_SHORTLIST);
+  const bool do_rerank = L.rerank_k != 1u && L.vectors != nullptr;
+  if (mode == IVF_PQ && (L.sub_dim == 0 || L.m_pq * L.sub_dim > L.dim)) return FV_ERR_ARG;
+
+  // scratch: coarse heaps | probes | work counter
+  const FlatPlan cp = plan_flat_f32(L.nlist, L.nq, nprobe, 0);
+  const size_t coarse_bytes = align256(cp.scratch_bytes);
+  const size_t probe_bytes = align256((size_t)L.nq * nprobe * sizeof(GpuSearchResult));
+  uint8_t* scratch = static_cast<uint8_t*>(scratch_get(stream, coarse_bytes + probe_bytes + 256));
+  if (!scratch) return (int)cudaErrorMemoryAllocation;
+  GpuSearchResult* probes = reinterpret_cast<GpuSearchResult*>(scratch + coarse_bytes);
+  uint32_t* work = reinterpret_cast<uint32_t*>(scratch + coarse_bytes + probe_bytes);
+
+  int rc = launch_flat_f32_planned(cp, L.centroids, nullptr, L.nlist, L.dim, L.queries, L.nq, nprobe, METRIC_L2,
+                                   nullptr, probes, true, cp.scratch_bytes ? scratch : nullptr, stream);
+  if (rc != 0) return rc;
+  cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return (int)e;
+
+  IvfArgs a{};
+  a.centroids = L.centroids;
+  a.codebooks = L.codebooks;
+  a.sq_mins = L.sq_mins;
+  a.sq_scales = L.sq_scales;
+  a.codes = L.codes;
+  a.offsets = L.offsets;
+  a.vec_ids = L.vec_ids;
+  a.vectors = L.vectors;
+  a.num_vectors = L.num_vectors;
+  a.dim = L.dim;
+  a.nlist = L.nlist;
+  a.m_pq = L.m_pq;
+  a.sub_dim = L.sub_dim;
+  a.code_bytes = mode == IVF_PQ ? L.m_pq : L.dim;
+  a.queries = L.queries;
+  a.nq = L.nq;
+  a.top_k = top_k;
+  a.nprobe = nprobe;
+  a.shortlist = shortlist;
+  a.list_major = L.list_major ? 1u : 0u;
+  a.do_rerank = do_rerank ? 1u : 0u;
+  a.metric = (int)L.metric;
+  a.mask = L.mask;
+  a.probes = probes;
+  a.work = work;
+  a.out = L.out;
+  a.status = status_word();
+  a.keys_pow2 = next_pow2(shortlist + IVF_BUF);
+
+  const size_t smem = IvfSmem::bytes(mode, a.keys_pow2, L.dim, L.m_pq);
+  if (smem > 227 * 1024) return FV_ERR_ARG;
+  auto kern = mode == IVF_PQ ? ivf_scan_kernel<IVF_PQ> : ivf_scan_kernel<IVF_SQ8>;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, IVF_THREADS, smem);
+  const uint32_t grid = std::max(1u, std::min<uint32_t>(L.nq, (uint32_t)(std::max(1, per_sm) * device_sm_count())));
+  {
+    ProfScope ps(mode == IVF_PQ ? "ivf_pq_scan" : "ivf_sq8_scan", stream);
+    kern<<<grid, IVF_THREADS, smem, stream>>>(a);
+    note_launch();
+  }
+  return (int)cudaGetLastError();
+}
+
+int launch_relayout_codes(const uint8_t* by_id, const uint32_t* vec_ids, uint32_t n, uint32_t row_bytes,
+                          uint8_t* by_list, cudaStream_t stream) {
+  if (n == 0 || row_bytes == 0) return 0;
+  const uint64_t total = (uint64_t)n * row_bytes;
+  const uint32_t blocks = (uint32_t)std::min<uint64_t>((total + 255) / 256, 65535ull * 16);
+  relayout_codes_kernel<<<blocks, 256, 0, stream>>>(by_id, vec_ids, n, row_bytes, by_list);
+  note_launch();
+  return (int)cudaGetLastError();
+}
+
+}  // namespace fv

@@ -67,6 +67,16 @@ void* scratch_get(cudaStream_t stream, size_t bytes);
 int launch_fill_sentinel(GpuSearchResult* out, size_t count, cudaStream_t stream);
 
 // exact fp32 flat scan (flat_fp32.cu)
+struct FlatPlan {
+  uint32_t splits = 1, tiles_per_split = 0;
+  size_t scratch_bytes = 0;  // per-split heaps (0 when one split)
+};
+FlatPlan plan_flat_f32(uint32_t n, uint32_t nq, uint32_t k, uint32_t forced_splits);
+// fused = true accumulates fmaf(diff, diff, acc) (L2 only): the coarse quantizer
+int launch_flat_f32_planned(const FlatPlan& p, const float* vectors, const uint32_t* vec_ids, uint32_t n,
+                            uint32_t dim, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
+                            const uint32_t* mask, GpuSearchResult* out, bool fused, void* scratch,
+                            cudaStream_t stream);
 int launch_flat_f32(const float* vectors, const uint32_t* vec_ids, uint32_t n, uint32_t dim, const float* queries,
                     uint32_t nq, uint32_t k, MetricType metric, const uint32_t* mask, GpuSearchResult* out,
                     uint32_t forced_splits, cudaStream_t stream);
@@ -82,6 +92,28 @@ struct TcTables {
 };
 int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
                    const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream);
+
+// IVF-PQ / IVF-SQ8 search (ivf.cu)
+struct IvfLaunch {
+  const float* centroids;
+  const float* codebooks;   // PQ
+  const float* sq_mins;     // SQ8
+  const float* sq_scales;   // SQ8
+  const uint8_t* codes;
+  const uint32_t* offsets;
+  const uint32_t* vec_ids;
+  const float* vectors;
+  uint32_t num_vectors, dim, nlist, m_pq, sub_dim;
+  bool list_major;
+  const float* queries;
+  uint32_t nq, top_k, nprobe, rerank_k;
+  MetricType metric;
+  const uint32_t* mask;
+  GpuSearchResult* out;
+};
+int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream);  // mode 0 = PQ, 1 = SQ8
+int launch_relayout_codes(const uint8_t* by_id, const uint32_t* vec_ids, uint32_t n, uint32_t row_bytes,
+                          uint8_t* by_list, cudaStream_t stream);
 
 // reduced-precision table encoders (encode.cu)
 int launch_encode_fp16(const float* x, uint32_t n, uint32_t dim, uint32_t pd, uint16_t* out, float* norms,

@@ -44,6 +44,10 @@ class FvFp8GpuTables(C.Structure):
                 ("num_vectors", U32), ("dim", U32), ("padded_dim", U32)]
 
 
+class FvIvfOptions(C.Structure):
+    _fields_ = [("codes_list_major", U32), ("reserved", U32 * 3)]
+
+
 class FvScanOptions(C.Structure):
     _fields_ = [("overfetch", U32), ("boundary_fp64", U32), ("boundary_eps", F32), ("splits", U32)]
 
@@ -70,6 +74,11 @@ SIGNATURES = {
     "fv_flat_scan_batch_noalloc": (I32, [P, P, U32, U32, P, U32, U32, I32, P, P, P]),
     "cuda_compute_distances_warp": (I32, [P, P, U32, U32, U32, I32, P, P]),
     "cuda_bitonic_sort_test": (I32, [P, P, P, P, U32, P]),
+    "cuda_ivf_pq_search_batch": (I32, [P, P, U32, U32, U32, U32, I32, P, P, P]),
+    "cuda_ivf_sq_search_batch": (I32, [P, P, U32, U32, U32, U32, I32, P, P, P]),
+    "fv_ivf_pq_search_ex": (I32, [P, P, P, U32, U32, U32, U32, I32, P, P, P]),
+    "fv_ivf_sq_search_ex": (I32, [P, P, P, U32, U32, U32, U32, I32, P, P, P]),
+    "fv_ivf_relayout_codes": (I32, [P, P, U32, U32, P, P]),
     "cuda_fp16_tc_search_batch": (I32, [P, P, U32, U32, I32, P, P, P]),
     "fv_fp16_search_batch_ex": (I32, [P, P, U32, U32, I32, P, P, P, P]),
     "fv_fp8_search_batch": (I32, [P, P, U32, U32, I32, P, P, P, P]),

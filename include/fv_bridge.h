@@ -90,6 +90,42 @@ int fv_flat_scan_batch_noalloc(const float* d_vectors, const uint32_t* d_vec_ids
                                const uint32_t* d_valid_mask,
                                GpuSearchResult* d_out_results, void* stream);
 
+/* ---- IVF-PQ / IVF-SQ8 inverted-list scans -------------------------------
+ * Replace cuda_bridge.h:96-121 (ivf_pq_lookup.cu:450-473,
+ * ivf_quant_lookup.cu:1064-1083). Clamps as launch_ivf_pq_search
+ * (ivf_pq_lookup.cu:351-362): top_k <= 256, nprobe in [1, nlist],
+ * shortlist = rerank_k ? rerank_k : top_k (>= top_k, <= 10240), exact fp32
+ * rerank when rerank_k != 1 and tables->d_vectors is non-null. Coarse
+ * probe exact by (L2, list id); nprobe above 256 returns FV_ERR_ARG.
+ * Results are vector ids sorted by (distance, id). */
+int cuda_ivf_pq_search_batch(const IvfPqGpuTables* tables, const float* d_queries,
+                             uint32_t num_queries, uint32_t top_k, uint32_t nprobe,
+                             uint32_t rerank_k, MetricType metric,
+                             const uint32_t* d_valid_mask, GpuSearchResult* d_out_results,
+                             void* stream);
+int cuda_ivf_sq_search_batch(const IvfSqGpuTables* tables, const float* d_queries,
+                             uint32_t num_queries, uint32_t top_k, uint32_t nprobe,
+                             uint32_t rerank_k, MetricType metric,
+                             const uint32_t* d_valid_mask, GpuSearchResult* d_out_results,
+                             void* stream);
+/* Same searches with options (FvIvfOptions, may be NULL): list-major codes
+ * stream each posting list as contiguous 16-byte loads. */
+int fv_ivf_pq_search_ex(const IvfPqGpuTables* tables, const FvIvfOptions* options,
+                        const float* d_queries, uint32_t num_queries, uint32_t top_k,
+                        uint32_t nprobe, uint32_t rerank_k, MetricType metric,
+                        const uint32_t* d_valid_mask, GpuSearchResult* d_out_results,
+                        void* stream);
+int fv_ivf_sq_search_ex(const IvfSqGpuTables* tables, const FvIvfOptions* options,
+                        const float* d_queries, uint32_t num_queries, uint32_t top_k,
+                        uint32_t nprobe, uint32_t rerank_k, MetricType metric,
+                        const uint32_t* d_valid_mask, GpuSearchResult* d_out_results,
+                        void* stream);
+/* Gathers id-indexed code rows into list order:
+ * d_out[i] = d_codes_by_id[d_ivf_vec_ids[i]] (row_bytes each). */
+int fv_ivf_relayout_codes(const uint8_t* d_codes_by_id, const uint32_t* d_ivf_vec_ids,
+                          uint32_t num_vectors, uint32_t row_bytes, uint8_t* d_out_by_list,
+                          void* stream);
+
 /* ---- tensor-core flat scans --------------------------------------------
  * Replaces cuda_bridge.h:138-147 (ivf_quant_lookup.cu:1106-1123). Per
  * query the top_k (<= 256) rows by the fp16 tensor-core distance

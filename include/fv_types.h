@@ -105,6 +105,13 @@ typedef struct {
     uint32_t splits;         /* base-range splits per query block (0 = auto)   */
 } FvScanOptions;
 
+/* Options of the IVF extensions; no reference counterpart. */
+typedef struct {
+    uint32_t codes_list_major; /* 1: d_pq_codes / d_sq_codes row i belongs to list
+                                  position i (fv_ivf_relayout_codes), 0: row v = id v */
+    uint32_t reserved[3];
+} FvIvfOptions;
+
 #undef FV_ALIGN8
 
 #ifdef __cplusplus
