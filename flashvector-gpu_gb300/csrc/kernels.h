@@ -2,6 +2,7 @@
 // kernel translation units. Nothing here crosses the library boundary.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -90,6 +91,11 @@ struct TcTables {
   const float* vectors;  // [n][dim] fp32 rows for the rescore (optional)
   uint32_t n, dim, padded_dim;
 };
+struct TcScanArgs;
+cudaError_t dispatch_tc_scan_fp16(int kl, int metric, const CUtensorMap& ta, const CUtensorMap& tb,
+                                  const TcScanArgs& a, uint32_t grid, cudaStream_t stream);
+cudaError_t dispatch_tc_scan_fp8(int kl, int metric, const CUtensorMap& ta, const CUtensorMap& tb,
+                                 const TcScanArgs& a, uint32_t grid, cudaStream_t stream);
 int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
                    const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream);
 

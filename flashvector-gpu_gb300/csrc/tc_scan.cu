@@ -7,7 +7,9 @@
 // layout; the reference scores 16 queries x 64 rows per step with wmma and
 // re-streams the whole fp16 base set once per 16 queries.
 //
-// Machine mapping (one CTA per SM, 192 threads):
+// The scan kernel itself (tc_scan_kernel.cuh) is instantiated per precision
+// in tc_scan_fp16.cu / tc_scan_fp8.cu. Machine mapping (one CTA per SM,
+// 192 threads):
 //   warp 0    TMA producer: per K block, a 128-query tile (A) and a 256-row
 //             base tile (B), 128-byte-swizzled, into a STAGES-deep ring;
 //   warp 1    TMEM owner + single-thread tcgen05.mma issuer (M=128, N=256,
@@ -24,337 +26,11 @@
 #include <cudaTypedefs.h>
 
 #include "../../include/fv_bridge.h"
-#include "common.cuh"
-#include "kernels.h"
-#include "tc_ptx.cuh"
-#include "topk.cuh"
+#include "tc_scan_kernel.cuh"
 
 namespace fv {
 
 namespace {
-
-constexpr int TC_M = 128;                  // queries per CTA (TMEM lanes)
-constexpr int TC_N = 256;                  // base rows per tile (MMA N)
-constexpr int KB_BYTES = 128;              // K bytes per stage row (one 128B swizzle atom)
-constexpr int A_STAGE = TC_M * KB_BYTES;   // 16 KB
-constexpr int B_STAGE = TC_N * KB_BYTES;   // 32 KB
-constexpr int SCAN_THREADS = 192;
-
-struct TcScanArgs {
-  uint32_t n, nq, kblocks, nqb, splits, tiles_per_split;
-  int metric;
-  const float* xnorm;    // [n] ||x||^2 of the fp32 rows (L2, cosine)
-  const float* xscale;   // [n] per-row fp8 scale (FP8 only)
-  const float* qnorm;    // [nq] ||q||^2
-  const float* qscale;   // [nq] per-query fp8 scale (FP8 only)
-  const uint32_t* mask;
-  uint64_t* partial;     // [nq][splits][KL]
-  uint32_t* tau;         // [nq] shared bound on each query's kl-th distance (float_order)
-  uint32_t kl;           // heap entries used (<= KL); == shortlist when shared bounds are on
-  uint32_t share_tau;    // 1: CTAs of one query publish / read tau (kl == shortlist)
-  uint32_t* status;
-};
-
-template <int KL, int STAGES>
-struct ScanSmem {
-  static constexpr size_t a_off = 0;
-  static constexpr size_t b_off = a_off + (size_t)STAGES * A_STAGE;
-  static constexpr size_t heap_off = b_off + (size_t)STAGES * B_STAGE;
-  static constexpr size_t col_off = heap_off + (size_t)KL * TC_M * 8;   // [4 warps][2][TC_N] floats
-  static constexpr size_t cmask_off = col_off + 4 * 2 * TC_N * 4;       // [4 warps][8] words
-  static constexpr size_t bar_off = cmask_off + 4 * 8 * 4;              // barriers
-  static constexpr size_t nbars = 2 * STAGES + 5;
-  static constexpr size_t misc_off = bar_off + nbars * 8;
-  static constexpr size_t bytes = misc_off + 16 + 1024;                 // + alignment slack
-};
-
-__device__ __noinline__ void heap_sift(uint64_t* h, int kl, uint64_t key) {
-  // replace the root of a max-heap stored with stride TC_M
-  int i = 0;
-  while (true) {
-    int l = 2 * i + 1;
-    if (l >= kl) break;
-    uint64_t cv = h[l * TC_M];
-    int c = l;
-    if (l + 1 < kl) {
-      uint64_t rv = h[(l + 1) * TC_M];
-      if (rv > cv) { cv = rv; c = l + 1; }
-    }
-    if (cv <= key) break;
-    h[i * TC_M] = cv;
-    i = c;
-  }
-  h[i * TC_M] = key;
-}
-
-// v[j] for a lane-varying j without local memory: a 6-level select tree.
-__device__ __forceinline__ float select64(const float (&v)[64], int j) {
-  float t[32];
-#pragma unroll
-  for (int i = 0; i < 32; ++i) t[i] = (j & 1) ? v[2 * i + 1] : v[2 * i];
-#pragma unroll
-  for (int i = 0; i < 16; ++i) t[i] = (j & 2) ? t[2 * i + 1] : t[2 * i];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) t[i] = (j & 4) ? t[2 * i + 1] : t[2 * i];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) t[i] = (j & 8) ? t[2 * i + 1] : t[2 * i];
-#pragma unroll
-  for (int i = 0; i < 2; ++i) t[i] = (j & 16) ? t[2 * i + 1] : t[2 * i];
-  return (j & 32) ? t[1] : t[0];
-}
-
-template <bool FP8, int KL, int STAGES>
-__global__ void __launch_bounds__(SCAN_THREADS, 1)
-    tc_scan_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcScanArgs a) {
-  using L = ScanSmem<KL, STAGES>;
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  uint8_t* sA = sm + L::a_off;
-  uint8_t* sB = sm + L::b_off;
-  uint64_t* heap = reinterpret_cast<uint64_t*>(sm + L::heap_off);
-  float* colbuf = reinterpret_cast<float*>(sm + L::col_off);
-  uint32_t* colmask = reinterpret_cast<uint32_t*>(sm + L::cmask_off);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L::bar_off);
-  uint64_t* full = bars;
-  uint64_t* empty = bars + STAGES;
-  uint64_t* acc_full = bars + 2 * STAGES;
-  uint64_t* acc_empty = acc_full + 2;
-  uint64_t* mma_done = acc_empty + 2;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + L::misc_off);
-  volatile uint32_t* abort_flag = tmem_slot + 1;
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t qb = blockIdx.x % a.nqb, split = blockIdx.x / a.nqb;
-  const uint32_t ntiles = (a.n + TC_N - 1) / TC_N;
-  const uint32_t t_begin = split * a.tiles_per_split;
-  const uint32_t t_end = min(t_begin + a.tiles_per_split, ntiles);
-  const uint32_t my_tiles = t_end > t_begin ? t_end - t_begin : 0;
-
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; ++s) {
-      tc::mbar_init(&full[s], 1);
-      tc::mbar_init(&empty[s], 1);
-    }
-    for (int b = 0; b < 2; ++b) {
-      tc::mbar_init(&acc_full[b], 1);
-      tc::mbar_init(&acc_empty[b], 4);
-    }
-    tc::mbar_init(mma_done, 1);
-    *abort_flag = 0;
-    tc::fence_mbar_init();
-  }
-  if (warp == 1) {
-    tc::tmem_alloc(tmem_slot, 512);
-    tc::tc_fence_before();
-  }
-  __syncthreads();
-  tc::tc_fence_after();
-  const uint32_t tmem = *tmem_slot;
-
-  if (warp == 0) {
-    // ------------------------------------------------------ TMA producer
-    if (lane == 0) {
-      tc::prefetch_tmap(&tmA);
-      tc::prefetch_tmap(&tmB);
-      const uint64_t pol_a = tc::policy_evict_last();
-      const uint64_t pol_b = tc::policy_evict_first();
-      const int kb_elems = FP8 ? 128 : 64;
-      uint32_t stage = 0, phase = 0;
-      int32_t issued_parity[STAGES];
-#pragma unroll
-      for (int s = 0; s < STAGES; ++s) issued_parity[s] = -1;
-      bool ok = true;
-      for (uint32_t i = 0; ok && i < my_tiles; ++i) {
-        const int32_t row_b = (int32_t)((t_begin + i) * TC_N);
-        for (uint32_t kb = 0; kb < a.kblocks; ++kb) {
-          if (!tc::mbar_wait(&empty[stage], phase ^ 1, abort_flag, a.status)) {
-            ok = false;
-            break;
-          }
-          tc::mbar_arrive_expect_tx(&full[stage], A_STAGE + B_STAGE);
-          tc::tma_load_2d(sA + stage * A_STAGE, &tmA, &full[stage], (int32_t)(kb * kb_elems), (int32_t)(qb * TC_M),
-                          pol_a);
-          tc::tma_load_2d(sB + stage * B_STAGE, &tmB, &full[stage], (int32_t)(kb * kb_elems), row_b, pol_b);
-          issued_parity[stage] = (int32_t)phase;
-          if (++stage == STAGES) {
-            stage = 0;
-            phase ^= 1;
-          }
-        }
-      }
-      // drain: every copy issued must have landed before the CTA may exit
-      // (normally they all have; after an abort this waits a bounded time)
-      uint32_t no_abort = 0;
-#pragma unroll
-      for (int s = 0; s < STAGES; ++s)
-        if (issued_parity[s] >= 0)
-          tc::mbar_wait(&full[s], (uint32_t)issued_parity[s], &no_abort, a.status, 100000000ull);
-    }
-  } else if (warp == 1) {
-    // ------------------------------------------------------- MMA issuer
-    if (lane == 0) {
-      constexpr uint32_t idesc = tc::idesc_f32acc(0, 0, TC_M, TC_N);
-      uint32_t stage = 0, phase = 0;
-      bool ok = true;
-      for (uint32_t i = 0; ok && i < my_tiles; ++i) {
-        const uint32_t buf = i & 1, use = i >> 1;
-        if (!tc::mbar_wait(&acc_empty[buf], (use & 1) ^ 1, abort_flag, a.status)) break;
-        tc::tc_fence_after();
-        const uint32_t d_tmem = tmem + buf * TC_N;
-        for (uint32_t kb = 0; kb < a.kblocks; ++kb) {
-          if (!tc::mbar_wait(&full[stage], phase, abort_flag, a.status)) {
-            ok = false;
-            break;
-          }
-          tc::tc_fence_after();
-          const uint32_t a_base = tc::smem_addr(sA + stage * A_STAGE);
-          const uint32_t b_base = tc::smem_addr(sB + stage * B_STAGE);
-#pragma unroll
-          for (uint32_t kk = 0; kk < 4; ++kk) {
-            tc::mma<FP8>(d_tmem, tc::sdesc_k_sw128(a_base + kk * 32), tc::sdesc_k_sw128(b_base + kk * 32), idesc,
-                         (kb | kk) != 0);
-          }
-          tc::mma_commit(&empty[stage]);
-          if (++stage == STAGES) {
-            stage = 0;
-            phase ^= 1;
-          }
-        }
-        if (ok) tc::mma_commit(&acc_full[buf]);
-      }
-      tc::mma_commit(mma_done);
-    }
-  } else {
-    // --------------------------------------------------------- epilogue
-    const int quad = warp & 3;                    // TMEM lane quadrant of this warp
-    const int row = quad * 32 + lane;             // query row in the block
-    const uint32_t q = qb * TC_M + row;
-    const bool qvalid = q < a.nq;
-    uint64_t* h = heap + row;
-    const int kl = (int)a.kl;
-    for (int i = 0; i < kl; ++i) h[i * TC_M] = kSentinelKey;
-    // Shared bound: every CTA scanning query q publishes the distance of its
-    // kl-th best key once its heap is full; the minimum over CTAs bounds the
-    // query's global kl-th best distance from above, so any row farther
-    // than it cannot be in the shortlist and is skipped by every CTA.
-    float tau_d = kSentinelDist;
-    float published = kSentinelDist;
-    uint32_t* tau_ptr = (a.share_tau && qvalid) ? a.tau + q : nullptr;
-    const float qn = qvalid ? __ldg(a.qnorm + q) : 0.f;
-    const float qs = (FP8 && qvalid) ? __ldg(a.qscale + q) : 1.f;
-    float worst = kSentinelDist;
-    const int metric = a.metric;
-
-    // per-warp copy of the current tile's column data (norms, fp8 scales,
-    // mask words): staged by the warp itself, so the epilogue warps never
-    // wait on one another
-    float* cb = colbuf + (warp - 2) * 2 * TC_N;
-    uint32_t* cm = colmask + (warp - 2) * 8;
-    for (uint32_t i = 0; i < my_tiles; ++i) {
-      const uint32_t buf = i & 1, use = i >> 1;
-      const uint32_t v0 = (t_begin + i) * TC_N;
-      __syncwarp();
-      for (int c = lane; c < TC_N; c += 32) {
-        const uint32_t slot = v0 + c;
-        const bool in = slot < a.n;
-        cb[c] = (in && a.xnorm) ? __ldg(a.xnorm + slot) : 0.f;
-        if (FP8) cb[TC_N + c] = in ? __ldg(a.xscale + slot) : 0.f;
-      }
-      if (lane < 8) {
-        const uint32_t c0 = v0 + lane * 32;
-        uint32_t w = 0;
-        if (c0 < a.n) {
-          const uint32_t cnt = min(32u, a.n - c0);
-          w = cnt == 32 ? 0xFFFFFFFFu : ((1u << cnt) - 1u);
-          if (a.mask) w &= __ldg(a.mask + (c0 >> 5));
-        }
-        cm[lane] = w;
-      }
-      __syncwarp();
-      const uint32_t tau_raw = tau_ptr ? __ldcg(tau_ptr) : 0u;
-      if (!tc::mbar_wait(&acc_full[buf], use & 1, abort_flag, a.status)) break;
-      tc::tc_fence_after();
-      if (tau_ptr) tau_d = fminf(tau_d, order_float(tau_raw));
-
-      const uint32_t t_row = tmem + ((uint32_t)(quad * 32) << 16) + buf * TC_N;
-#pragma unroll 1
-      for (int c0 = 0; c0 < TC_N; c0 += 64) {
-        uint32_t ra[32], rb[32];
-        tc::tmem_ld32_async(t_row + c0, ra);
-        tc::tmem_ld32_async(t_row + c0 + 32, rb);
-        tc::tmem_wait_ld(ra);
-        tc::reg_fence(rb);
-        const uint64_t mw = qvalid ? ((uint64_t)cm[(c0 >> 5) + 1] << 32 | cm[c0 >> 5]) : 0ull;
-        if (mw == 0ull) continue;
-        // exact per-column distances (the same expressions the insertion
-        // test uses), reduced to their minimum: a 64-column batch whose
-        // minimum cannot beat the worst kept distance is skipped whole
-        float v[64];
-#pragma unroll
-        for (int j = 0; j < 64; ++j) {
-          float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
-          if (FP8) dot = dot * (qs * cb[TC_N + c0 + j]);
-          float dist;
-          if (metric == METRIC_INNER_PRODUCT) {
-            dist = -dot;
-          } else if (metric == METRIC_COSINE) {
-            dist = 1.0f - dot / (sqrtf(qn * cb[c0 + j]) + 1e-8f);
-          } else {
-            dist = fmaxf(0.f, fmaf(-2.0f, dot, qn + cb[c0 + j]));
-          }
-          v[j] = dist;
-        }
-        float m[32];
-#pragma unroll
-        for (int j = 0; j < 32; ++j) m[j] = fminf(v[j], v[j + 32]);
-#pragma unroll
-        for (int w = 16; w > 0; w >>= 1)
-#pragma unroll
-          for (int j = 0; j < w; ++j) m[j] = fminf(m[j], m[j + w]);
-        if (!(m[0] < worst && m[0] <= tau_d)) continue;
-        // columns that may enter: the warp walks them lane-parallel, one
-        // per lane per round, fetching v[j] with a depth-6 select tree
-        uint64_t pass = 0;
-#pragma unroll
-        for (int j = 0; j < 64; ++j) pass |= (uint64_t)(v[j] < worst && v[j] <= tau_d) << j;
-        pass &= mw;
-        while (pass) {
-          const int j = __ffsll((long long)pass) - 1;
-          pass &= pass - 1;
-          const float dist = select64(v, j);
-          if (dist < worst && dist <= tau_d) {
-            heap_sift(h, kl, make_key(dist, v0 + c0 + j));
-            const uint64_t root = h[0];
-            worst = root == kSentinelKey ? kSentinelDist : key_dist(root);
-          }
-        }
-      }
-      if (tau_ptr && worst < published) {
-        // heap full (worst < 1e30 only then): publish its kl-th distance
-        atomicMin(tau_ptr, float_order(worst));
-        published = worst;
-      }
-      tc::tc_fence_before();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&acc_empty[buf]);
-    }
-    if (qvalid) {
-      uint64_t* dst = a.partial + ((size_t)q * a.splits + split) * kl;
-      for (int i = 0; i < kl; ++i) dst[i] = h[i * TC_M];
-    }
-  }
-
-  __syncthreads();
-  if (warp == 1) {
-    // all MMAs must have retired before the accumulators are released; this
-    // wait ignores the abort flag (bounded by time only)
-    uint32_t no_abort = 0;
-    tc::mbar_wait(mma_done, 0, &no_abort, a.status, 100000000ull);
-    __syncwarp();
-    tc::tc_fence_after();
-    tc::tmem_dealloc(tmem, 512);
-  }
-}
 
 // ---------------------------------------------------------------------------
 // Query preparation: fp32 -> fp16 (round to nearest even, as the reference
@@ -366,13 +42,15 @@ template <bool FP8>
 __global__ void __launch_bounds__(256) tc_prep_queries_kernel(const float* __restrict__ q, uint32_t nq, uint32_t dim,
                                                               uint32_t pd, void* __restrict__ out,
                                                               float* __restrict__ qnorm, float* __restrict__ qscale,
-                                                              uint32_t* __restrict__ tau) {
+                                                              uint32_t* __restrict__ tslot, uint32_t kl,
+                                                              uint32_t stride) {
   const uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (qi >= nq) return;
   const float* src = q + (size_t)qi * dim;
+  // shared-bound slots: empty (all ones) for the kl used, 0 for the padding
+  for (uint32_t s = lane; s < stride; s += 32) tslot[(size_t)qi * stride + s] = s < kl ? 0xFFFFFFFFu : 0u;
   if (lane == 0) {
-    tau[qi] = float_order(kSentinelDist);
     float s = 0.f;
     for (uint32_t d = 0; d < dim; ++d) s = fmaf(src[d], src[d], s);
     qnorm[qi] = s;
@@ -554,29 +232,6 @@ bool encode_tmap(CUtensorMap* m, const void* ptr, bool fp8, uint64_t inner_elems
   return r == CUDA_SUCCESS;
 }
 
-template <bool FP8, int KL, int STAGES>
-cudaError_t launch_scan_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a, uint32_t grid,
-                               cudaStream_t stream) {
-  using L = ScanSmem<KL, STAGES>;
-  auto kern = tc_scan_kernel<FP8, KL, STAGES>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes);
-  if (e != cudaSuccess) return e;
-  kern<<<grid, SCAN_THREADS, L::bytes, stream>>>(ta, tb, a);
-  note_launch();
-  return cudaGetLastError();
-}
-
-template <bool FP8>
-cudaError_t dispatch_scan(int kl, const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a, uint32_t grid,
-                          cudaStream_t stream) {
-  switch (kl) {
-    case 16: return launch_scan_kernel<FP8, 16, 4>(ta, tb, a, grid, stream);
-    case 32: return launch_scan_kernel<FP8, 32, 3>(ta, tb, a, grid, stream);
-    case 48: return launch_scan_kernel<FP8, 48, 3>(ta, tb, a, grid, stream);
-    default: return launch_scan_kernel<FP8, 64, 3>(ta, tb, a, grid, stream);
-  }
-}
-
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 }  // namespace
@@ -605,23 +260,25 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   const size_t q_bytes = align_up((size_t)nq * t.padded_dim * elem, 1024);
   const size_t qn_bytes = align_up((size_t)nq * 4, 256);
   const size_t part_bytes = align_up((size_t)nq * splits * kl * 8, 256);
-  uint8_t* scratch = static_cast<uint8_t*>(scratch_get(stream, q_bytes + 3 * qn_bytes + part_bytes));
+  const uint32_t slot_stride = (kl + 3) / 4 * 4;
+  const size_t slot_bytes = align_up((size_t)nq * slot_stride * 4, 256);
+  uint8_t* scratch = static_cast<uint8_t*>(scratch_get(stream, q_bytes + 2 * qn_bytes + part_bytes + slot_bytes));
   if (!scratch) return (int)cudaErrorMemoryAllocation;
   void* qprep = scratch;
   float* qnorm = reinterpret_cast<float*>(scratch + q_bytes);
   float* qscale = reinterpret_cast<float*>(scratch + q_bytes + qn_bytes);
   uint64_t* partial = reinterpret_cast<uint64_t*>(scratch + q_bytes + 2 * qn_bytes);
-  uint32_t* tau = reinterpret_cast<uint32_t*>(scratch + q_bytes + 2 * qn_bytes + part_bytes);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(scratch + q_bytes + 2 * qn_bytes + part_bytes);
 
   {
     ProfScope ps(fp8 ? "tc_prep_queries_fp8" : "tc_prep_queries_fp16", stream);
     const uint32_t blocks = (nq * 32 + 255) / 256;
     if (fp8)
       tc_prep_queries_kernel<true><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm, qscale,
-                                                               tau);
+                                                               tslot, kl, slot_stride);
     else
       tc_prep_queries_kernel<false><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm,
-                                                                qscale, tau);
+                                                                qscale, tslot, kl, slot_stride);
     note_launch();
   }
 
@@ -630,13 +287,29 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
       !encode_tmap(&tb, t.base, fp8, t.padded_dim, t.n, (uint64_t)t.padded_dim * elem, TC_N))
     return FV_ERR_ARG;
 
-  TcScanArgs a{t.n,   nq,      kblocks, nqb, splits, tps, (int)metric, t.norms, t.scales, qnorm, qscale, mask, partial,
-               tau, kl,     kl == shortlist ? 1u : 0u, status_word()};
+  TcScanArgs a{};
+  a.n = t.n;
+  a.nq = nq;
+  a.kblocks = kblocks;
+  a.nqb = nqb;
+  a.splits = splits;
+  a.tiles_per_split = tps;
+  a.xnorm = t.norms;
+  a.xscale = t.scales;
+  a.qnorm = qnorm;
+  a.qscale = qscale;
+  a.mask = mask;
+  a.partial = partial;
+  a.tslot = tslot;
+  a.tslot_stride = slot_stride;
+  a.kl = kl;
+  a.share = kl == shortlist ? 1u : 0u;
+  a.status = status_word();
   cudaError_t e;
   {
     ProfScope ps(fp8 ? "tc_scan_fp8" : "tc_scan_fp16", stream);
-    e = fp8 ? dispatch_scan<true>((int)kl_tmpl, ta, tb, a, nqb * splits, stream)
-            : dispatch_scan<false>((int)kl_tmpl, ta, tb, a, nqb * splits, stream);
+    e = fp8 ? dispatch_tc_scan_fp8((int)kl_tmpl, (int)metric, ta, tb, a, nqb * splits, stream)
+            : dispatch_tc_scan_fp16((int)kl_tmpl, (int)metric, ta, tb, a, nqb * splits, stream);
   }
   if (e != cudaSuccess) return (int)e;
 

@@ -1,0 +1,389 @@
+// tc_scan_kernel.cuh -- the tcgen05 scan kernel template shared by the fp16
+// and fp8 translation units (tc_scan_fp16.cu, tc_scan_fp8.cu), which each
+// instantiate one precision so the two compile in parallel.
+//
+// Warp roles (192 threads, one CTA per SM):
+//   warp 0    TMA producer: per K block, a 128-query tile (A) and a 256-row
+//             base tile (B), 128-byte-swizzled, into a STAGES-deep ring;
+//   warp 1    TMEM owner + single-thread tcgen05.mma issuer (M=128, N=256,
+//             fp32 accumulators, two 256-column buffers so the epilogue of
+//             tile i overlaps the MMAs of tile i+1);
+//   warps 2-5 epilogue: thread r owns query r of the block (TMEM lane r),
+//             turns dot products into distances, applies the slot mask and
+//             keeps that query's best kl (distance, slot) keys in a shared-
+//             memory max-heap. No distance matrix ever reaches HBM.
+//
+// Shared bound. Every query owns kl global "slots"; a CTA that keeps a key
+// also lowers slot hash(row) of its query to the key's distance (red.min).
+// Each slot then holds a distance of a distinct real row, so the maximum
+// over the kl slots is >= the query's global kl-th best distance: a row
+// farther than it cannot be in the shortlist, and every CTA scanning the
+// query drops it. The maximum sits near rank kl * H(kl) of all rows scanned
+// so far, so after the first tiles almost no row reaches the heap.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_fp8.h>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "tc_ptx.cuh"
+#include "topk.cuh"
+
+namespace fv {
+
+constexpr int TC_M = 128;                  // queries per CTA (TMEM lanes)
+constexpr int TC_N = 256;                  // base rows per tile (MMA N)
+constexpr int KB_BYTES = 128;              // K bytes per stage row (one 128B swizzle atom)
+constexpr int A_STAGE = TC_M * KB_BYTES;   // 16 KB
+constexpr int B_STAGE = TC_N * KB_BYTES;   // 32 KB
+constexpr int SCAN_THREADS = 192;
+
+struct TcScanArgs {
+  uint32_t n, nq, kblocks, nqb, splits, tiles_per_split;
+  const float* xnorm;    // [n] ||x||^2 of the fp32 rows (L2, cosine)
+  const float* xscale;   // [n] per-row fp8 scale (FP8 only)
+  const float* qnorm;    // [nq] ||q||^2
+  const float* qscale;   // [nq] per-query fp8 scale (FP8 only)
+  const uint32_t* mask;
+  uint64_t* partial;     // [nq][splits][kl]
+  uint32_t* tslot;       // [nq][tslot_stride] shared-bound slots (float_order distances)
+  uint32_t tslot_stride; // kl rounded up to a multiple of 4 (padding slots hold 0)
+  uint32_t kl;           // heap entries used (<= KL); == shortlist when the bound is shared
+  uint32_t share;        // 1: the CTAs of a query share the slot bound (kl == shortlist)
+  uint32_t* status;
+};
+
+template <int KL, int STAGES>
+struct ScanSmem {
+  static constexpr size_t a_off = 0;
+  static constexpr size_t b_off = a_off + (size_t)STAGES * A_STAGE;
+  static constexpr size_t heap_off = b_off + (size_t)STAGES * B_STAGE;
+  static constexpr size_t col_off = heap_off + (size_t)KL * TC_M * 8;   // [4 warps][2][TC_N] floats
+  static constexpr size_t cmask_off = col_off + 4 * 2 * TC_N * 4;       // [4 warps][8] words
+  static constexpr size_t bar_off = cmask_off + 4 * 8 * 4;              // barriers
+  static constexpr size_t nbars = 2 * STAGES + 5;
+  static constexpr size_t misc_off = bar_off + nbars * 8;
+  static constexpr size_t bytes = misc_off + 16 + 1024;                 // + alignment slack
+};
+
+static __device__ __noinline__ void heap_sift(uint64_t* h, int kl, uint64_t key) {
+  // replace the root of a max-heap stored with stride TC_M
+  int i = 0;
+  while (true) {
+    int l = 2 * i + 1;
+    if (l >= kl) break;
+    uint64_t cv = h[l * TC_M];
+    int c = l;
+    if (l + 1 < kl) {
+      uint64_t rv = h[(l + 1) * TC_M];
+      if (rv > cv) { cv = rv; c = l + 1; }
+    }
+    if (cv <= key) break;
+    h[i * TC_M] = cv;
+    i = c;
+  }
+  h[i * TC_M] = key;
+}
+
+// v[j] for a lane-varying j without local memory: a 5-level select tree.
+static __device__ __forceinline__ float select32(const float* v, int j) {
+  float t[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) t[i] = (j & 1) ? v[2 * i + 1] : v[2 * i];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) t[i] = (j & 2) ? t[2 * i + 1] : t[2 * i];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) t[i] = (j & 4) ? t[2 * i + 1] : t[2 * i];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) t[i] = (j & 8) ? t[2 * i + 1] : t[2 * i];
+  return (j & 16) ? t[1] : t[0];
+}
+
+template <bool FP8, int KL, int STAGES, int METRIC>
+__global__ void __launch_bounds__(SCAN_THREADS, 1)
+    tc_scan_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcScanArgs a) {
+  using L = ScanSmem<KL, STAGES>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  uint8_t* sA = sm + L::a_off;
+  uint8_t* sB = sm + L::b_off;
+  uint64_t* heap = reinterpret_cast<uint64_t*>(sm + L::heap_off);
+  float* colbuf = reinterpret_cast<float*>(sm + L::col_off);
+  uint32_t* colmask = reinterpret_cast<uint32_t*>(sm + L::cmask_off);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L::bar_off);
+  uint64_t* full = bars;
+  uint64_t* empty = bars + STAGES;
+  uint64_t* acc_full = bars + 2 * STAGES;
+  uint64_t* acc_empty = acc_full + 2;
+  uint64_t* mma_done = acc_empty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + L::misc_off);
+  volatile uint32_t* abort_flag = tmem_slot + 1;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t qb = blockIdx.x % a.nqb, split = blockIdx.x / a.nqb;
+  const uint32_t ntiles = (a.n + TC_N - 1) / TC_N;
+  const uint32_t t_begin = split * a.tiles_per_split;
+  const uint32_t t_end = min(t_begin + a.tiles_per_split, ntiles);
+  const uint32_t my_tiles = t_end > t_begin ? t_end - t_begin : 0;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&acc_full[b], 1);
+      tc::mbar_init(&acc_empty[b], 4);
+    }
+    tc::mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    tc::fence_mbar_init();
+  }
+  if (warp == 1) {
+    tc::tmem_alloc(tmem_slot, 512);
+    tc::tc_fence_before();
+  }
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------------ TMA producer
+    if (lane == 0) {
+      tc::prefetch_tmap(&tmA);
+      tc::prefetch_tmap(&tmB);
+      const uint64_t pol_a = tc::policy_evict_last();
+      const uint64_t pol_b = tc::policy_evict_first();
+      const int kb_elems = FP8 ? 128 : 64;
+      uint32_t stage = 0, phase = 0;
+      int32_t issued_parity[STAGES];
+#pragma unroll
+      for (int s = 0; s < STAGES; ++s) issued_parity[s] = -1;
+      bool ok = true;
+      for (uint32_t i = 0; ok && i < my_tiles; ++i) {
+        const int32_t row_b = (int32_t)((t_begin + i) * TC_N);
+        for (uint32_t kb = 0; kb < a.kblocks; ++kb) {
+          if (!tc::mbar_wait(&empty[stage], phase ^ 1, abort_flag, a.status)) {
+            ok = false;
+            break;
+          }
+          tc::mbar_arrive_expect_tx(&full[stage], A_STAGE + B_STAGE);
+          tc::tma_load_2d(sA + stage * A_STAGE, &tmA, &full[stage], (int32_t)(kb * kb_elems), (int32_t)(qb * TC_M),
+                          pol_a);
+          tc::tma_load_2d(sB + stage * B_STAGE, &tmB, &full[stage], (int32_t)(kb * kb_elems), row_b, pol_b);
+          issued_parity[stage] = (int32_t)phase;
+          if (++stage == STAGES) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+      // drain: every copy issued must have landed before the CTA may exit
+      // (normally they all have; after an abort this waits a bounded time)
+      uint32_t no_abort = 0;
+#pragma unroll
+      for (int s = 0; s < STAGES; ++s)
+        if (issued_parity[s] >= 0)
+          tc::mbar_wait(&full[s], (uint32_t)issued_parity[s], &no_abort, a.status, 100000000ull);
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------- MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc::idesc_f32acc(0, 0, TC_M, TC_N);
+      uint32_t stage = 0, phase = 0;
+      bool ok = true;
+      for (uint32_t i = 0; ok && i < my_tiles; ++i) {
+        const uint32_t buf = i & 1, use = i >> 1;
+        if (!tc::mbar_wait(&acc_empty[buf], (use & 1) ^ 1, abort_flag, a.status)) break;
+        tc::tc_fence_after();
+        const uint32_t d_tmem = tmem + buf * TC_N;
+        for (uint32_t kb = 0; kb < a.kblocks; ++kb) {
+          if (!tc::mbar_wait(&full[stage], phase, abort_flag, a.status)) {
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          const uint32_t a_base = tc::smem_addr(sA + stage * A_STAGE);
+          const uint32_t b_base = tc::smem_addr(sB + stage * B_STAGE);
+#pragma unroll
+          for (uint32_t kk = 0; kk < 4; ++kk) {
+            tc::mma<FP8>(d_tmem, tc::sdesc_k_sw128(a_base + kk * 32), tc::sdesc_k_sw128(b_base + kk * 32), idesc,
+                         (kb | kk) != 0);
+          }
+          tc::mma_commit(&empty[stage]);
+          if (++stage == STAGES) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+        if (ok) tc::mma_commit(&acc_full[buf]);
+      }
+      tc::mma_commit(mma_done);
+    }
+  } else {
+    // --------------------------------------------------------- epilogue
+    const int quad = warp & 3;                    // TMEM lane quadrant of this warp
+    const int row = quad * 32 + lane;             // query row in the block
+    const uint32_t q = qb * TC_M + row;
+    const bool qvalid = q < a.nq;
+    uint64_t* h = heap + row;
+    const int kl = (int)a.kl;
+    for (int i = 0; i < kl; ++i) h[i * TC_M] = kSentinelKey;
+    const float qn = qvalid ? __ldg(a.qnorm + q) : 0.f;
+    const float qs = (FP8 && qvalid) ? __ldg(a.qscale + q) : 1.f;
+    float worst = kSentinelDist;  // this CTA's kl-th best distance (1e30 until the heap is full)
+    float bound = kSentinelDist;  // shared bound: max over the query's slots
+    uint32_t* slots = (a.share && qvalid) ? a.tslot + (size_t)q * a.tslot_stride : nullptr;
+
+    auto keep = [&](float dist, uint32_t slot) {
+      heap_sift(h, kl, make_key(dist, slot));
+      const uint64_t root = h[0];
+      worst = root == kSentinelKey ? kSentinelDist : key_dist(root);
+      if (slots) atomicMin(slots + __umulhi(slot * 2654435761u, (uint32_t)kl), float_order(dist));
+    };
+
+    // per-warp copy of the current tile's column data (norms, fp8 scales,
+    // mask words): staged by the warp itself, so the epilogue warps never
+    // wait on one another
+    float* cb = colbuf + (warp - 2) * 2 * TC_N;
+    uint32_t* cm = colmask + (warp - 2) * 8;
+    for (uint32_t i = 0; i < my_tiles; ++i) {
+      const uint32_t buf = i & 1, use = i >> 1;
+      const uint32_t v0 = (t_begin + i) * TC_N;
+      __syncwarp();
+      for (int c = lane; c < TC_N; c += 32) {
+        const uint32_t slot = v0 + c;
+        const bool in = slot < a.n;
+        if (METRIC != METRIC_INNER_PRODUCT) cb[c] = in ? __ldg(a.xnorm + slot) : 0.f;
+        if (FP8) cb[TC_N + c] = in ? __ldg(a.xscale + slot) : 0.f;
+      }
+      if (lane < 8) {
+        const uint32_t c0 = v0 + lane * 32;
+        uint32_t w = 0;
+        if (c0 < a.n) {
+          const uint32_t cnt = min(32u, a.n - c0);
+          w = cnt == 32 ? 0xFFFFFFFFu : ((1u << cnt) - 1u);
+          if (a.mask) w &= __ldg(a.mask + (c0 >> 5));
+        }
+        cm[lane] = w;
+      }
+      __syncwarp();
+      // the shared bound, loaded before the accumulator wait hides its latency
+      uint32_t smax = 0;
+      if (slots)
+        for (uint32_t s4 = 0; s4 < a.tslot_stride; s4 += 4) {
+          const uint4 w = __ldcg(reinterpret_cast<const uint4*>(slots + s4));
+          smax = max(smax, max(max(w.x, w.y), max(w.z, w.w)));
+        }
+      if (!tc::mbar_wait(&acc_full[buf], use & 1, abort_flag, a.status)) break;
+      tc::tc_fence_after();
+      if (slots && smax != 0xFFFFFFFFu) bound = fminf(bound, order_float(smax));
+
+      const uint32_t t_row = tmem + ((uint32_t)(quad * 32) << 16) + buf * TC_N;
+#pragma unroll 1
+      for (int c0 = 0; c0 < TC_N; c0 += 64) {
+        uint32_t ra[32], rb[32];
+        tc::tmem_ld32_async(t_row + c0, ra);
+        tc::tmem_ld32_async(t_row + c0 + 32, rb);
+        tc::tmem_wait_ld(ra);
+        tc::reg_fence(rb);
+        const uint64_t mw = qvalid ? ((uint64_t)cm[(c0 >> 5) + 1] << 32 | cm[c0 >> 5]) : 0ull;
+        if (mw == 0ull) continue;
+        // exact per-column distances (the expressions the insertion test
+        // uses); v[0..32) columns c0.., v[32..64) columns c0+32..
+        float v[64];
+#pragma unroll
+        for (int j = 0; j < 64; ++j) {
+          float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
+          if (FP8) dot = dot * (qs * cb[TC_N + c0 + j]);
+          if (METRIC == METRIC_INNER_PRODUCT)
+            v[j] = -dot;
+          else if (METRIC == METRIC_COSINE)
+            v[j] = 1.0f - dot / (sqrtf(qn * cb[c0 + j]) + 1e-8f);
+          else
+            v[j] = fmaxf(0.f, fmaf(-2.0f, dot, qn + cb[c0 + j]));
+        }
+        // pairwise minima, then a min tree: a 64-column batch whose minimum
+        // cannot enter is skipped whole (the common case once warm)
+        float m1[32], m[16];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) m1[j] = fminf(v[j], v[j + 32]);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) m[j] = fminf(m1[j], m1[j + 16]);
+#pragma unroll
+        for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+          for (int j = 0; j < w; ++j) m[j] = fminf(m[j], m[j + w]);
+        if (!(m[0] < worst && m[0] <= bound)) continue;
+        // pairs (j, j+32) that may enter, walked lane-parallel
+        uint32_t pass = 0;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) pass |= (uint32_t)(m1[j] < worst && m1[j] <= bound) << j;
+        pass &= (uint32_t)mw | (uint32_t)(mw >> 32);
+        while (pass) {
+          const int j = __ffs(pass) - 1;
+          pass &= pass - 1;
+          const float dlo = select32(v, j);
+          const float dhi = select32(v + 32, j);
+          if (((mw >> j) & 1ull) && dlo < worst && dlo <= bound) keep(dlo, v0 + c0 + j);
+          if (((mw >> (j + 32)) & 1ull) && dhi < worst && dhi <= bound) keep(dhi, v0 + c0 + j + 32);
+        }
+      }
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&acc_empty[buf]);
+    }
+    if (qvalid) {
+      uint64_t* dst = a.partial + ((size_t)q * a.splits + split) * kl;
+      for (int i = 0; i < kl; ++i) dst[i] = h[i * TC_M];
+    }
+  }
+
+  __syncthreads();
+  if (warp == 1) {
+    // all MMAs must have retired before the accumulators are released; this
+    // wait ignores the abort flag (bounded by time only)
+    uint32_t no_abort = 0;
+    tc::mbar_wait(mma_done, 0, &no_abort, a.status, 100000000ull);
+    __syncwarp();
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, 512);
+  }
+}
+
+
+template <bool FP8, int KL, int STAGES, int METRIC>
+cudaError_t launch_scan_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a, uint32_t grid,
+                               cudaStream_t stream) {
+  using L = ScanSmem<KL, STAGES>;
+  auto kern = tc_scan_kernel<FP8, KL, STAGES, METRIC>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, SCAN_THREADS, L::bytes, stream>>>(ta, tb, a);
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <bool FP8, int METRIC>
+cudaError_t dispatch_scan_kl(int kl, const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a, uint32_t grid,
+                             cudaStream_t stream) {
+  switch (kl) {
+    case 16: return launch_scan_kernel<FP8, 16, 4, METRIC>(ta, tb, a, grid, stream);
+    case 32: return launch_scan_kernel<FP8, 32, 3, METRIC>(ta, tb, a, grid, stream);
+    case 48: return launch_scan_kernel<FP8, 48, 3, METRIC>(ta, tb, a, grid, stream);
+    default: return launch_scan_kernel<FP8, 64, 3, METRIC>(ta, tb, a, grid, stream);
+  }
+}
+
+template <bool FP8>
+cudaError_t dispatch_scan(int kl, int metric, const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a,
+                          uint32_t grid, cudaStream_t stream) {
+  switch (metric) {
+    case METRIC_INNER_PRODUCT: return dispatch_scan_kl<FP8, METRIC_INNER_PRODUCT>(kl, ta, tb, a, grid, stream);
+    case METRIC_COSINE: return dispatch_scan_kl<FP8, METRIC_COSINE>(kl, ta, tb, a, grid, stream);
+    default: return dispatch_scan_kl<FP8, METRIC_L2>(kl, ta, tb, a, grid, stream);
+  }
+}
+
+}  // namespace fv
