@@ -26,7 +26,7 @@ LIB = PKG / "fvgb300" / "libfvgb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills", f"-I{ROOT / 'include'}"]
-CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", f"-I{ROOT / 'include'}", "-I/usr/local/cuda/include"]
+CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", f"-I{ROOT / 'include'}", "-I/usr/local/cuda/include"]
 
 
 def _nvcc() -> str:

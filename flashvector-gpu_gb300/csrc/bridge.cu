@@ -340,6 +340,33 @@ int fv_ivf_relayout_codes(const uint8_t* d_codes_by_id, const uint32_t* d_ivf_ve
                                    (cudaStream_t)stream);
 }
 
+// ---------------------------------------------------------- index build
+int fv_build_pq_encode(const float* d_residuals, uint32_t num_vectors, uint32_t dim, uint32_t m_pq,
+                       const float* d_codebooks, uint8_t* d_out_codes, void* stream) {
+  if (num_vectors && (!d_residuals || !d_codebooks || !d_out_codes)) return FV_ERR_NULL;
+  if (num_vectors == 0) return 0;
+  return fv::launch_pq_encode(d_residuals, num_vectors, dim, m_pq, d_codebooks, d_out_codes, (cudaStream_t)stream);
+}
+int fv_build_sq8(const float* d_residuals, uint32_t num_vectors, uint32_t dim, float* d_out_mins,
+                 float* d_out_scales, uint8_t* d_out_codes, void* stream) {
+  if (!d_residuals || !d_out_mins || !d_out_scales || (num_vectors && !d_out_codes)) return FV_ERR_NULL;
+  cudaStream_t s = (cudaStream_t)stream;
+  uint32_t* work = static_cast<uint32_t*>(fv::scratch_get(s, (size_t)dim * 8));
+  if (!work) return (int)cudaErrorMemoryAllocation;
+  int rc = fv::launch_sq8_fit(d_residuals, num_vectors, dim, d_out_mins, d_out_scales, work, s);
+  if (rc || num_vectors == 0) return rc;
+  return fv::launch_sq8_encode(d_residuals, num_vectors, dim, d_out_mins, d_out_scales, d_out_codes, s);
+}
+int fv_build_ivf_lists(const GpuSearchResult* d_assign, uint32_t num_vectors, uint32_t nlist, uint32_t* d_out_offsets,
+                       uint32_t* d_out_vec_ids, void* stream) {
+  if (!d_out_offsets || (num_vectors && (!d_assign || !d_out_vec_ids))) return FV_ERR_NULL;
+  if (nlist == 0) return FV_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  uint32_t* work = static_cast<uint32_t*>(fv::scratch_get(s, (size_t)nlist * 4));
+  if (!work) return (int)cudaErrorMemoryAllocation;
+  return fv::launch_build_lists(d_assign, num_vectors, nlist, d_out_offsets, d_out_vec_ids, work, s);
+}
+
 // ------------------------------------------------------------- fixtures
 int cuda_compute_distances_warp(const float* d_queries, const float* d_dataset, uint32_t num_queries,
                                 uint32_t num_vectors, uint32_t dim, MetricType metric, float* d_out_distances,

@@ -1,0 +1,761 @@
+// engine.cpp -- host orchestration of the scan path: the reference's
+// GpuVectorIndex (crates/engine/src/index.rs:131-2634) restated in C++ for the
+// scan engines only (exact flat, fp16 / fp8 tensor core, IVF-PQ, IVF-SQ8).
+//
+// Mirrors, per reference method:
+//   build           index.rs:328-576   (cosine rows normalised on the host,
+//                                       normalize_slice_in_place :30-38;
+//                                       tables built on the GPU: fp16 / fp8
+//                                       encoders, k-means, PQ, SQ8, lists)
+//   add_vectors     index.rs:647-694   (live-insert ("delta") buffer, logical
+//                                       ids from next_logical_id, device copy
+//                                       regrown to the next power of two >= 256)
+//   delete_ids      index.rs:583-643   (tombstones; main slots cleared in the
+//                                       validity words)
+//   batch_search_*  index.rs:1979-2237 (query prep, slot mask = user mask AND
+//                                       live, main search on a pooled stream,
+//                                       delta flat scan concurrently on the
+//                                       delta stream, D2H, stable merge)
+//   finish_delta_merge index.rs:1353-1387, build_slot_mask_words :1264-1292,
+//   build_delta_mask_words :1294-1316, MetricsTracker metrics.rs:21-97.
+// Differences: the batch size is not capped at 1024 and masks are not capped
+// at 2M ids (streams.rs:12-20); k-means seeds from a seeded sample rather than
+// k-means++, and an empty cluster keeps its centroid.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <shared_mutex>
+#include <unordered_set>
+#include <vector>
+
+#include "../../include/fv_bridge.h"
+#include "kernels.h"
+
+namespace fv {
+
+namespace {
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  int alloc(size_t count) {
+    release();
+    if (count == 0) return 0;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return (int)e;
+    }
+    n = count;
+    return 0;
+  }
+  int ensure(size_t count) { return count <= n ? 0 : alloc(count); }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+template <class T>
+struct PinnedBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  int ensure(size_t count) {
+    if (count <= n) return 0;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    if (cudaMallocHost(&p, std::max<size_t>(count, 1) * sizeof(T)) != cudaSuccess) return (int)cudaErrorMemoryAllocation;
+    n = count;
+    return 0;
+  }
+};
+
+uint64_t splitmix(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// `count` distinct indices of [0, n) (Floyd's algorithm), ascending.
+std::vector<uint32_t> sample_rows(uint32_t n, uint32_t count, uint64_t seed) {
+  count = std::min(count, n);
+  std::unordered_set<uint32_t> pick;
+  uint64_t s = seed ^ 0xA5A5A5A5DEADBEEFull;
+  for (uint32_t j = n - count; j < n; ++j) {
+    const uint32_t t = (uint32_t)(splitmix(s) % ((uint64_t)j + 1));
+    if (!pick.insert(t).second) pick.insert(j);
+  }
+  std::vector<uint32_t> out(pick.begin(), pick.end());
+  std::sort(out.begin(), out.end());
+  return out;
+}
+
+// normalize_slice_in_place (index.rs:30-38)
+void normalize_rows(float* v, size_t n, uint32_t dim) {
+  for (size_t i = 0; i < n; ++i) {
+    float* r = v + i * dim;
+    float s = 0.f;
+    for (uint32_t d = 0; d < dim; ++d) s = s + r[d] * r[d];
+    float norm = std::sqrt(s);
+    if (norm < 1e-8f) norm = 1e-8f;
+    const float inv = 1.0f / norm;
+    for (uint32_t d = 0; d < dim; ++d) r[d] = r[d] * inv;
+  }
+}
+
+struct Stream {
+  cudaStream_t s = nullptr;
+  std::mutex mu;
+  DevBuf<float> q;
+  DevBuf<GpuSearchResult> res;
+  DevBuf<uint32_t> mask;
+  PinnedBuf<float> hq;
+  PinnedBuf<GpuSearchResult> hres;
+  cudaEvent_t ready = nullptr;  // queries resident on the device
+};
+
+struct Delta {
+  std::vector<float> vectors;
+  std::vector<uint32_t> ids;
+  DevBuf<float> d_vectors;
+  DevBuf<uint32_t> d_ids;
+  DevBuf<uint32_t> d_mask;
+  DevBuf<GpuSearchResult> d_res;
+  PinnedBuf<GpuSearchResult> h_res;
+  size_t capacity = 0;
+  uint32_t len() const { return (uint32_t)ids.size(); }
+};
+
+}  // namespace
+
+class Index {
+ public:
+  explicit Index(const FvIndexConfig& c) : cfg_(c), start_(std::chrono::steady_clock::now()) {
+    if (cfg_.build_flags == 0) cfg_.build_flags = FV_BUILD_FP16 | FV_BUILD_IVF_PQ | FV_BUILD_IVF_SQ8;
+    if (cfg_.kmeans_iters == 0) cfg_.kmeans_iters = 10;
+    if (cfg_.pq_iters == 0) cfg_.pq_iters = 10;
+    const uint32_t ns = cfg_.streams ? cfg_.streams : 4;
+    streams_.resize(ns);
+    for (auto& st : streams_) {
+      st = std::make_unique<Stream>();
+      cudaStreamCreateWithFlags(&st->s, cudaStreamNonBlocking);
+      cudaEventCreateWithFlags(&st->ready, cudaEventDisableTiming);
+    }
+    cudaStreamCreateWithFlags(&delta_stream_, cudaStreamNonBlocking);
+  }
+  ~Index() {
+    cudaDeviceSynchronize();
+    for (auto& st : streams_) {
+      fv_release_stream_scratch(st->s);
+      cudaEventDestroy(st->ready);
+      cudaStreamDestroy(st->s);
+    }
+    fv_release_stream_scratch(delta_stream_);
+    cudaStreamDestroy(delta_stream_);
+  }
+
+  int build(const float* host, uint32_t n);
+  int add(const float* host, uint32_t n, uint32_t* out_ids);
+  int remove(const uint32_t* ids, uint32_t n, uint32_t* out_deleted);
+  int search(const FvSearchParams& p, const float* q, uint32_t nq, bool device_queries, const uint32_t* user_mask,
+             uint32_t mask_words, GpuSearchResult* out);
+  void stats(FvLatencyStats* s);
+  void info(FvIndexInfo* i);
+  int export_ivf(uint32_t what, void* host_out, size_t bytes);
+
+ private:
+  int build_ivf(cudaStream_t s);
+  int kmeans(const float* d_x, uint32_t n, uint32_t dim, uint32_t k, uint32_t iters, uint64_t seed, float* d_cent,
+             cudaStream_t s);
+  int assign_rows(const float* d_x, uint32_t n, uint32_t dim, const float* d_cent, uint32_t k, GpuSearchResult* out,
+                  cudaStream_t s);
+  void slot_mask(const uint32_t* user, uint32_t words, std::vector<uint32_t>& out, bool& use) const;
+  void delta_mask(const uint32_t* user, uint32_t words, std::vector<uint32_t>& out, bool& use) const;
+  void record(double seconds, uint32_t nq);
+
+  FvIndexConfig cfg_;
+  std::vector<std::unique_ptr<Stream>> streams_;
+  std::atomic<uint32_t> rr_{0};
+  cudaStream_t delta_stream_ = nullptr;
+  std::mutex delta_mu_;
+  mutable std::shared_mutex state_mu_;  // searches shared; build / add / delete exclusive
+
+  bool built_ = false;
+  uint32_t n_ = 0;
+  uint32_t pd16_ = 0, pd8_ = 0, nlist_ = 0;
+  DevBuf<float> vectors_, norms16_, fp8_scales_, fp8_norms_;
+  DevBuf<uint16_t> fp16_;
+  DevBuf<uint8_t> fp8_;
+  DevBuf<float> centroids_, codebooks_, sq_mins_, sq_scales_;
+  DevBuf<uint8_t> pq_codes_, pq_codes_lm_, sq_codes_, sq_codes_lm_;
+  DevBuf<uint32_t> offsets_, vec_ids_;
+  DevBuf<uint32_t> valid_words_;
+  std::vector<uint32_t> main_valid_;
+  std::unordered_set<uint32_t> tombstones_;
+  uint32_t next_id_ = 0;
+  Delta delta_;
+
+  std::mutex metrics_mu_;
+  std::vector<double> lat_us_;
+  uint64_t total_queries_ = 0;
+  std::chrono::steady_clock::time_point start_;
+};
+
+// ------------------------------------------------------------------ build
+int Index::assign_rows(const float* d_x, uint32_t n, uint32_t dim, const float* d_cent, uint32_t k,
+                       GpuSearchResult* out, cudaStream_t s) {
+  // nearest centroid of every row: the exact flat scan with k = 1, in
+  // chunks so that the per-stream scratch stays small
+  const uint32_t chunk = 1u << 20;
+  for (uint32_t b = 0; b < n; b += chunk) {
+    const uint32_t cnt = std::min(chunk, n - b);
+    int rc = launch_flat_f32(d_cent, nullptr, k, dim, d_x + (size_t)b * dim, cnt, 1, METRIC_L2, nullptr, out + b, 0,
+                             s);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+int Index::kmeans(const float* d_x, uint32_t n, uint32_t dim, uint32_t k, uint32_t iters, uint64_t seed,
+                  float* d_cent, cudaStream_t s) {
+  std::vector<uint32_t> init = sample_rows(n, k, seed);
+  DevBuf<uint32_t> rows;
+  DevBuf<GpuSearchResult> assign;
+  DevBuf<uint32_t> counts;
+  DevBuf<double> sums;
+  int rc = rows.alloc(init.size());
+  if (!rc) rc = assign.alloc(n);
+  if (!rc) rc = counts.alloc(k);
+  if (!rc) rc = sums.alloc((size_t)k * dim);
+  if (rc) return rc;
+  cudaMemcpyAsync(rows.p, init.data(), init.size() * 4, cudaMemcpyHostToDevice, s);
+  rc = launch_gather_rows(d_x, rows.p, (uint32_t)init.size(), dim, d_cent, s);
+  if (rc) return rc;
+  for (uint32_t it = 0; it < iters; ++it) {
+    rc = assign_rows(d_x, n, dim, d_cent, k, assign.p, s);
+    if (!rc) rc = launch_kmeans_update(d_x, n, dim, assign.p, k, d_cent, counts.p, sums.p, s);
+    if (rc) return rc;
+  }
+  return (int)cudaStreamSynchronize(s);
+}
+
+int Index::build_ivf(cudaStream_t s) {
+  const uint32_t dim = cfg_.dim;
+  nlist_ = std::max(1u, std::min(cfg_.nlist, n_));
+  uint32_t train = cfg_.train_rows ? cfg_.train_rows : (uint32_t)std::min<uint64_t>(n_, 256ull * nlist_);
+  train = std::max(std::min(train, n_), nlist_);
+  int rc = centroids_.alloc((size_t)nlist_ * dim);
+  if (rc) return rc;
+  {
+    // coarse centroids trained on a sample, then every row assigned
+    std::vector<uint32_t> rows = sample_rows(n_, train, cfg_.seed + 1);
+    DevBuf<uint32_t> d_rows;
+    DevBuf<float> sample;
+    rc = d_rows.alloc(rows.size());
+    if (!rc) rc = sample.alloc((size_t)rows.size() * dim);
+    if (rc) return rc;
+    cudaMemcpyAsync(d_rows.p, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice, s);
+    rc = launch_gather_rows(vectors_.p, d_rows.p, (uint32_t)rows.size(), dim, sample.p, s);
+    if (!rc) rc = kmeans(sample.p, (uint32_t)rows.size(), dim, nlist_, cfg_.kmeans_iters, cfg_.seed + 2, centroids_.p, s);
+    if (rc) return rc;
+  }
+  DevBuf<GpuSearchResult> assign;
+  DevBuf<float> residuals;
+  DevBuf<uint32_t> work;
+  rc = assign.alloc(n_);
+  if (!rc) rc = residuals.alloc((size_t)n_ * dim);
+  if (!rc) rc = work.alloc(std::max<size_t>(nlist_, 2 * dim));
+  if (!rc) rc = offsets_.alloc(nlist_ + 1);
+  if (!rc) rc = vec_ids_.alloc(n_);
+  if (rc) return rc;
+  rc = assign_rows(vectors_.p, n_, dim, centroids_.p, nlist_, assign.p, s);
+  if (!rc) rc = launch_build_lists(assign.p, n_, nlist_, offsets_.p, vec_ids_.p, work.p, s);
+  if (!rc) rc = launch_residuals(vectors_.p, n_, dim, centroids_.p, assign.p, residuals.p, s);
+  if (rc) return rc;
+
+  if ((cfg_.build_flags & FV_BUILD_IVF_PQ) && cfg_.m_pq && dim % cfg_.m_pq == 0) {
+    const uint32_t m = cfg_.m_pq, sub = dim / m;
+    rc = codebooks_.alloc((size_t)m * 256 * sub);
+    if (rc) return rc;
+    const uint32_t kk = std::min(n_, 256u);
+    std::vector<uint32_t> rows = sample_rows(n_, std::min(n_, std::max(65536u, kk)), cfg_.seed + 3);
+    DevBuf<uint32_t> d_rows;
+    DevBuf<float> sample, subv, cb;
+    rc = d_rows.alloc(rows.size());
+    if (!rc) rc = sample.alloc((size_t)rows.size() * dim);
+    if (!rc) rc = subv.alloc((size_t)rows.size() * sub);
+    if (!rc) rc = cb.alloc((size_t)256 * sub);
+    if (rc) return rc;
+    cudaMemcpyAsync(d_rows.p, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice, s);
+    rc = launch_gather_rows(residuals.p, d_rows.p, (uint32_t)rows.size(), dim, sample.p, s);
+    if (!rc) rc = launch_fill_f32(codebooks_.p, codebooks_.n, 3.4028234663852886e38f, s);  // unused codewords: FLT_MAX
+    for (uint32_t mm = 0; !rc && mm < m; ++mm) {
+      rc = launch_extract_subspace(sample.p, (uint32_t)rows.size(), dim, mm * sub, sub, subv.p, s);
+      if (!rc) rc = kmeans(subv.p, (uint32_t)rows.size(), sub, kk, cfg_.pq_iters, cfg_.seed + 100 + mm, cb.p, s);
+      if (!rc)
+        rc = (int)cudaMemcpyAsync(codebooks_.p + (size_t)mm * 256 * sub, cb.p, (size_t)kk * sub * 4,
+                                  cudaMemcpyDeviceToDevice, s);
+    }
+    if (!rc) rc = pq_codes_.alloc((size_t)n_ * m);
+    if (!rc) rc = launch_pq_encode(residuals.p, n_, dim, m, codebooks_.p, pq_codes_.p, s);
+    if (!rc) rc = pq_codes_lm_.alloc((size_t)n_ * m);
+    if (!rc) rc = launch_relayout_codes(pq_codes_.p, vec_ids_.p, n_, m, pq_codes_lm_.p, s);
+    if (rc) return rc;
+  }
+  if (cfg_.build_flags & FV_BUILD_IVF_SQ8) {
+    rc = sq_mins_.alloc(dim);
+    if (!rc) rc = sq_scales_.alloc(dim);
+    if (!rc) rc = sq_codes_.alloc((size_t)n_ * dim);
+    if (!rc) rc = launch_sq8_fit(residuals.p, n_, dim, sq_mins_.p, sq_scales_.p, work.p, s);
+    if (!rc) rc = launch_sq8_encode(residuals.p, n_, dim, sq_mins_.p, sq_scales_.p, sq_codes_.p, s);
+    if (!rc) rc = sq_codes_lm_.alloc((size_t)n_ * dim);
+    if (!rc) rc = launch_relayout_codes(sq_codes_.p, vec_ids_.p, n_, dim, sq_codes_lm_.p, s);
+    if (rc) return rc;
+  }
+  return (int)cudaStreamSynchronize(s);
+}
+
+int Index::build(const float* host, uint32_t n) {
+  if (!host) return FV_ERR_NULL;
+  if (n == 0 || cfg_.dim == 0 || cfg_.dim > 4096) return FV_ERR_ARG;
+  std::unique_lock<std::shared_mutex> lk(state_mu_);
+  const uint32_t dim = cfg_.dim;
+  cudaStream_t s = streams_[0]->s;
+  std::vector<float> staged;
+  const float* src = host;
+  if (cfg_.metric == METRIC_COSINE) {
+    staged.assign(host, host + (size_t)n * dim);
+    normalize_rows(staged.data(), n, dim);
+    src = staged.data();
+  }
+  n_ = n;
+  int rc = vectors_.alloc((size_t)n * dim);
+  if (rc) return rc;
+  rc = (int)cudaMemcpyAsync(vectors_.p, src, (size_t)n * dim * 4, cudaMemcpyHostToDevice, s);
+  if (rc) return rc;
+  if (cfg_.build_flags & FV_BUILD_FP16) {
+    pd16_ = (dim + 15) / 16 * 16;
+    rc = fp16_.alloc((size_t)n * pd16_);
+    if (!rc) rc = norms16_.alloc(n);
+    if (!rc) rc = launch_encode_fp16(vectors_.p, n, dim, pd16_, fp16_.p, norms16_.p, s);
+    if (rc) return rc;
+  }
+  if (cfg_.build_flags & FV_BUILD_FP8) {
+    pd8_ = (dim + 15) / 16 * 16;
+    rc = fp8_.alloc((size_t)n * pd8_);
+    if (!rc) rc = fp8_scales_.alloc(n);
+    if (!rc) rc = fp8_norms_.alloc(n);
+    if (!rc) rc = launch_encode_fp8(vectors_.p, n, dim, pd8_, fp8_.p, fp8_scales_.p, fp8_norms_.p, s);
+    if (rc) return rc;
+  }
+  if (cfg_.nlist && (cfg_.build_flags & (FV_BUILD_IVF_PQ | FV_BUILD_IVF_SQ8))) {
+    rc = build_ivf(s);
+    if (rc) return rc;
+  }
+  // validity words: every main slot live (index.rs:505-511)
+  main_valid_.assign((n + 31) / 32, 0xFFFFFFFFu);
+  if (n % 32) main_valid_.back() = (1u << (n % 32)) - 1u;
+  rc = valid_words_.alloc(main_valid_.size());
+  if (!rc) rc = (int)cudaMemcpyAsync(valid_words_.p, main_valid_.data(), main_valid_.size() * 4,
+                                     cudaMemcpyHostToDevice, s);
+  if (!rc) rc = (int)cudaStreamSynchronize(s);
+  if (rc) return rc;
+  tombstones_.clear();
+  delta_.vectors.clear();
+  delta_.ids.clear();
+  next_id_ = n;
+  built_ = true;
+  return 0;
+}
+
+// --------------------------------------------------------- add / delete
+int Index::add(const float* host, uint32_t n, uint32_t* out_ids) {
+  if (n == 0) return 0;
+  if (!host || !out_ids) return FV_ERR_NULL;
+  {
+    std::shared_lock<std::shared_mutex> rl(state_mu_);
+    if (!built_) {
+      rl.unlock();
+      int rc = build(host, n);
+      if (rc) return rc;
+      for (uint32_t i = 0; i < n; ++i) out_ids[i] = i;
+      return 0;
+    }
+  }
+  std::unique_lock<std::shared_mutex> lk(state_mu_);
+  const uint32_t dim = cfg_.dim;
+  const size_t off = delta_.vectors.size();
+  delta_.vectors.insert(delta_.vectors.end(), host, host + (size_t)n * dim);
+  if (cfg_.metric == METRIC_COSINE) normalize_rows(delta_.vectors.data() + off, n, dim);
+  for (uint32_t i = 0; i < n; ++i) {
+    out_ids[i] = next_id_ + i;
+    delta_.ids.push_back(next_id_ + i);
+  }
+  next_id_ += n;
+  const size_t len = delta_.ids.size();
+  int rc = 0;
+  if (len > delta_.capacity) {
+    size_t cap = 256;
+    while (cap < len) cap <<= 1;
+    rc = delta_.d_vectors.alloc(cap * dim);
+    if (!rc) rc = delta_.d_ids.alloc(cap);
+    if (!rc) rc = delta_.d_mask.alloc((cap + 31) / 32);
+    if (rc) return rc;
+    delta_.capacity = cap;
+  }
+  rc = (int)cudaMemcpyAsync(delta_.d_vectors.p, delta_.vectors.data(), delta_.vectors.size() * 4,
+                            cudaMemcpyHostToDevice, delta_stream_);
+  if (!rc)
+    rc = (int)cudaMemcpyAsync(delta_.d_ids.p, delta_.ids.data(), len * 4, cudaMemcpyHostToDevice, delta_stream_);
+  if (!rc) rc = (int)cudaStreamSynchronize(delta_stream_);
+  return rc;
+}
+
+int Index::remove(const uint32_t* ids, uint32_t n, uint32_t* out_deleted) {
+  if (!out_deleted) return FV_ERR_NULL;
+  *out_deleted = 0;
+  if (n == 0) return 0;
+  if (!ids) return FV_ERR_NULL;
+  std::unique_lock<std::shared_mutex> lk(state_mu_);
+  if (!built_) return 0;
+  std::unordered_set<uint32_t> in_delta(delta_.ids.begin(), delta_.ids.end());
+  uint32_t deleted = 0;
+  bool main_dirty = false;
+  for (uint32_t i = 0; i < n; ++i) {
+    const uint32_t lid = ids[i];
+    if (tombstones_.count(lid)) continue;
+    if (in_delta.count(lid)) {
+      tombstones_.insert(lid);
+      ++deleted;
+      continue;
+    }
+    if (lid < n_) {  // slot == logical id (the index is never compacted here)
+      tombstones_.insert(lid);
+      main_valid_[lid >> 5] &= ~(1u << (lid & 31));
+      main_dirty = true;
+      ++deleted;
+    }
+  }
+  if (main_dirty) {
+    cudaStream_t s = streams_[0]->s;
+    int rc = (int)cudaMemcpyAsync(valid_words_.p, main_valid_.data(), main_valid_.size() * 4, cudaMemcpyHostToDevice,
+                                  s);
+    if (!rc) rc = (int)cudaStreamSynchronize(s);
+    if (rc) return rc;
+  }
+  *out_deleted = deleted;
+  return 0;
+}
+
+// --------------------------------------------------------------- masks
+// build_slot_mask_words (index.rs:1264-1292): user mask over logical ids AND
+// the live words; words beyond the user mask count as 0.
+void Index::slot_mask(const uint32_t* user, uint32_t words, std::vector<uint32_t>& out, bool& use) const {
+  use = user != nullptr || !tombstones_.empty();
+  if (!use) return;
+  const uint32_t nw = (n_ + 31) / 32;
+  out.resize(nw);
+  for (uint32_t w = 0; w < nw; ++w) out[w] = main_valid_[w] & (user ? (w < words ? user[w] : 0u) : 0xFFFFFFFFu);
+}
+
+// build_delta_mask_words (index.rs:1294-1316)
+void Index::delta_mask(const uint32_t* user, uint32_t words, std::vector<uint32_t>& out, bool& use) const {
+  use = delta_.len() > 0 && (user != nullptr || !tombstones_.empty());
+  if (!use) return;
+  out.assign((delta_.len() + 31) / 32, 0u);
+  for (uint32_t i = 0; i < delta_.len(); ++i) {
+    const uint32_t lid = delta_.ids[i];
+    if (tombstones_.count(lid)) continue;
+    bool allow = true;
+    if (user) {
+      const uint32_t w = (lid >> 5) < words ? user[lid >> 5] : 0u;
+      allow = (w >> (lid & 31)) & 1u;
+    }
+    if (allow) out[i >> 5] |= 1u << (i & 31);
+  }
+}
+
+// -------------------------------------------------------------- search
+int Index::search(const FvSearchParams& p, const float* q, uint32_t nq, bool device_queries, const uint32_t* user_mask,
+                  uint32_t mask_words, GpuSearchResult* out) {
+  if (!q || !out) return FV_ERR_NULL;
+  std::shared_lock<std::shared_mutex> lk(state_mu_);
+  if (!built_) return FV_ERR_ARG;
+  if (nq == 0 || p.top_k == 0) return 0;
+  const uint32_t dim = cfg_.dim;
+  if (p.top_k > 256) return FV_ERR_ARG;  // validate_search_shape (index.rs:309-326)
+  const auto t0 = std::chrono::steady_clock::now();
+  const uint32_t k = p.top_k;
+  Stream& st = *streams_[rr_.fetch_add(1) % streams_.size()];
+  std::lock_guard<std::mutex> sl(st.mu);
+  int rc = st.q.ensure((size_t)nq * dim);
+  if (!rc) rc = st.res.ensure((size_t)nq * k);
+  if (!rc) rc = st.hres.ensure((size_t)nq * k);
+  if (rc) return rc;
+
+  // queries (prepare_queries, index.rs:1473-1483)
+  const float* d_q = q;
+  if (!device_queries) {
+    rc = st.hq.ensure((size_t)nq * dim);
+    if (rc) return rc;
+    memcpy(st.hq.p, q, (size_t)nq * dim * 4);
+    if (cfg_.metric == METRIC_COSINE) normalize_rows(st.hq.p, nq, dim);
+    rc = (int)cudaMemcpyAsync(st.q.p, st.hq.p, (size_t)nq * dim * 4, cudaMemcpyHostToDevice, st.s);
+    if (rc) return rc;
+    d_q = st.q.p;
+  }
+  cudaEventRecord(st.ready, st.s);
+
+  std::vector<uint32_t> words;
+  bool use_mask = false;
+  slot_mask(user_mask, mask_words, words, use_mask);
+  const uint32_t* d_mask = nullptr;
+  if (use_mask) {
+    rc = st.mask.ensure(words.size());
+    if (!rc) rc = (int)cudaMemcpyAsync(st.mask.p, words.data(), words.size() * 4, cudaMemcpyHostToDevice, st.s);
+    if (rc) return rc;
+    d_mask = st.mask.p;
+  }
+
+  switch (p.engine) {
+    case FV_ENGINE_FLAT:
+      rc = cuda_flat_scan_batch(vectors_.p, nullptr, n_, dim, d_q, nq, k, (MetricType)cfg_.metric, d_mask, st.res.p,
+                                st.s);
+      break;
+    case FV_ENGINE_FP16: {
+      if (!fp16_.p) return FV_ERR_ARG;
+      Fp16GpuTables t{fp16_.p, norms16_.p, vectors_.p, n_, dim, pd16_};
+      rc = fv_fp16_search_batch_ex(&t, d_q, nq, k, (MetricType)cfg_.metric, d_mask, &p.scan, st.res.p, st.s);
+      break;
+    }
+    case FV_ENGINE_FP8: {
+      if (!fp8_.p) return FV_ERR_ARG;
+      FvFp8GpuTables t{fp8_.p, fp8_scales_.p, fp8_norms_.p, vectors_.p, n_, dim, pd8_};
+      rc = fv_fp8_search_batch(&t, d_q, nq, k, (MetricType)cfg_.metric, d_mask, &p.scan, st.res.p, st.s);
+      break;
+    }
+    case FV_ENGINE_IVF_PQ: {
+      if (!pq_codes_.p) return FV_ERR_ARG;
+      IvfPqGpuTables t{centroids_.p, codebooks_.p, pq_codes_lm_.p, offsets_.p, vec_ids_.p, vectors_.p, n_, dim,
+                       nlist_,       cfg_.m_pq,    dim / cfg_.m_pq};
+      FvIvfOptions o{1, {0, 0, 0}};
+      rc = fv_ivf_pq_search_ex(&t, &o, d_q, nq, k, p.nprobe, p.rerank_k, (MetricType)cfg_.metric, d_mask, st.res.p,
+                               st.s);
+      break;
+    }
+    case FV_ENGINE_IVF_SQ8: {
+      if (!sq_codes_.p) return FV_ERR_ARG;
+      IvfSqGpuTables t{centroids_.p, sq_mins_.p, sq_scales_.p, sq_codes_lm_.p, offsets_.p, vec_ids_.p, vectors_.p,
+                       n_,           dim,        nlist_};
+      FvIvfOptions o{1, {0, 0, 0}};
+      rc = fv_ivf_sq_search_ex(&t, &o, d_q, nq, k, p.nprobe, p.rerank_k, (MetricType)cfg_.metric, d_mask, st.res.p,
+                               st.s);
+      break;
+    }
+    default:
+      return FV_ERR_ARG;
+  }
+  if (rc) return rc;
+
+  // concurrent delta scan (launch_delta_scan_inner, index.rs:1424-1471)
+  std::unique_lock<std::mutex> dl(delta_mu_, std::defer_lock);
+  const bool has_delta = delta_.len() > 0;
+  if (has_delta) {
+    dl.lock();
+    rc = delta_.d_res.ensure((size_t)nq * k);
+    if (!rc) rc = delta_.h_res.ensure((size_t)nq * k);
+    if (rc) return rc;
+    cudaStreamWaitEvent(delta_stream_, st.ready, 0);
+    std::vector<uint32_t> dw;
+    bool use_dmask = false;
+    delta_mask(user_mask, mask_words, dw, use_dmask);
+    if (use_dmask) {
+      rc = (int)cudaMemcpyAsync(delta_.d_mask.p, dw.data(), dw.size() * 4, cudaMemcpyHostToDevice, delta_stream_);
+      if (rc) return rc;
+    }
+    rc = cuda_flat_scan_batch(delta_.d_vectors.p, delta_.d_ids.p, delta_.len(), dim, d_q, nq, k,
+                              (MetricType)cfg_.metric, use_dmask ? delta_.d_mask.p : nullptr, delta_.d_res.p,
+                              delta_stream_);
+    if (!rc)
+      rc = (int)cudaMemcpyAsync(delta_.h_res.p, delta_.d_res.p, (size_t)nq * k * sizeof(GpuSearchResult),
+                                cudaMemcpyDeviceToHost, delta_stream_);
+    if (rc) return rc;
+  }
+  rc = (int)cudaMemcpyAsync(st.hres.p, st.res.p, (size_t)nq * k * sizeof(GpuSearchResult), cudaMemcpyDeviceToHost,
+                            st.s);
+  if (!rc) rc = (int)cudaStreamSynchronize(st.s);
+  if (!rc && has_delta) rc = (int)cudaStreamSynchronize(delta_stream_);
+  if (rc) return rc;
+
+  if (!has_delta) {
+    memcpy(out, st.hres.p, (size_t)nq * k * sizeof(GpuSearchResult));
+  } else {
+    // finish_delta_merge (index.rs:1353-1387): main then delta, invalid ids
+    // dropped, stable sort by distance, truncate, pad with {u32::MAX, +inf}
+    std::vector<GpuSearchResult> comb;
+    for (uint32_t qi = 0; qi < nq; ++qi) {
+      comb.clear();
+      for (uint32_t r = 0; r < k; ++r)
+        if (st.hres.p[(size_t)qi * k + r].id != 0xFFFFFFFFu) comb.push_back(st.hres.p[(size_t)qi * k + r]);
+      for (uint32_t r = 0; r < k; ++r)
+        if (delta_.h_res.p[(size_t)qi * k + r].id != 0xFFFFFFFFu) comb.push_back(delta_.h_res.p[(size_t)qi * k + r]);
+      std::stable_sort(comb.begin(), comb.end(),
+                       [](const GpuSearchResult& a, const GpuSearchResult& b) { return a.distance < b.distance; });
+      for (uint32_t r = 0; r < k; ++r)
+        out[(size_t)qi * k + r] = r < comb.size() ? comb[r] : GpuSearchResult{0xFFFFFFFFu, INFINITY};
+    }
+  }
+  record(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(), nq);
+  return 0;
+}
+
+// ------------------------------------------------------------- metrics
+void Index::record(double seconds, uint32_t nq) {
+  std::lock_guard<std::mutex> lk(metrics_mu_);
+  const double us = seconds * 1e6 / std::max<uint32_t>(nq, 1);
+  if (lat_us_.size() >= 100000) lat_us_.erase(lat_us_.begin(), lat_us_.begin() + 50000);
+  lat_us_.push_back(us);
+  total_queries_ += nq;
+}
+
+void Index::stats(FvLatencyStats* s) {
+  std::lock_guard<std::mutex> lk(metrics_mu_);
+  *s = FvLatencyStats{};
+  s->count = total_queries_;
+  const double el = std::max(1e-3, std::chrono::duration<double>(std::chrono::steady_clock::now() - start_).count());
+  s->qps = (double)total_queries_ / el;
+  if (lat_us_.empty()) return;
+  std::vector<double> v = lat_us_;
+  std::sort(v.begin(), v.end());
+  const size_t n = v.size();
+  auto at = [&](double f) { return v[std::min(n - 1, (size_t)((double)n * f))]; };
+  s->p50_us = at(0.5);
+  s->p90_us = at(0.9);
+  s->p99_us = at(0.99);
+  s->p999_us = at(0.999);
+  s->min_us = v.front();
+  s->max_us = v.back();
+  double sum = 0;
+  for (double x : v) sum += x;
+  s->mean_us = sum / (double)n;
+}
+
+void Index::info(FvIndexInfo* i) {
+  std::shared_lock<std::shared_mutex> lk(state_mu_);
+  *i = FvIndexInfo{};
+  i->num_vectors = n_;
+  i->delta_len = delta_.len();
+  i->tombstones = (uint32_t)tombstones_.size();
+  i->dim = cfg_.dim;
+  i->padded_dim = pd16_;
+  i->nlist = nlist_;
+  i->m_pq = cfg_.m_pq;
+  i->metric = cfg_.metric;
+  i->next_id = next_id_;
+  i->device_bytes = vectors_.bytes() + fp16_.bytes() + norms16_.bytes() + fp8_.bytes() + fp8_scales_.bytes() +
+                    fp8_norms_.bytes() + centroids_.bytes() + codebooks_.bytes() + pq_codes_.bytes() +
+                    pq_codes_lm_.bytes() + sq_codes_.bytes() + sq_codes_lm_.bytes() + offsets_.bytes() +
+                    vec_ids_.bytes();
+}
+
+// Copies one IVF table to the host (for checking the build against a CPU
+// restatement): 0 centroids, 1 codebooks, 2 pq codes (by id), 3 sq mins,
+// 4 sq scales, 5 sq codes (by id), 6 offsets, 7 vec ids.
+int Index::export_ivf(uint32_t what, void* host_out, size_t bytes) {
+  std::shared_lock<std::shared_mutex> lk(state_mu_);
+  const void* src = nullptr;
+  size_t have = 0;
+  switch (what) {
+    case 0: src = centroids_.p; have = centroids_.bytes(); break;
+    case 1: src = codebooks_.p; have = codebooks_.bytes(); break;
+    case 2: src = pq_codes_.p; have = pq_codes_.bytes(); break;
+    case 3: src = sq_mins_.p; have = sq_mins_.bytes(); break;
+    case 4: src = sq_scales_.p; have = sq_scales_.bytes(); break;
+    case 5: src = sq_codes_.p; have = sq_codes_.bytes(); break;
+    case 6: src = offsets_.p; have = offsets_.bytes(); break;
+    case 7: src = vec_ids_.p; have = vec_ids_.bytes(); break;
+    default: return FV_ERR_ARG;
+  }
+  if (!host_out || bytes < have) return FV_ERR_ARG;
+  if (have == 0) return 0;
+  return (int)cudaMemcpy(host_out, src, have, cudaMemcpyDeviceToHost);
+}
+
+}  // namespace fv
+
+// ------------------------------------------------------------------ C ABI
+struct FvIndex {
+  fv::Index impl;
+  explicit FvIndex(const FvIndexConfig& c) : impl(c) {}
+};
+
+extern "C" {
+
+int fv_index_create(const FvIndexConfig* config, FvIndex** out) {
+  if (!config || !out) return FV_ERR_NULL;
+  if (config->dim == 0 || config->dim > 4096 || config->metric > 2) return FV_ERR_ARG;
+  try {
+    *out = new FvIndex(*config);
+  } catch (...) {
+    return FV_ERR_NOMEM;
+  }
+  return 0;
+}
+int fv_index_destroy(FvIndex* index) {
+  delete index;
+  return 0;
+}
+int fv_index_build(FvIndex* index, const float* host_vectors, uint32_t num_vectors) {
+  if (!index) return FV_ERR_NULL;
+  return index->impl.build(host_vectors, num_vectors);
+}
+int fv_index_add(FvIndex* index, const float* host_vectors, uint32_t num_vectors, uint32_t* out_ids) {
+  if (!index) return FV_ERR_NULL;
+  return index->impl.add(host_vectors, num_vectors, out_ids);
+}
+int fv_index_delete(FvIndex* index, const uint32_t* ids, uint32_t count, uint32_t* out_deleted) {
+  if (!index) return FV_ERR_NULL;
+  return index->impl.remove(ids, count, out_deleted);
+}
+int fv_index_search(FvIndex* index, const FvSearchParams* params, const float* host_queries, uint32_t num_queries,
+                    const uint32_t* host_mask_words, uint32_t mask_words, GpuSearchResult* host_out) {
+  if (!index || !params) return FV_ERR_NULL;
+  return index->impl.search(*params, host_queries, num_queries, false, host_mask_words, mask_words, host_out);
+}
+int fv_index_search_device(FvIndex* index, const FvSearchParams* params, const float* d_queries, uint32_t num_queries,
+                           GpuSearchResult* host_out) {
+  if (!index || !params) return FV_ERR_NULL;
+  return index->impl.search(*params, d_queries, num_queries, true, nullptr, 0, host_out);
+}
+int fv_index_stats(FvIndex* index, FvLatencyStats* out) {
+  if (!index || !out) return FV_ERR_NULL;
+  index->impl.stats(out);
+  return 0;
+}
+int fv_index_info(FvIndex* index, FvIndexInfo* out) {
+  if (!index || !out) return FV_ERR_NULL;
+  index->impl.info(out);
+  return 0;
+}
+int fv_index_export_ivf(FvIndex* index, uint32_t table, void* host_out, size_t bytes) {
+  if (!index) return FV_ERR_NULL;
+  return index->impl.export_ivf(table, host_out, bytes);
+}
+
+}  // extern "C"

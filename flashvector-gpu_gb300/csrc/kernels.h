@@ -121,6 +121,25 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream);  // mo
 int launch_relayout_codes(const uint8_t* by_id, const uint32_t* vec_ids, uint32_t n, uint32_t row_bytes,
                           uint8_t* by_list, cudaStream_t stream);
 
+// IVF index build (index_build.cu)
+int launch_kmeans_update(const float* x, uint32_t n, uint32_t dim, const GpuSearchResult* assign, uint32_t k,
+                         float* centroids, uint32_t* counts, double* sums, cudaStream_t stream);
+int launch_build_lists(const GpuSearchResult* assign, uint32_t n, uint32_t nlist, uint32_t* offsets, uint32_t* vec_ids,
+                       uint32_t* work, cudaStream_t stream);
+int launch_residuals(const float* x, uint32_t n, uint32_t dim, const float* centroids, const GpuSearchResult* assign,
+                     float* out, cudaStream_t stream);
+int launch_extract_subspace(const float* x, uint32_t n, uint32_t dim, uint32_t off, uint32_t sub, float* out,
+                            cudaStream_t stream);
+int launch_pq_encode(const float* x, uint32_t n, uint32_t dim, uint32_t m_pq, const float* codebooks, uint8_t* codes,
+                     cudaStream_t stream);
+int launch_sq8_fit(const float* r, uint32_t n, uint32_t dim, float* mins, float* scales, uint32_t* work,
+                   cudaStream_t stream);
+int launch_sq8_encode(const float* r, uint32_t n, uint32_t dim, const float* mins, const float* scales, uint8_t* codes,
+                      cudaStream_t stream);
+int launch_gather_rows(const float* x, const uint32_t* rows, uint32_t count, uint32_t dim, float* out,
+                       cudaStream_t stream);
+int launch_fill_f32(float* p, size_t n, float v, cudaStream_t stream);
+
 // reduced-precision table encoders (encode.cu)
 int launch_encode_fp16(const float* x, uint32_t n, uint32_t dim, uint32_t pd, uint16_t* out, float* norms,
                        cudaStream_t stream);

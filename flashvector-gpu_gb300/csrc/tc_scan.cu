@@ -250,6 +250,12 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   const uint32_t ntiles = (t.n + TC_N - 1) / TC_N;
   const int sms = device_sm_count();
   uint32_t splits = opt.splits ? opt.splits : std::max<uint32_t>(1u, (uint32_t)sms / nqb);
+  if (!opt.splits && shortlist > kl) {
+    // a (query, range) heap keeps kl keys: split the base so that each range
+    // holds, in expectation, a third of that share of the shortlist (a range
+    // that still overflows is reported through the status word)
+    splits = std::max<uint32_t>(splits, (3 * shortlist + kl - 1) / kl);
+  }
   splits = std::max(1u, std::min(splits, ntiles));
   // the select kernel sorts lists*kl keys in shared memory: <= 16384
   while (splits > 1 && next_pow2(splits * kl) > 16384u) --splits;

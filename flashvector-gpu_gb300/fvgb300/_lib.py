@@ -52,6 +52,27 @@ class FvScanOptions(C.Structure):
     _fields_ = [("overfetch", U32), ("boundary_fp64", U32), ("boundary_eps", F32), ("splits", U32)]
 
 
+class FvIndexConfig(C.Structure):
+    _fields_ = [("dim", U32), ("metric", U32), ("nlist", U32), ("m_pq", U32), ("build_flags", U32),
+                ("kmeans_iters", U32), ("pq_iters", U32), ("train_rows", U32), ("streams", U32), ("reserved", U32),
+                ("seed", C.c_uint64)]
+
+
+class FvSearchParams(C.Structure):
+    _fields_ = [("engine", U32), ("top_k", U32), ("nprobe", U32), ("rerank_k", U32), ("scan", FvScanOptions)]
+
+
+class FvLatencyStats(C.Structure):
+    _fields_ = [("count", C.c_uint64)] + [(n, C.c_double) for n in
+                                          ("p50_us", "p90_us", "p99_us", "p999_us", "min_us", "max_us", "mean_us",
+                                           "qps")]
+
+
+class FvIndexInfo(C.Structure):
+    _fields_ = [(n, U32) for n in ("num_vectors", "delta_len", "tombstones", "dim", "padded_dim", "nlist", "m_pq",
+                                   "metric", "next_id", "reserved")] + [("device_bytes", C.c_uint64)]
+
+
 # name -> (restype, argtypes); every function declared in include/fv_bridge.h
 SIGNATURES = {
     "cuda_init_device": (I32, [I32]),
@@ -79,11 +100,24 @@ SIGNATURES = {
     "fv_ivf_pq_search_ex": (I32, [P, P, P, U32, U32, U32, U32, I32, P, P, P]),
     "fv_ivf_sq_search_ex": (I32, [P, P, P, U32, U32, U32, U32, I32, P, P, P]),
     "fv_ivf_relayout_codes": (I32, [P, P, U32, U32, P, P]),
+    "fv_build_pq_encode": (I32, [P, U32, U32, U32, P, P, P]),
+    "fv_build_sq8": (I32, [P, U32, U32, P, P, P, P]),
+    "fv_build_ivf_lists": (I32, [P, U32, U32, P, P, P]),
     "cuda_fp16_tc_search_batch": (I32, [P, P, U32, U32, I32, P, P, P]),
     "fv_fp16_search_batch_ex": (I32, [P, P, U32, U32, I32, P, P, P, P]),
     "fv_fp8_search_batch": (I32, [P, P, U32, U32, I32, P, P, P, P]),
     "fv_encode_fp16_padded": (I32, [P, U32, U32, U32, P, P, P]),
     "fv_encode_fp8": (I32, [P, U32, U32, U32, P, P, P, P]),
+    "fv_index_create": (I32, [P, P]),
+    "fv_index_destroy": (I32, [P]),
+    "fv_index_build": (I32, [P, P, U32]),
+    "fv_index_add": (I32, [P, P, U32, P]),
+    "fv_index_delete": (I32, [P, P, U32, P]),
+    "fv_index_search": (I32, [P, P, P, U32, P, U32, P]),
+    "fv_index_search_device": (I32, [P, P, P, U32, P]),
+    "fv_index_stats": (I32, [P, P]),
+    "fv_index_info": (I32, [P, P]),
+    "fv_index_export_ivf": (I32, [P, U32, P, SZ]),
     "fv_version": (C.c_char_p, []),
     "fv_read_device_status": (I32, [P]),
     "fv_launch_count": (C.c_uint64, []),

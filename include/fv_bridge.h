@@ -126,6 +126,20 @@ int fv_ivf_relayout_codes(const uint8_t* d_codes_by_id, const uint32_t* d_ivf_ve
                           uint32_t num_vectors, uint32_t row_bytes, uint8_t* d_out_by_list,
                           void* stream);
 
+/* ---- IVF index build (GPU) ---------------------------------------------
+ * Restate the reference's host encoders on the device: PQ nearest-codeword
+ * encode of residual rows (cluster.rs:247-287; codebooks [m_pq][256][dim/m_pq]),
+ * SQ8 fit + encode of residual rows (quant.rs:14-75), posting lists from a
+ * nearest-centroid assignment (index.rs:445-458; ids within a list in no
+ * particular order). d_assign is the k = 1 result of a flat scan of the rows
+ * against the centroids. */
+int fv_build_pq_encode(const float* d_residuals, uint32_t num_vectors, uint32_t dim, uint32_t m_pq,
+                       const float* d_codebooks, uint8_t* d_out_codes, void* stream);
+int fv_build_sq8(const float* d_residuals, uint32_t num_vectors, uint32_t dim, float* d_out_mins,
+                 float* d_out_scales, uint8_t* d_out_codes, void* stream);
+int fv_build_ivf_lists(const GpuSearchResult* d_assign, uint32_t num_vectors, uint32_t nlist,
+                       uint32_t* d_out_offsets, uint32_t* d_out_vec_ids, void* stream);
+
 /* ---- tensor-core flat scans --------------------------------------------
  * Replaces cuda_bridge.h:138-147 (ivf_quant_lookup.cu:1106-1123). Per
  * query the top_k (<= 256) rows by the fp16 tensor-core distance
@@ -166,6 +180,38 @@ int fv_encode_fp16_padded(const float* d_vectors, uint32_t num_vectors, uint32_t
 int fv_encode_fp8(const float* d_vectors, uint32_t num_vectors, uint32_t dim,
                   uint32_t padded_dim, uint8_t* d_out_fp8, float* d_out_scales,
                   float* d_out_norms_sq, void* stream);
+
+/* ---- host engine -------------------------------------------------------
+ * The reference's GpuVectorIndex (crates/engine/src/index.rs:131-2634) for
+ * the scan engines, behind an opaque handle. Host buffers in and out; every
+ * call is synchronous like the reference's methods.
+ *   fv_index_build    index.rs:328-576 (tables built on the GPU)
+ *   fv_index_add      add_vectors, index.rs:647-694 (ids written to out_ids)
+ *   fv_index_delete   delete_ids, index.rs:583-643
+ *   fv_index_search   batch_search_fp16_tc / batch_search_ivf_mode / the
+ *                     exact flat scan (index.rs:1979-2237): params->engine
+ *                     selects FV_ENGINE_*; host_mask_words is the optional
+ *                     user filter over logical ids (mask_words words);
+ *                     host_out receives num_queries * top_k results.
+ *   fv_index_search_device  batch_search_ivf_device_ptr (index.rs:2110)
+ *   fv_index_stats    MetricsTracker::get_stats (metrics.rs:47-90) */
+typedef struct FvIndex FvIndex;
+int fv_index_create(const FvIndexConfig* config, FvIndex** out);
+int fv_index_destroy(FvIndex* index);
+int fv_index_build(FvIndex* index, const float* host_vectors, uint32_t num_vectors);
+int fv_index_add(FvIndex* index, const float* host_vectors, uint32_t num_vectors, uint32_t* out_ids);
+int fv_index_delete(FvIndex* index, const uint32_t* ids, uint32_t count, uint32_t* out_deleted);
+int fv_index_search(FvIndex* index, const FvSearchParams* params, const float* host_queries,
+                    uint32_t num_queries, const uint32_t* host_mask_words, uint32_t mask_words,
+                    GpuSearchResult* host_out);
+int fv_index_search_device(FvIndex* index, const FvSearchParams* params, const float* d_queries,
+                           uint32_t num_queries, GpuSearchResult* host_out);
+int fv_index_stats(FvIndex* index, FvLatencyStats* out);
+int fv_index_info(FvIndex* index, FvIndexInfo* out);
+/* Copies IVF table `table` to host memory: 0 centroids, 1 codebooks, 2 PQ
+ * codes by id, 3 SQ8 mins, 4 SQ8 scales, 5 SQ8 codes by id, 6 list offsets,
+ * 7 list ids. */
+int fv_index_export_ivf(FvIndex* index, uint32_t table, void* host_out, size_t bytes);
 
 /* ---- test fixtures -----------------------------------------------------
  * Replace cuda_bridge.h:195-213 (hnsw_traverse.cu:387-437, 694-735). */

@@ -112,6 +112,65 @@ typedef struct {
     uint32_t reserved[3];
 } FvIvfOptions;
 
+/* ---- host engine (the reference's GpuVectorIndex, index.rs:131-2634) ---- */
+
+/* Index configuration; dim / nlist / m_pq / metric as IndexConfig
+ * (types.h:74-82). The graph fields of the reference (m, ef_construction)
+ * belong to engines outside the scan path and are absent. */
+typedef struct {
+    uint32_t dim;
+    uint32_t metric;        /* MetricType                                     */
+    uint32_t nlist;         /* IVF lists (0 = no IVF tables)                  */
+    uint32_t m_pq;          /* PQ sub-quantisers (0 = no IVF-PQ)              */
+    uint32_t build_flags;   /* FV_BUILD_* bits (0 = FP16 | IVF_PQ | IVF_SQ8)   */
+    uint32_t kmeans_iters;  /* Lloyd iterations (0 = 10)                      */
+    uint32_t pq_iters;      /* per-sub-space k-means iterations (0 = 10)      */
+    uint32_t train_rows;    /* rows sampled to train centroids / codebooks
+                               (0 = min(n, 256 * nlist))                       */
+    uint32_t streams;       /* search stream pool size (0 = 4)               */
+    uint32_t reserved;
+    uint64_t seed;
+} FvIndexConfig;
+
+#define FV_BUILD_FP16 1u
+#define FV_BUILD_FP8 2u
+#define FV_BUILD_IVF_PQ 4u
+#define FV_BUILD_IVF_SQ8 8u
+
+/* Search engines of the scan path. */
+enum {
+    FV_ENGINE_FLAT = 0,    /* exact fp32 scan (cuda_flat_scan_batch)          */
+    FV_ENGINE_FP16 = 1,    /* fp16 tensor-core scan + fp32 rescore            */
+    FV_ENGINE_FP8 = 2,     /* e4m3 tensor-core scan + fp32 rescore            */
+    FV_ENGINE_IVF_PQ = 3,  /* IvfQuantMode::Pq                                */
+    FV_ENGINE_IVF_SQ8 = 4  /* IvfQuantMode::Sq8                               */
+};
+
+typedef struct {
+    uint32_t engine;       /* FV_ENGINE_*                                     */
+    uint32_t top_k;
+    uint32_t nprobe;       /* IVF                                             */
+    uint32_t rerank_k;     /* IVF                                             */
+    FvScanOptions scan;    /* FP16 / FP8                                      */
+} FvSearchParams;
+
+/* Latency statistics of MetricsTracker::get_stats (metrics.rs:47-90):
+ * per-query amortised batch latency in microseconds, QPS since creation. */
+typedef struct {
+    uint64_t count;
+    double p50_us, p90_us, p99_us, p999_us, min_us, max_us, mean_us, qps;
+} FvLatencyStats;
+
+typedef struct {
+    uint32_t num_vectors;  /* main slots                                      */
+    uint32_t delta_len;    /* live-insert buffer rows                         */
+    uint32_t tombstones;
+    uint32_t dim, padded_dim, nlist, m_pq, metric;
+    uint32_t next_id;
+    uint32_t reserved;
+    uint64_t device_bytes;
+} FvIndexInfo;
+
 #undef FV_ALIGN8
 
 #ifdef __cplusplus
