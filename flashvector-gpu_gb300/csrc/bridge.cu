@@ -367,6 +367,67 @@ int fv_build_ivf_lists(const GpuSearchResult* d_assign, uint32_t num_vectors, ui
   return fv::launch_build_lists(d_assign, num_vectors, nlist, d_out_offsets, d_out_vec_ids, work, s);
 }
 
+// ------------------------------------------------------------ CUDA graphs
+// A captured sequence of this library's calls on one stream, replayed with
+// one launch. The captured calls keep their pointers: refill the same input
+// buffers (queries, masks) before each replay. Scratch must already be large
+// enough when capture starts (make the same call once before capturing), so
+// that nothing is allocated inside the capture.
+}  // extern "C"
+
+struct FvGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  size_t kernels = 0;
+};
+
+extern "C" {
+
+int fv_graph_begin(void* stream) {
+  if (!stream) return FV_ERR_NULL;  // the legacy stream cannot be captured
+  return (int)cudaStreamBeginCapture((cudaStream_t)stream, cudaStreamCaptureModeThreadLocal);
+}
+
+int fv_graph_end(void* stream, FvGraph** out) {
+  if (!stream || !out) return FV_ERR_NULL;
+  FvGraph* g = new FvGraph();
+  cudaError_t e = cudaStreamEndCapture((cudaStream_t)stream, &g->graph);
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  if (e != cudaSuccess) {
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    *out = nullptr;
+    return (int)e;
+  }
+  size_t n = 0;
+  cudaGraphGetNodes(g->graph, nullptr, &n);
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (n) cudaGraphGetNodes(g->graph, nodes.data(), &n);
+  for (auto nd : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++g->kernels;
+  }
+  *out = g;
+  return 0;
+}
+
+int fv_graph_launch(FvGraph* graph, void* stream) {
+  if (!graph) return FV_ERR_NULL;
+  cudaError_t e = cudaGraphLaunch(graph->exec, (cudaStream_t)stream);
+  if (e == cudaSuccess) fv::note_launch((uint32_t)graph->kernels);
+  return (int)e;
+}
+
+uint64_t fv_graph_kernel_count(const FvGraph* graph) { return graph ? graph->kernels : 0; }
+
+int fv_graph_destroy(FvGraph* graph) {
+  if (!graph) return 0;
+  if (graph->exec) cudaGraphExecDestroy(graph->exec);
+  if (graph->graph) cudaGraphDestroy(graph->graph);
+  delete graph;
+  return 0;
+}
+
 // ------------------------------------------------------------- fixtures
 int cuda_compute_distances_warp(const float* d_queries, const float* d_dataset, uint32_t num_queries,
                                 uint32_t num_vectors, uint32_t dim, MetricType metric, float* d_out_distances,

@@ -170,7 +170,10 @@ class Index {
     cudaStreamDestroy(delta_stream_);
   }
 
-  int build(const float* host, uint32_t n);
+  int build(const float* host, uint32_t n) { return build_from(host, n, false, nullptr); }
+  int build_device(const float* d_vectors, uint32_t n, const float* d_init_centroids) {
+    return build_from(d_vectors, n, true, d_init_centroids);
+  }
   int add(const float* host, uint32_t n, uint32_t* out_ids);
   int remove(const uint32_t* ids, uint32_t n, uint32_t* out_deleted);
   int search(const FvSearchParams& p, const float* q, uint32_t nq, bool device_queries, const uint32_t* user_mask,
@@ -178,11 +181,13 @@ class Index {
   void stats(FvLatencyStats* s);
   void info(FvIndexInfo* i);
   int export_ivf(uint32_t what, void* host_out, size_t bytes);
+  int tables(IvfPqGpuTables* pq, IvfSqGpuTables* sq, FvIvfOptions* opt);
 
  private:
-  int build_ivf(cudaStream_t s);
+  int build_from(const float* src, uint32_t n, bool device, const float* d_init_centroids);
+  int build_ivf(cudaStream_t s, const float* d_init_centroids);
   int kmeans(const float* d_x, uint32_t n, uint32_t dim, uint32_t k, uint32_t iters, uint64_t seed, float* d_cent,
-             cudaStream_t s);
+             cudaStream_t s, const float* d_init = nullptr);
   int assign_rows(const float* d_x, uint32_t n, uint32_t dim, const float* d_cent, uint32_t k, GpuSearchResult* out,
                   cudaStream_t s);
   void slot_mask(const uint32_t* user, uint32_t words, std::vector<uint32_t>& out, bool& use) const;
@@ -233,19 +238,23 @@ int Index::assign_rows(const float* d_x, uint32_t n, uint32_t dim, const float* 
 }
 
 int Index::kmeans(const float* d_x, uint32_t n, uint32_t dim, uint32_t k, uint32_t iters, uint64_t seed,
-                  float* d_cent, cudaStream_t s) {
-  std::vector<uint32_t> init = sample_rows(n, k, seed);
+                  float* d_cent, cudaStream_t s, const float* d_init) {
   DevBuf<uint32_t> rows;
   DevBuf<GpuSearchResult> assign;
   DevBuf<uint32_t> counts;
   DevBuf<double> sums;
-  int rc = rows.alloc(init.size());
-  if (!rc) rc = assign.alloc(n);
+  int rc = assign.alloc(n);
   if (!rc) rc = counts.alloc(k);
   if (!rc) rc = sums.alloc((size_t)k * dim);
   if (rc) return rc;
-  cudaMemcpyAsync(rows.p, init.data(), init.size() * 4, cudaMemcpyHostToDevice, s);
-  rc = launch_gather_rows(d_x, rows.p, (uint32_t)init.size(), dim, d_cent, s);
+  if (d_init) {
+    rc = (int)cudaMemcpyAsync(d_cent, d_init, (size_t)k * dim * 4, cudaMemcpyDeviceToDevice, s);
+  } else {
+    std::vector<uint32_t> init = sample_rows(n, k, seed);
+    rc = rows.alloc(init.size());
+    if (!rc) rc = (int)cudaMemcpyAsync(rows.p, init.data(), init.size() * 4, cudaMemcpyHostToDevice, s);
+    if (!rc) rc = launch_gather_rows(d_x, rows.p, (uint32_t)init.size(), dim, d_cent, s);
+  }
   if (rc) return rc;
   for (uint32_t it = 0; it < iters; ++it) {
     rc = assign_rows(d_x, n, dim, d_cent, k, assign.p, s);
@@ -255,9 +264,10 @@ int Index::kmeans(const float* d_x, uint32_t n, uint32_t dim, uint32_t k, uint32
   return (int)cudaStreamSynchronize(s);
 }
 
-int Index::build_ivf(cudaStream_t s) {
+int Index::build_ivf(cudaStream_t s, const float* d_init_centroids) {
   const uint32_t dim = cfg_.dim;
   nlist_ = std::max(1u, std::min(cfg_.nlist, n_));
+  if (d_init_centroids && nlist_ != cfg_.nlist) return FV_ERR_ARG;
   uint32_t train = cfg_.train_rows ? cfg_.train_rows : (uint32_t)std::min<uint64_t>(n_, 256ull * nlist_);
   train = std::max(std::min(train, n_), nlist_);
   int rc = centroids_.alloc((size_t)nlist_ * dim);
@@ -272,7 +282,9 @@ int Index::build_ivf(cudaStream_t s) {
     if (rc) return rc;
     cudaMemcpyAsync(d_rows.p, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice, s);
     rc = launch_gather_rows(vectors_.p, d_rows.p, (uint32_t)rows.size(), dim, sample.p, s);
-    if (!rc) rc = kmeans(sample.p, (uint32_t)rows.size(), dim, nlist_, cfg_.kmeans_iters, cfg_.seed + 2, centroids_.p, s);
+    if (!rc)
+      rc = kmeans(sample.p, (uint32_t)rows.size(), dim, nlist_, d_init_centroids ? cfg_.kmeans_iters_given : cfg_.kmeans_iters,
+                  cfg_.seed + 2, centroids_.p, s, d_init_centroids);
     if (rc) return rc;
   }
   DevBuf<GpuSearchResult> assign;
@@ -331,7 +343,7 @@ int Index::build_ivf(cudaStream_t s) {
   return (int)cudaStreamSynchronize(s);
 }
 
-int Index::build(const float* host, uint32_t n) {
+int Index::build_from(const float* host, uint32_t n, bool device, const float* d_init_centroids) {
   if (!host) return FV_ERR_NULL;
   if (n == 0 || cfg_.dim == 0 || cfg_.dim > 4096) return FV_ERR_ARG;
   std::unique_lock<std::shared_mutex> lk(state_mu_);
@@ -339,15 +351,25 @@ int Index::build(const float* host, uint32_t n) {
   cudaStream_t s = streams_[0]->s;
   std::vector<float> staged;
   const float* src = host;
-  if (cfg_.metric == METRIC_COSINE) {
-    staged.assign(host, host + (size_t)n * dim);
+  if (device && cfg_.metric == METRIC_COSINE) {
+    staged.resize((size_t)n * dim);
+    int rc = (int)cudaMemcpy(staged.data(), host, staged.size() * 4, cudaMemcpyDeviceToHost);
+    if (rc) return rc;
+    device = false;
+    host = staged.data();
+  }
+  if (!device && cfg_.metric == METRIC_COSINE) {
+    if (staged.empty()) staged.assign(host, host + (size_t)n * dim);
     normalize_rows(staged.data(), n, dim);
     src = staged.data();
+  } else {
+    src = host;
   }
   n_ = n;
   int rc = vectors_.alloc((size_t)n * dim);
   if (rc) return rc;
-  rc = (int)cudaMemcpyAsync(vectors_.p, src, (size_t)n * dim * 4, cudaMemcpyHostToDevice, s);
+  rc = (int)cudaMemcpyAsync(vectors_.p, src, (size_t)n * dim * 4,
+                            device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s);
   if (rc) return rc;
   if (cfg_.build_flags & FV_BUILD_FP16) {
     pd16_ = (dim + 15) / 16 * 16;
@@ -365,7 +387,7 @@ int Index::build(const float* host, uint32_t n) {
     if (rc) return rc;
   }
   if (cfg_.nlist && (cfg_.build_flags & (FV_BUILD_IVF_PQ | FV_BUILD_IVF_SQ8))) {
-    rc = build_ivf(s);
+    rc = build_ivf(s, d_init_centroids);
     if (rc) return rc;
   }
   // validity words: every main slot live (index.rs:505-511)
@@ -674,6 +696,18 @@ void Index::info(FvIndexInfo* i) {
                     vec_ids_.bytes();
 }
 
+// Device views of the IVF tables (list-major codes) for direct kernel calls.
+int Index::tables(IvfPqGpuTables* pq, IvfSqGpuTables* sq, FvIvfOptions* opt) {
+  std::shared_lock<std::shared_mutex> lk(state_mu_);
+  if (!built_ || !offsets_.p) return FV_ERR_ARG;
+  if (pq) *pq = IvfPqGpuTables{centroids_.p, codebooks_.p, pq_codes_lm_.p, offsets_.p, vec_ids_.p, vectors_.p, n_,
+                               cfg_.dim,     nlist_,       cfg_.m_pq,      cfg_.m_pq ? cfg_.dim / cfg_.m_pq : 0};
+  if (sq) *sq = IvfSqGpuTables{centroids_.p, sq_mins_.p, sq_scales_.p, sq_codes_lm_.p, offsets_.p, vec_ids_.p,
+                               vectors_.p,   n_,         cfg_.dim,     nlist_};
+  if (opt) *opt = FvIvfOptions{1, {0, 0, 0}};
+  return 0;
+}
+
 // Copies one IVF table to the host (for checking the build against a CPU
 // restatement): 0 centroids, 1 codebooks, 2 pq codes (by id), 3 sq mins,
 // 4 sq scales, 5 sq codes (by id), 6 offsets, 7 vec ids.
@@ -725,6 +759,11 @@ int fv_index_build(FvIndex* index, const float* host_vectors, uint32_t num_vecto
   if (!index) return FV_ERR_NULL;
   return index->impl.build(host_vectors, num_vectors);
 }
+int fv_index_build_device(FvIndex* index, const float* d_vectors, uint32_t num_vectors,
+                          const float* d_init_centroids) {
+  if (!index) return FV_ERR_NULL;
+  return index->impl.build_device(d_vectors, num_vectors, d_init_centroids);
+}
 int fv_index_add(FvIndex* index, const float* host_vectors, uint32_t num_vectors, uint32_t* out_ids) {
   if (!index) return FV_ERR_NULL;
   return index->impl.add(host_vectors, num_vectors, out_ids);
@@ -752,6 +791,10 @@ int fv_index_info(FvIndex* index, FvIndexInfo* out) {
   if (!index || !out) return FV_ERR_NULL;
   index->impl.info(out);
   return 0;
+}
+int fv_index_ivf_tables(FvIndex* index, IvfPqGpuTables* pq, IvfSqGpuTables* sq, FvIvfOptions* options) {
+  if (!index) return FV_ERR_NULL;
+  return index->impl.tables(pq, sq, options);
 }
 int fv_index_export_ivf(FvIndex* index, uint32_t table, void* host_out, size_t bytes) {
   if (!index) return FV_ERR_NULL;

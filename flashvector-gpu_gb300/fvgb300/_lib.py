@@ -54,7 +54,8 @@ class FvScanOptions(C.Structure):
 
 class FvIndexConfig(C.Structure):
     _fields_ = [("dim", U32), ("metric", U32), ("nlist", U32), ("m_pq", U32), ("build_flags", U32),
-                ("kmeans_iters", U32), ("pq_iters", U32), ("train_rows", U32), ("streams", U32), ("reserved", U32),
+                ("kmeans_iters", U32), ("pq_iters", U32), ("train_rows", U32), ("streams", U32),
+                ("kmeans_iters_given", U32),
                 ("seed", C.c_uint64)]
 
 
@@ -111,13 +112,20 @@ SIGNATURES = {
     "fv_index_create": (I32, [P, P]),
     "fv_index_destroy": (I32, [P]),
     "fv_index_build": (I32, [P, P, U32]),
+    "fv_index_build_device": (I32, [P, P, U32, P]),
     "fv_index_add": (I32, [P, P, U32, P]),
     "fv_index_delete": (I32, [P, P, U32, P]),
     "fv_index_search": (I32, [P, P, P, U32, P, U32, P]),
     "fv_index_search_device": (I32, [P, P, P, U32, P]),
     "fv_index_stats": (I32, [P, P]),
     "fv_index_info": (I32, [P, P]),
+    "fv_index_ivf_tables": (I32, [P, P, P, P]),
     "fv_index_export_ivf": (I32, [P, U32, P, SZ]),
+    "fv_graph_begin": (I32, [P]),
+    "fv_graph_end": (I32, [P, P]),
+    "fv_graph_launch": (I32, [P, P]),
+    "fv_graph_kernel_count": (C.c_uint64, [P]),
+    "fv_graph_destroy": (I32, [P]),
     "fv_version": (C.c_char_p, []),
     "fv_read_device_status": (I32, [P]),
     "fv_launch_count": (C.c_uint64, []),

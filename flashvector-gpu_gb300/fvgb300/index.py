@@ -38,13 +38,14 @@ class IndexConfig:
     pq_iters: int = 10
     train_rows: int = 0
     streams: int = 4
+    kmeans_iters_given: int = 0
     seed: int = 0
     max_elements: int = 0  # accepted for signature compatibility; capacity grows on demand
 
     def to_c(self):
         m = METRIC[self.metric] if isinstance(self.metric, str) else int(self.metric)
         return _lib.FvIndexConfig(self.dim, m, self.nlist, self.m_pq, self.build_flags, self.kmeans_iters,
-                                  self.pq_iters, self.train_rows, self.streams, 0, self.seed)
+                                  self.pq_iters, self.train_rows, self.streams, self.kmeans_iters_given, self.seed)
 
 
 def _f32(a):
@@ -79,6 +80,13 @@ class GpuVectorIndex:
         if x.shape[0] == 0:
             raise ValueError("Dataset cannot be empty")
         call("fv_index_build", self._h, x.ctypes.data_as(C.c_void_p), x.shape[0])
+
+    def build_device(self, d_vectors, d_init_centroids=None):
+        """Build from a CUDA tensor of rows; optional CUDA tensor of initial
+        coarse centroids (nlist rows)."""
+        n = d_vectors.shape[0]
+        call("fv_index_build_device", self._h, C.c_void_p(d_vectors.data_ptr()), n,
+             None if d_init_centroids is None else C.c_void_p(d_init_centroids.data_ptr()))
 
     def add_vectors(self, vectors) -> np.ndarray:
         x = _f32(vectors).reshape(-1, self.config.dim)
@@ -147,6 +155,12 @@ class GpuVectorIndex:
 
     def tombstone_count(self) -> int:
         return self.info()["tombstones"]
+
+    def ivf_tables(self):
+        """(IvfPqGpuTables, IvfSqGpuTables, FvIvfOptions) device views."""
+        pq, sq, opt = _lib.IvfPqGpuTables(), _lib.IvfSqGpuTables(), _lib.FvIvfOptions()
+        call("fv_index_ivf_tables", self._h, C.byref(pq), C.byref(sq), C.byref(opt))
+        return pq, sq, opt
 
     def export_ivf(self) -> dict:
         """The built IVF tables as host arrays (for checking the build)."""

@@ -168,3 +168,44 @@ def profile_summary() -> dict:
     buf = C.create_string_buffer(1 << 16)
     call("fv_profile_summary", buf, len(buf))
     return json.loads(buf.value.decode())
+
+
+class Graph:
+    """A captured sequence of library calls on one stream (fv_graph_*).
+
+        g = Graph.capture(lambda: ivf.search(q_buf, 10, 32, 400, out=out_buf), stream)
+        g.launch(stream)   # replays the same calls on the same buffers
+    """
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def capture(cls, fn, stream):
+        s = C.c_void_p(stream.cuda_stream)
+        call("fv_graph_begin", s)
+        try:
+            with torch.cuda.stream(stream):
+                fn()
+        except Exception:
+            h = C.c_void_p()
+            _lib.lib().fv_graph_end(s, C.byref(h))
+            if h.value:
+                _lib.lib().fv_graph_destroy(h)
+            raise
+        h = C.c_void_p()
+        call("fv_graph_end", s, C.byref(h))
+        return cls(h)
+
+    def launch(self, stream):
+        call("fv_graph_launch", self._h, C.c_void_p(stream.cuda_stream))
+
+    @property
+    def kernels(self) -> int:
+        return int(_lib.lib().fv_graph_kernel_count(self._h))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.lib().fv_graph_destroy(h)
+            self._h = None

@@ -199,6 +199,11 @@ typedef struct FvIndex FvIndex;
 int fv_index_create(const FvIndexConfig* config, FvIndex** out);
 int fv_index_destroy(FvIndex* index);
 int fv_index_build(FvIndex* index, const float* host_vectors, uint32_t num_vectors);
+/* Build from rows already in device memory; d_init_centroids (nlist rows,
+ * may be NULL) seeds the coarse k-means, which then runs
+ * config.kmeans_iters_given Lloyd iterations (0 = keep them as given). */
+int fv_index_build_device(FvIndex* index, const float* d_vectors, uint32_t num_vectors,
+                          const float* d_init_centroids);
 int fv_index_add(FvIndex* index, const float* host_vectors, uint32_t num_vectors, uint32_t* out_ids);
 int fv_index_delete(FvIndex* index, const uint32_t* ids, uint32_t count, uint32_t* out_deleted);
 int fv_index_search(FvIndex* index, const FvSearchParams* params, const float* host_queries,
@@ -208,10 +213,28 @@ int fv_index_search_device(FvIndex* index, const FvSearchParams* params, const f
                            uint32_t num_queries, GpuSearchResult* host_out);
 int fv_index_stats(FvIndex* index, FvLatencyStats* out);
 int fv_index_info(FvIndex* index, FvIndexInfo* out);
+/* Device views of the engine's IVF tables (list-major code rows) and the
+ * matching options, for calling fv_ivf_{pq,sq}_search_ex directly (for
+ * example inside a captured CUDA graph). Valid until the next build. */
+int fv_index_ivf_tables(FvIndex* index, IvfPqGpuTables* pq, IvfSqGpuTables* sq, FvIvfOptions* options);
 /* Copies IVF table `table` to host memory: 0 centroids, 1 codebooks, 2 PQ
  * codes by id, 3 SQ8 mins, 4 SQ8 scales, 5 SQ8 codes by id, 6 list offsets,
  * 7 list ids. */
 int fv_index_export_ivf(FvIndex* index, uint32_t table, void* host_out, size_t bytes);
+
+/* ---- CUDA graphs -------------------------------------------------------
+ * Capture the library calls issued on `stream` between fv_graph_begin and
+ * fv_graph_end into one replayable graph (the steady-state search of a fixed
+ * batch shape). Captured calls keep their device pointers: refill the same
+ * query / mask buffers before each fv_graph_launch. Make the same calls once
+ * before capturing so that per-stream scratch is already large enough (no
+ * allocation happens inside a capture). Not for the legacy NULL stream. */
+typedef struct FvGraph FvGraph;
+int fv_graph_begin(void* stream);
+int fv_graph_end(void* stream, FvGraph** out);
+int fv_graph_launch(FvGraph* graph, void* stream);
+uint64_t fv_graph_kernel_count(const FvGraph* graph);
+int fv_graph_destroy(FvGraph* graph);
 
 /* ---- test fixtures -----------------------------------------------------
  * Replace cuda_bridge.h:195-213 (hnsw_traverse.cu:387-437, 694-735). */

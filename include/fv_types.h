@@ -128,7 +128,8 @@ typedef struct {
     uint32_t train_rows;    /* rows sampled to train centroids / codebooks
                                (0 = min(n, 256 * nlist))                       */
     uint32_t streams;       /* search stream pool size (0 = 4)               */
-    uint32_t reserved;
+    uint32_t kmeans_iters_given; /* Lloyd iterations when initial centroids are
+                                    given to fv_index_build_device            */
     uint64_t seed;
 } FvIndexConfig;
 
