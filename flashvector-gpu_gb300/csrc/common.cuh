@@ -13,6 +13,7 @@
 #include <stdint.h>
 
 #include "../../include/fv_types.h"
+#include "kernels.h"
 
 namespace fv {
 
@@ -84,6 +85,29 @@ __host__ __device__ __forceinline__ uint32_t next_pow2_dev(uint32_t v) {
 // filter.rs:364-371).
 __device__ __forceinline__ bool mask_allows(const uint32_t* __restrict__ mask, uint32_t i) {
   return mask == nullptr || ((__ldg(mask + (i >> 5)) >> (i & 31u)) & 1u);
+}
+
+// Query q's filter row (an empty filter when there are no per-query filters).
+__device__ __forceinline__ QueryFilter load_filter(const QueryFilter* __restrict__ f, uint32_t q) {
+  if (f == nullptr) return QueryFilter{nullptr, 0u, 0u};
+  const uint4 v = __ldg(reinterpret_cast<const uint4*>(f + q));
+  QueryFilter r;
+  r.words = reinterpret_cast<const uint32_t*>(((uint64_t)v.y << 32) | v.x);
+  r.nwords = v.z;
+  r.reserved = 0;
+  return r;
+}
+
+// Logical id `id` passes the query's filter.
+__device__ __forceinline__ bool filter_allows(const QueryFilter& f, uint32_t id) {
+  if (f.words == nullptr) return true;
+  return (id >> 5) < f.nwords && ((__ldg(f.words + (id >> 5)) >> (id & 31u)) & 1u);
+}
+
+// The filter word covering ids [32 w, 32 w + 32) (all ones without a filter).
+__device__ __forceinline__ uint32_t filter_word(const QueryFilter& f, uint32_t w) {
+  if (f.words == nullptr) return 0xFFFFFFFFu;
+  return w < f.nwords ? __ldg(f.words + w) : 0u;
 }
 
 __device__ __forceinline__ GpuSearchResult key_to_result(uint64_t key, const uint32_t* __restrict__ vec_ids) {

@@ -25,6 +25,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -33,6 +34,7 @@
 #include <vector>
 
 #include "../../include/fv_bridge.h"
+#include "engine.h"
 #include "kernels.h"
 
 namespace fv {
@@ -138,6 +140,8 @@ struct Delta {
   DevBuf<uint32_t> d_mask;
   DevBuf<GpuSearchResult> d_res;
   PinnedBuf<GpuSearchResult> h_res;
+  std::vector<uint32_t> live;  // validity words over delta slots (tombstones cleared)
+  DevBuf<uint32_t> d_live;
   size_t capacity = 0;
   uint32_t len() const { return (uint32_t)ids.size(); }
 };
@@ -152,12 +156,15 @@ class Index {
     if (cfg_.pq_iters == 0) cfg_.pq_iters = 10;
     const uint32_t ns = cfg_.streams ? cfg_.streams : 4;
     streams_.resize(ns);
+    // blocking streams: work the caller queued on the legacy default stream
+    // (device queries, device rows of a build) is ordered before the
+    // engine's work, as with the reference's pool streams
     for (auto& st : streams_) {
       st = std::make_unique<Stream>();
-      cudaStreamCreateWithFlags(&st->s, cudaStreamNonBlocking);
+      cudaStreamCreateWithFlags(&st->s, cudaStreamDefault);
       cudaEventCreateWithFlags(&st->ready, cudaEventDisableTiming);
     }
-    cudaStreamCreateWithFlags(&delta_stream_, cudaStreamNonBlocking);
+    cudaStreamCreateWithFlags(&delta_stream_, cudaStreamDefault);
   }
   ~Index() {
     cudaDeviceSynchronize();
@@ -183,7 +190,31 @@ class Index {
   int export_ivf(uint32_t what, void* host_out, size_t bytes);
   int tables(IvfPqGpuTables* pq, IvfSqGpuTables* sq, FvIvfOptions* opt);
 
+  // served batches (serve.cpp)
+  void pin() {
+    std::shared_lock<std::shared_mutex> lk(state_mu_);
+    pins_.fetch_add(1);
+  }
+  void unpin() {
+    if (pins_.fetch_sub(1) == 1) {
+      std::lock_guard<std::mutex> g(pin_mu_);
+      pin_cv_.notify_all();
+    }
+  }
+  int launch_batch(const BatchLaunch& b, cudaStream_t s);
+  uint32_t dim() const { return cfg_.dim; }
+  int metric() const { return (int)cfg_.metric; }
+  bool built() const { return built_; }
+  uint32_t nlist() const { return nlist_; }
+
  private:
+  // called by writers holding state_mu_ exclusively: no new pin can start,
+  // wait for the batches in flight to release theirs
+  void wait_unpinned() {
+    std::unique_lock<std::mutex> g(pin_mu_);
+    pin_cv_.wait(g, [&] { return pins_.load() == 0; });
+  }
+  int upload_delta_live(cudaStream_t s);
   int build_from(const float* src, uint32_t n, bool device, const float* d_init_centroids);
   int build_ivf(cudaStream_t s, const float* d_init_centroids);
   int kmeans(const float* d_x, uint32_t n, uint32_t dim, uint32_t k, uint32_t iters, uint64_t seed, float* d_cent,
@@ -215,6 +246,10 @@ class Index {
   std::unordered_set<uint32_t> tombstones_;
   uint32_t next_id_ = 0;
   Delta delta_;
+
+  std::atomic<int> pins_{0};
+  std::mutex pin_mu_;
+  std::condition_variable pin_cv_;
 
   std::mutex metrics_mu_;
   std::vector<double> lat_us_;
@@ -347,8 +382,14 @@ int Index::build_from(const float* host, uint32_t n, bool device, const float* d
   if (!host) return FV_ERR_NULL;
   if (n == 0 || cfg_.dim == 0 || cfg_.dim > 4096) return FV_ERR_ARG;
   std::unique_lock<std::shared_mutex> lk(state_mu_);
+  wait_unpinned();
   const uint32_t dim = cfg_.dim;
   cudaStream_t s = streams_[0]->s;
+  if (device) {
+    // device rows may still be in production on any stream of the caller
+    const int rc = (int)cudaDeviceSynchronize();
+    if (rc) return rc;
+  }
   std::vector<float> staged;
   const float* src = host;
   if (device && cfg_.metric == METRIC_COSINE) {
@@ -401,6 +442,7 @@ int Index::build_from(const float* host, uint32_t n, bool device, const float* d
   tombstones_.clear();
   delta_.vectors.clear();
   delta_.ids.clear();
+  delta_.live.clear();
   next_id_ = n;
   built_ = true;
   return 0;
@@ -421,6 +463,7 @@ int Index::add(const float* host, uint32_t n, uint32_t* out_ids) {
     }
   }
   std::unique_lock<std::shared_mutex> lk(state_mu_);
+  wait_unpinned();
   const uint32_t dim = cfg_.dim;
   const size_t off = delta_.vectors.size();
   delta_.vectors.insert(delta_.vectors.end(), host, host + (size_t)n * dim);
@@ -438,15 +481,24 @@ int Index::add(const float* host, uint32_t n, uint32_t* out_ids) {
     rc = delta_.d_vectors.alloc(cap * dim);
     if (!rc) rc = delta_.d_ids.alloc(cap);
     if (!rc) rc = delta_.d_mask.alloc((cap + 31) / 32);
+    if (!rc) rc = delta_.d_live.alloc((cap + 31) / 32);
     if (rc) return rc;
     delta_.capacity = cap;
   }
+  delta_.live.resize((len + 31) / 32, 0u);
+  for (size_t i = len - n; i < len; ++i) delta_.live[i >> 5] |= 1u << (i & 31);
   rc = (int)cudaMemcpyAsync(delta_.d_vectors.p, delta_.vectors.data(), delta_.vectors.size() * 4,
                             cudaMemcpyHostToDevice, delta_stream_);
   if (!rc)
     rc = (int)cudaMemcpyAsync(delta_.d_ids.p, delta_.ids.data(), len * 4, cudaMemcpyHostToDevice, delta_stream_);
+  if (!rc) rc = upload_delta_live(delta_stream_);
   if (!rc) rc = (int)cudaStreamSynchronize(delta_stream_);
   return rc;
+}
+
+int Index::upload_delta_live(cudaStream_t s) {
+  if (delta_.live.empty()) return 0;
+  return (int)cudaMemcpyAsync(delta_.d_live.p, delta_.live.data(), delta_.live.size() * 4, cudaMemcpyHostToDevice, s);
 }
 
 int Index::remove(const uint32_t* ids, uint32_t n, uint32_t* out_deleted) {
@@ -455,15 +507,20 @@ int Index::remove(const uint32_t* ids, uint32_t n, uint32_t* out_deleted) {
   if (n == 0) return 0;
   if (!ids) return FV_ERR_NULL;
   std::unique_lock<std::shared_mutex> lk(state_mu_);
+  wait_unpinned();
   if (!built_) return 0;
   std::unordered_set<uint32_t> in_delta(delta_.ids.begin(), delta_.ids.end());
   uint32_t deleted = 0;
-  bool main_dirty = false;
+  bool main_dirty = false, delta_dirty = false;
   for (uint32_t i = 0; i < n; ++i) {
     const uint32_t lid = ids[i];
     if (tombstones_.count(lid)) continue;
     if (in_delta.count(lid)) {
       tombstones_.insert(lid);
+      // delta ids are assigned in increasing order: the slot is the rank
+      const size_t pos = (size_t)(std::lower_bound(delta_.ids.begin(), delta_.ids.end(), lid) - delta_.ids.begin());
+      delta_.live[pos >> 5] &= ~(1u << (pos & 31));
+      delta_dirty = true;
       ++deleted;
       continue;
     }
@@ -479,6 +536,11 @@ int Index::remove(const uint32_t* ids, uint32_t n, uint32_t* out_deleted) {
     int rc = (int)cudaMemcpyAsync(valid_words_.p, main_valid_.data(), main_valid_.size() * 4, cudaMemcpyHostToDevice,
                                   s);
     if (!rc) rc = (int)cudaStreamSynchronize(s);
+    if (rc) return rc;
+  }
+  if (delta_dirty) {
+    int rc = upload_delta_live(delta_stream_);
+    if (!rc) rc = (int)cudaStreamSynchronize(delta_stream_);
     if (rc) return rc;
   }
   *out_deleted = deleted;
@@ -647,6 +709,88 @@ int Index::search(const FvSearchParams& p, const float* q, uint32_t nq, bool dev
   return 0;
 }
 
+// ------------------------------------------------------- served batches
+// One heterogeneous batch on the caller's stream, with the semantics of
+// search() for every query taken alone: the main scan (shared validity
+// words for tombstones, per-query filters over logical ids), the delta
+// scan of the live-insert buffer (validity words over delta slots, filters
+// through the delta ids) and the stable merge, all stream-ordered.
+int Index::launch_batch(const BatchLaunch& b, cudaStream_t s) {
+  if (!built_) return FV_ERR_ARG;
+  if (b.nq == 0 || b.top_k == 0) return 0;
+  if (b.top_k > 256) return FV_ERR_ARG;
+  if (!b.d_queries || !b.d_out) return FV_ERR_NULL;
+  const bool ivf = b.engine == FV_ENGINE_IVF_PQ || b.engine == FV_ENGINE_IVF_SQ8;
+  if (!ivf && (b.d_topk || b.d_nprobe || b.d_rerank)) return FV_ERR_ARG;
+  const bool has_delta = delta_.len() > 0;
+  if (has_delta && (!b.d_main || !b.d_delta)) return FV_ERR_NULL;
+  const uint32_t dim = cfg_.dim, k = b.top_k, nq = b.nq;
+  const MetricType metric = (MetricType)cfg_.metric;
+  GpuSearchResult* main_out = has_delta ? b.d_main : b.d_out;
+  const uint32_t* shared_mask = tombstones_.empty() ? nullptr : valid_words_.p;
+  int rc = 0;
+  switch (b.engine) {
+    case FV_ENGINE_FLAT:
+      rc = launch_flat_f32(vectors_.p, nullptr, n_, dim, b.d_queries, nq, k, metric, shared_mask, main_out, 0, s,
+                           b.d_filters);
+      break;
+    case FV_ENGINE_FP16:
+    case FV_ENGINE_FP8: {
+      const bool fp8 = b.engine == FV_ENGINE_FP8;
+      if (fp8 ? !fp8_.p : !fp16_.p) return FV_ERR_ARG;
+      const TcTables t = fp8 ? TcTables{true, fp8_.p, fp8_norms_.p, fp8_scales_.p, vectors_.p, n_, dim, pd8_}
+                             : TcTables{false, fp16_.p, norms16_.p, nullptr, vectors_.p, n_, dim, pd16_};
+      rc = launch_tc_scan(t, b.d_queries, nq, k, metric, shared_mask, main_out, b.scan, s, b.d_filters);
+      break;
+    }
+    case FV_ENGINE_IVF_PQ:
+    case FV_ENGINE_IVF_SQ8: {
+      const bool pq = b.engine == FV_ENGINE_IVF_PQ;
+      if (pq ? !pq_codes_lm_.p : !sq_codes_lm_.p) return FV_ERR_ARG;
+      IvfLaunch L{};
+      L.centroids = centroids_.p;
+      L.codebooks = pq ? codebooks_.p : nullptr;
+      L.sq_mins = pq ? nullptr : sq_mins_.p;
+      L.sq_scales = pq ? nullptr : sq_scales_.p;
+      L.codes = pq ? pq_codes_lm_.p : sq_codes_lm_.p;
+      L.offsets = offsets_.p;
+      L.vec_ids = vec_ids_.p;
+      L.vectors = vectors_.p;
+      L.num_vectors = n_;
+      L.dim = dim;
+      L.nlist = nlist_;
+      L.m_pq = pq ? cfg_.m_pq : 0;
+      L.sub_dim = pq ? dim / cfg_.m_pq : 0;
+      L.list_major = true;
+      L.queries = b.d_queries;
+      L.nq = nq;
+      L.top_k = k;
+      L.nprobe = b.nprobe;
+      L.rerank_k = b.rerank_k;
+      L.metric = metric;
+      L.mask = shared_mask;
+      L.out = main_out;
+      L.q_topk = b.d_topk;
+      L.q_nprobe = b.d_nprobe;
+      L.q_rerank = b.d_rerank;
+      L.filters = b.d_filters;
+      if (nlist_ == 0 || (pq && cfg_.m_pq == 0)) {
+        rc = launch_fill_sentinel(main_out, (size_t)nq * k, s);
+        break;
+      }
+      rc = launch_ivf_search(pq ? 0 : 1, L, s);
+      break;
+    }
+    default:
+      return FV_ERR_ARG;
+  }
+  if (rc || !has_delta) return rc;
+  rc = launch_flat_f32(delta_.d_vectors.p, delta_.d_ids.p, delta_.len(), dim, b.d_queries, nq, k, metric,
+                       delta_.d_live.p, b.d_delta, 0, s, b.d_filters);
+  if (rc) return rc;
+  return launch_merge_main_delta(b.d_main, b.d_delta, nq, k, b.d_topk, k, b.d_out, s);
+}
+
 // ------------------------------------------------------------- metrics
 void Index::record(double seconds, uint32_t nq) {
   std::lock_guard<std::mutex> lk(metrics_mu_);
@@ -738,6 +882,20 @@ struct FvIndex {
   fv::Index impl;
   explicit FvIndex(const FvIndexConfig& c) : impl(c) {}
 };
+
+namespace fv {
+Index* index_of(FvIndex* handle) { return handle ? &handle->impl : nullptr; }
+uint32_t index_dim(const Index* index) { return index->dim(); }
+int index_metric(const Index* index) { return index->metric(); }
+bool index_built(const Index* index) { return index->built(); }
+void index_prepare_queries(const Index* index, float* rows, uint32_t n) {
+  if (index->metric() == METRIC_COSINE) normalize_rows(rows, n, index->dim());
+}
+uint32_t index_nlist(const Index* index) { return index->nlist(); }
+void index_pin(Index* index) { index->pin(); }
+void index_unpin(Index* index) { index->unpin(); }
+int index_launch_batch(Index* index, const BatchLaunch& b, cudaStream_t stream) { return index->launch_batch(b, stream); }
+}  // namespace fv
 
 extern "C" {
 

@@ -43,6 +43,7 @@ struct FlatArgs {
   GpuSearchResult* out;   // written directly when splits == 1
   uint64_t* partial;      // [nq][splits][k] heap dumps when splits > 1
   uint32_t splits, tiles_per_split;
+  const QueryFilter* filters;  // per-query filters over logical ids (vec_ids[slot], or slot), or null
 };
 
 __device__ __forceinline__ void heap_replace_root(uint64_t* heap, int k, int lane_stride, uint64_t key) {
@@ -122,6 +123,12 @@ __global__ void __launch_bounds__(NT) flat_f32_scan_kernel(FlatArgs a) {
   __syncthreads();
 
   uint64_t worst = kSentinelKey;  // cached heap root of query `tid` (tid < QT)
+  QueryFilter qf[4];              // filters of this thread's four queries
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const uint32_t q = q0 + ty * 4 + i;
+    qf[i] = (a.filters && q < a.nq) ? load_filter(a.filters, q) : QueryFilter{nullptr, 0u, 0u};
+  }
 
   for (uint32_t t = t_begin; t < t_end; ++t) {
     const uint32_t v0 = t * VT;
@@ -237,6 +244,7 @@ __global__ void __launch_bounds__(NT) flat_f32_scan_kernel(FlatArgs a) {
         }
         const uint32_t slot = v0 + vi;
         bool ok = slot < a.n && mask_allows(a.mask, slot);
+        if (ok && a.filters) ok = filter_allows(qf[i], a.vec_ids ? __ldg(a.vec_ids + slot) : slot);
         ds[qi * VS + vi] = ok ? dist : __int_as_float(0x7fc00000);  // NaN never passes `<`
       }
     }
@@ -313,7 +321,7 @@ FlatPlan plan_flat_f32(uint32_t n, uint32_t nq, uint32_t k, uint32_t forced_spli
 
 int launch_flat_f32(const float* vectors, const uint32_t* vec_ids, uint32_t n, uint32_t dim, const float* queries,
                     uint32_t nq, uint32_t k, MetricType metric, const uint32_t* mask, GpuSearchResult* out,
-                    uint32_t forced_splits, cudaStream_t stream) {
+                    uint32_t forced_splits, cudaStream_t stream, const QueryFilter* filters) {
   const FlatPlan p = plan_flat_f32(n, nq, k, forced_splits);
   void* scratch = nullptr;
   if (p.scratch_bytes) {
@@ -321,16 +329,17 @@ int launch_flat_f32(const float* vectors, const uint32_t* vec_ids, uint32_t n, u
     if (!scratch) return (int)cudaErrorMemoryAllocation;
   }
   return launch_flat_f32_planned(p, vectors, vec_ids, n, dim, queries, nq, k, metric, mask, out, false, scratch,
-                                 stream);
+                                 stream, filters);
 }
 
 int launch_flat_f32_planned(const FlatPlan& p, const float* vectors, const uint32_t* vec_ids, uint32_t n,
                             uint32_t dim, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
                             const uint32_t* mask, GpuSearchResult* out, bool fused, void* scratch,
-                            cudaStream_t stream) {
+                            cudaStream_t stream, const QueryFilter* filters) {
   const uint32_t nqb = (nq + QT - 1) / QT;
   const uint32_t splits = p.splits, tps = p.tiles_per_split;
-  FlatArgs a{vectors, vec_ids, n, dim, queries, nq, k, mask, out, static_cast<uint64_t*>(scratch), splits, tps};
+  FlatArgs a{vectors, vec_ids, n, dim, queries, nq, k, mask, out, static_cast<uint64_t*>(scratch), splits, tps,
+             filters};
   if (splits > 1 && !a.partial) return (int)cudaErrorMemoryAllocation;
 
   const size_t smem = flat_f32_smem_bytes(k);

@@ -56,15 +56,31 @@ struct IvfArgs {
   const float* vectors;     // fp32 rows (rerank) or null
   uint32_t num_vectors, dim, nlist, m_pq, sub_dim, code_bytes;
   const float* queries;
-  uint32_t nq, top_k, nprobe, shortlist, list_major, do_rerank;
+  uint32_t nq, top_k, nprobe, rerank_k, list_major;
   int metric;
   const uint32_t* mask;
+  const uint32_t* q_topk;         // per-query top_k / nprobe / rerank_k, or null (uniform)
+  const uint32_t* q_nprobe;
+  const uint32_t* q_rerank;
+  const QueryFilter* filters;     // per-query filters over ids, or null
   const GpuSearchResult* probes;  // [nq][nprobe] coarse result (id = list)
   uint32_t* work;                 // work counter (zeroed before the launch)
   GpuSearchResult* out;
   uint32_t* status;
-  uint32_t keys_pow2;             // pow2(shortlist + IVF_BUF)
+  uint32_t keys_pow2;             // pow2(largest shortlist + IVF_BUF)
 };
+
+// The reference's clamps (ivf_pq_lookup.cu:351-362) for one query: returns
+// the shortlist length; top_k and nprobe are clamped in place.
+__host__ __device__ __forceinline__ uint32_t ivf_clamps(uint32_t& top_k, uint32_t& nprobe, uint32_t rerank_k,
+                                                        uint32_t nlist) {
+  top_k = top_k < (uint32_t)kMaxTopK ? top_k : (uint32_t)kMaxTopK;
+  nprobe = nprobe == 0 ? 1u : nprobe;
+  nprobe = nprobe < nlist ? nprobe : nlist;
+  uint32_t s = rerank_k == 0 ? top_k : rerank_k;
+  s = s > top_k ? s : top_k;
+  return s < MAX_SHORTLIST ? s : MAX_SHORTLIST;
+}
 
 struct IvfSmem {
   // [keys_pow2] u64 keys | LUT (PQ: m*256 f32) or residual+mins+scales (SQ8: 3*dim f32) | query (dim f32)
@@ -133,7 +149,6 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
   __shared__ uint64_t s_tau;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t S = a.shortlist;
   const bool vec16 = (a.code_bytes % 16u) == 0 && ((uintptr_t)a.codes % 16u) == 0;
   float* mins = tab + a.dim;      // SQ8 only
   float* scales = tab + 2 * a.dim;
@@ -151,6 +166,14 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
     __syncthreads();
     const uint32_t q = s_q;
     if (q >= a.nq) break;
+    uint32_t kq = a.q_topk ? __ldg(a.q_topk + q) : a.top_k;
+    uint32_t npq = a.q_nprobe ? __ldg(a.q_nprobe + q) : a.nprobe;
+    const uint32_t rrq = a.q_rerank ? __ldg(a.q_rerank + q) : a.rerank_k;
+    const uint32_t S = ivf_clamps(kq, npq, rrq, a.nlist);
+    npq = min(npq, a.nprobe);
+    kq = min(kq, a.top_k);
+    const bool do_rerank = rrq != 1u && a.vectors != nullptr;
+    const QueryFilter qf = load_filter(a.filters, q);
 
     const float* qv = a.queries + (size_t)q * a.dim;
     for (uint32_t d = tid; d < a.dim; d += IVF_THREADS) qs[d] = __ldg(qv + d);
@@ -174,7 +197,7 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
       __syncthreads();
     };
 
-    for (uint32_t p = 0; p < a.nprobe; ++p) {
+    for (uint32_t p = 0; p < npq; ++p) {
       const uint32_t l = a.probes[(size_t)q * a.nprobe + p].id;
       if (l >= a.nlist) continue;  // uniform over the block
       const float* cent = a.centroids + (size_t)l * a.dim;
@@ -201,7 +224,7 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
         const uint32_t i = base + tid;
         if (i < end) {
           const uint32_t vid = __ldg(a.vec_ids + i);
-          if (mask_allows(a.mask, vid)) {
+          if (mask_allows(a.mask, vid) && filter_allows(qf, vid)) {
             const uint8_t* row = a.codes + (size_t)(a.list_major ? i : vid) * a.code_bytes;
             const float d = MODE == IVF_PQ ? adc_row(tab, row, a.m_pq, vec16)
                                            : sq8_row(tab, mins, scales, row, a.dim, vec16);
@@ -221,7 +244,7 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
     }
     flush();
 
-    if (a.do_rerank) {
+    if (do_rerank) {
       for (uint32_t c = warp; c < S; c += IVF_THREADS / 32) {
         const uint64_t key = keys[c];
         if (key == kSentinelKey) continue;
@@ -236,7 +259,7 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
       block_bitonic_sort(keys, p2);
     }
     for (uint32_t r = tid; r < a.top_k; r += IVF_THREADS)
-      a.out[(size_t)q * a.top_k + r] = key_to_result(r < S ? keys[r] : kSentinelKey, nullptr);
+      a.out[(size_t)q * a.top_k + r] = key_to_result(r < S && r < kq ? keys[r] : kSentinelKey, nullptr);
   }
 }
 
@@ -257,14 +280,12 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   if (L.nq == 0 || L.top_k == 0 || L.nlist == 0) return 0;
   if (mode == IVF_PQ && L.m_pq == 0) return 0;
   if (L.dim == 0) return 0;
-  const uint32_t top_k = std::min(L.top_k, (uint32_t)kMaxTopK);
-  uint32_t nprobe = L.nprobe == 0 ? 1u : L.nprobe;
-  nprobe = std::min(nprobe, L.nlist);
+  // uniform batch: the clamps of the call; heterogeneous batch: top_k,
+  // nprobe and rerank_k are the batch maxima and bound every query's values
+  uint32_t top_k = L.top_k, nprobe = L.nprobe;
+  uint32_t shortlist = ivf_clamps(top_k, nprobe, L.rerank_k, L.nlist);
+  if (L.q_rerank) shortlist = std::min(std::max(std::max(L.rerank_k, top_k), shortlist), MAX_SHORTLIST);
   if (nprobe > (uint32_t)kMaxTopK) return FV_ERR_ARG;  // coarse selection keeps <= 256 lists
-  uint32_t shortlist = L.rerank_k == 0 ? top_k : L.rerank_k;
-  shortlist = std::max(shortlist, top_k);
-  shortlist = std::min(shortlist, MAX_SHORTLIST);
-  const bool do_rerank = L.rerank_k != 1u && L.vectors != nullptr;
   if (mode == IVF_PQ && (L.sub_dim == 0 || L.m_pq * L.sub_dim > L.dim)) return FV_ERR_ARG;
 
   // scratch: coarse heaps | probes | work counter
@@ -301,11 +322,14 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   a.nq = L.nq;
   a.top_k = top_k;
   a.nprobe = nprobe;
-  a.shortlist = shortlist;
+  a.rerank_k = L.rerank_k;
   a.list_major = L.list_major ? 1u : 0u;
-  a.do_rerank = do_rerank ? 1u : 0u;
   a.metric = (int)L.metric;
   a.mask = L.mask;
+  a.q_topk = L.q_topk;
+  a.q_nprobe = L.q_nprobe;
+  a.q_rerank = L.q_rerank;
+  a.filters = L.filters;
   a.probes = probes;
   a.work = work;
   a.out = L.out;

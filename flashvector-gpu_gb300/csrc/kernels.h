@@ -23,6 +23,18 @@ inline uint32_t next_pow2(uint32_t v) {
   return v + 1;
 }
 
+// Per-query filter of a heterogeneous batch: packed LSB-first words over
+// logical ids, one row per query (rows may be shared). Ids at or beyond
+// nwords * 32 are filtered out, the rule the reference applies to words past
+// the end of a user mask (index.rs:1264-1292). words == nullptr: no filter.
+// Kernels take a device array of these (nullptr: no per-query filters); it
+// is applied on top of the shared slot-validity mask.
+struct QueryFilter {
+  const uint32_t* words;
+  uint32_t nwords;
+  uint32_t reserved;
+};
+
 // Streaming-multiprocessor count of the current device (cached per device).
 int device_sm_count();
 
@@ -77,10 +89,10 @@ FlatPlan plan_flat_f32(uint32_t n, uint32_t nq, uint32_t k, uint32_t forced_spli
 int launch_flat_f32_planned(const FlatPlan& p, const float* vectors, const uint32_t* vec_ids, uint32_t n,
                             uint32_t dim, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
                             const uint32_t* mask, GpuSearchResult* out, bool fused, void* scratch,
-                            cudaStream_t stream);
+                            cudaStream_t stream, const QueryFilter* filters = nullptr);
 int launch_flat_f32(const float* vectors, const uint32_t* vec_ids, uint32_t n, uint32_t dim, const float* queries,
                     uint32_t nq, uint32_t k, MetricType metric, const uint32_t* mask, GpuSearchResult* out,
-                    uint32_t forced_splits, cudaStream_t stream);
+                    uint32_t forced_splits, cudaStream_t stream, const QueryFilter* filters = nullptr);
 
 // tensor-core flat scans (tc_scan.cu)
 struct TcTables {
@@ -97,7 +109,8 @@ cudaError_t dispatch_tc_scan_fp16(int kl, int metric, const CUtensorMap& ta, con
 cudaError_t dispatch_tc_scan_fp8(int kl, int metric, const CUtensorMap& ta, const CUtensorMap& tb,
                                  const TcScanArgs& a, uint32_t grid, cudaStream_t stream);
 int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
-                   const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream);
+                   const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream,
+                   const QueryFilter* filters = nullptr);
 
 // IVF-PQ / IVF-SQ8 search (ivf.cu)
 struct IvfLaunch {
@@ -116,10 +129,24 @@ struct IvfLaunch {
   MetricType metric;
   const uint32_t* mask;
   GpuSearchResult* out;
+  // heterogeneous batches (all optional): per-query top_k / nprobe / rerank_k
+  // (top_k, nprobe and rerank_k above are then their maxima; results are
+  // written with a stride of top_k), per-query filters over logical ids
+  const uint32_t* q_topk;
+  const uint32_t* q_nprobe;
+  const uint32_t* q_rerank;
+  const QueryFilter* filters;
 };
 int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream);  // mode 0 = PQ, 1 = SQ8
 int launch_relayout_codes(const uint8_t* by_id, const uint32_t* vec_ids, uint32_t n, uint32_t row_bytes,
                           uint8_t* by_list, cudaStream_t stream);
+
+// main + live-insert merge of a served batch (batch.cu): per query the
+// stable merge of the two answer rows (stride `stride`), truncated to the
+// query's k (q_topk[q], or top_k), padded with {u32::MAX, +inf}
+int launch_merge_main_delta(const GpuSearchResult* main_res, const GpuSearchResult* delta_res, uint32_t nq,
+                            uint32_t stride, const uint32_t* q_topk, uint32_t top_k, GpuSearchResult* out,
+                            cudaStream_t stream);
 
 // IVF index build (index_build.cu)
 int launch_kmeans_update(const float* x, uint32_t n, uint32_t dim, const GpuSearchResult* assign, uint32_t k,

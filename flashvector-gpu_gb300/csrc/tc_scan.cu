@@ -237,7 +237,8 @@ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 }  // namespace
 
 int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
-                   const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream) {
+                   const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream,
+                   const QueryFilter* filters) {
   const bool fp8 = t.fp8;
   const uint32_t elem = fp8 ? 1 : 2;
   const uint32_t kb_elems = fp8 ? 128 : 64;
@@ -311,6 +312,7 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   a.kl = kl;
   a.share = kl == shortlist ? 1u : 0u;
   a.status = status_word();
+  a.filters = filters;
   cudaError_t e;
   {
     ProfScope ps(fp8 ? "tc_scan_fp8" : "tc_scan_fp16", stream);

@@ -52,6 +52,7 @@ struct TcScanArgs {
   uint32_t kl;           // heap entries used (<= KL); == shortlist when the bound is shared
   uint32_t share;        // 1: the CTAs of a query share the slot bound (kl == shortlist)
   uint32_t* status;
+  const QueryFilter* filters;  // per-query filters over slots (== logical ids), or null
 };
 
 template <int KL, int STAGES>
@@ -231,6 +232,7 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
     const int kl = (int)a.kl;
     for (int i = 0; i < kl; ++i) h[i * TC_M] = kSentinelKey;
     const float qn = qvalid ? __ldg(a.qnorm + q) : 0.f;
+    const QueryFilter qf = (a.filters && qvalid) ? load_filter(a.filters, q) : QueryFilter{nullptr, 0u, 0u};
     const float qs = (FP8 && qvalid) ? __ldg(a.qscale + q) : 1.f;
     float worst = kSentinelDist;  // this CTA's kl-th best distance (1e30 until the heap is full)
     float bound = kSentinelDist;  // shared bound: max over the query's slots
@@ -284,11 +286,16 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
 #pragma unroll 1
       for (int c0 = 0; c0 < TC_N; c0 += 64) {
         uint32_t ra[32], rb[32];
+        __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent insertions
         tc::tmem_ld32_async(t_row + c0, ra);
         tc::tmem_ld32_async(t_row + c0 + 32, rb);
+        uint64_t mw = qvalid ? ((uint64_t)cm[(c0 >> 5) + 1] << 32 | cm[c0 >> 5]) : 0ull;
+        if (qf.words) {
+          const uint32_t w0 = (v0 + (uint32_t)c0) >> 5;
+          mw &= ((uint64_t)filter_word(qf, w0 + 1) << 32) | filter_word(qf, w0);
+        }
         tc::tmem_wait_ld(ra);
         tc::reg_fence(rb);
-        const uint64_t mw = qvalid ? ((uint64_t)cm[(c0 >> 5) + 1] << 32 | cm[c0 >> 5]) : 0ull;
         if (mw == 0ull) continue;
         // exact per-column distances (the expressions the insertion test
         // uses); v[0..32) columns c0.., v[32..64) columns c0+32..

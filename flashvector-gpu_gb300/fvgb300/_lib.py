@@ -74,7 +74,31 @@ class FvIndexInfo(C.Structure):
                                    "metric", "next_id", "reserved")] + [("device_bytes", C.c_uint64)]
 
 
-# name -> (restype, argtypes); every function declared in include/fv_bridge.h
+class FvServeConfig(C.Structure):
+    _fields_ = [("max_batch", U32), ("max_wait_us", U32), ("inflight", U32), ("group_by_params", U32),
+                ("queue_capacity", U32), ("reserved", U32 * 3)]
+
+
+class FvRequest(C.Structure):
+    _fields_ = [("engine", U32), ("top_k", U32), ("nprobe", U32), ("rerank_k", U32), ("filter_id", C.c_int32),
+                ("reserved", U32)]
+
+
+class FvServeStats(C.Structure):
+    _fields_ = [("total_requests", C.c_uint64), ("total_batches", C.c_uint64), ("avg_batch_size", C.c_double),
+                ("completed", C.c_uint64), ("failed", C.c_uint64)] + \
+               [(n, C.c_double) for n in ("qps", "p50_us", "p90_us", "p99_us", "p999_us", "max_us", "mean_us",
+                                          "queue_p50_us", "queue_p99_us")] + \
+               [("max_inflight", U32), ("reserved", U32)]
+
+
+# int (*)(void* user, const FvRequest*, const float* queries, uint32_t nq, uint32_t dim, uint32_t k_stride,
+#         GpuSearchResult* out)
+FvServeExecutor = C.CFUNCTYPE(I32, P, C.POINTER(FvRequest), C.POINTER(F32), U32, U32, U32,
+                              C.POINTER(GpuSearchResult))
+
+
+# name -> (restype, argtypes); every function declared in include/fv_bridge.h and include/fv_serve.h
 SIGNATURES = {
     "cuda_init_device": (I32, [I32]),
     "cuda_set_device": (I32, [I32]),
@@ -133,6 +157,16 @@ SIGNATURES = {
     "fv_profile_summary": (I32, [C.c_char_p, SZ]),
     "fv_set_stream_scratch": (I32, [P, P, SZ]),
     "fv_release_stream_scratch": (I32, [P]),
+    "fv_serve_create": (I32, [P, P, P]),
+    "fv_serve_create_with_executor": (I32, [U32, P, FvServeExecutor, P, P]),
+    "fv_serve_destroy": (I32, [P]),
+    "fv_serve_add_filter": (I32, [P, P, U32, P]),
+    "fv_serve_remove_filter": (I32, [P, C.c_int32]),
+    "fv_serve_submit": (I32, [P, P, P, P]),
+    "fv_serve_wait": (I32, [P, C.c_uint64, P, U32, U32, P]),
+    "fv_serve_replay": (I32, [P, P, P, P, U32, P, U32, P]),
+    "fv_serve_stats": (I32, [P, P]),
+    "fv_serve_reset_stats": (I32, [P]),
 }
 
 _lib = None

@@ -33,6 +33,7 @@ extern "C" {
 #define FV_ERR_NOMEM (-4)      /* scratch admission refused                   */
 #define FV_ERR_ARCH (-5)       /* device is not sm_103 / sm_100 class         */
 #define FV_ERR_SCRATCH_LIMIT (-6) /* work exceeds a fixed scratch area's size  */
+#define FV_ERR_QUEUE_FULL (-7)    /* serving loop: admission queue at capacity */
 
 /* ---- device, memory and stream plumbing -------------------------------
  * Replace cuda_bridge.h:11-31 (hnsw_traverse.cu:525-637). */

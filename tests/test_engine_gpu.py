@@ -180,3 +180,21 @@ def test_metrics_and_argument_errors(cuda):
         idx.batch_search_flat(x[:1], 1, 300)  # top_k > 256 (index.rs:322)
     with pytest.raises(ValueError):
         idx.build(np.zeros((0, 32), np.float32))  # test_bindings.py:79-86
+
+
+def test_build_device_orders_after_the_producer(cuda):
+    """Rows still being produced on the caller's stream when build_device is
+    called are copied only once they are complete."""
+    torch = cuda
+    from fvgb300.index import BUILD_FP16, GpuVectorIndex, IndexConfig
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(3)
+    x = torch.randn((2_000_000, 64), generator=g, device="cuda")
+    for _ in range(20):  # more queued work on the producer's stream
+        x = x * 1.0001 + 0.001
+    idx = GpuVectorIndex(IndexConfig(dim=64, nlist=0, build_flags=BUILD_FP16))
+    idx.build_device(x)
+    q = x[[123, 1_999_999]].cpu().numpy()
+    ids, _ = idx.batch_search_flat(q, 2, 1)
+    assert ids[:, 0].tolist() == [123, 1_999_999]

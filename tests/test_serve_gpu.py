@@ -1,0 +1,120 @@
+"""The serving loop on the GPU: every answer served in a mixed batch is
+the answer the engine's blocking search gives that request alone
+(fv_index_search: same clamps, filter AND tombstones, live-insert merge)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def gen_clustered(n, dim, clusters, seed, sigma=0.25):
+    rng = np.random.default_rng(seed)
+    centers = rng.uniform(-1, 1, size=(clusters, dim)).astype(np.float32)
+    return (centers[np.arange(n) % clusters] + np.float32(sigma) * rng.standard_normal((n, dim))).astype(np.float32)
+
+
+@pytest.fixture(scope="module")
+def served(cuda):
+    from fvgb300.index import BUILD_FP8, BUILD_FP16, BUILD_IVF_PQ, BUILD_IVF_SQ8, GpuVectorIndex, IndexConfig
+
+    x = gen_clustered(6000, 64, 24, 11)
+    idx = GpuVectorIndex(IndexConfig(dim=64, nlist=32, m_pq=8, metric="l2",
+                                     build_flags=BUILD_FP16 | BUILD_FP8 | BUILD_IVF_PQ | BUILD_IVF_SQ8))
+    idx.build(x)
+    extra = gen_clustered(300, 64, 24, 12)
+    idx.add_vectors(extra)
+    idx.delete_ids([3, 5, 6000, 6001, 4242])
+    return idx, np.vstack([x, extra])
+
+
+def make_mix(n, rng, dim, engines):
+    from fvgb300.serve import BatchKey
+
+    keys, fids = [], []
+    for i in range(n):
+        eng = engines[rng.integers(len(engines))]
+        k = int(rng.choice([1, 10, 100]))
+        npb = int(rng.choice([4, 16])) if eng.startswith("ivf") else 0
+        rr = int(rng.choice([0, 64, 1])) if eng.startswith("ivf") else 0
+        keys.append(BatchKey(eng, k, npb, rr))
+        fids.append(int(rng.integers(-1, 2)))
+    q = gen_clustered(n, dim, 24, int(rng.integers(1 << 30)))
+    return keys, fids, q
+
+
+def alone(idx, key, q, filt):
+    from fvgb300.serve import ALGORITHM
+
+    eng = ALGORITHM[key.algorithm]
+    if eng == 0:
+        return idx.batch_search_flat(q[None], 1, key.top_k, filt)
+    if eng in (1, 2):
+        return (idx.batch_search_fp16_tc if eng == 1 else idx.batch_search_fp8)(q[None], 1, key.top_k, filt)
+    return idx.batch_search_ivf_mode(q[None], 1, key.top_k, key.ef_or_nprobe, key.rerank_k,
+                                     "pq" if eng == 3 else "sq8", filt)
+
+
+@pytest.mark.parametrize("group", [False, True])
+def test_identical_alone_and_in_the_mix(served, group):
+    from fvgb300.serve import SearchBatcher
+
+    idx, rows = served
+    rng = np.random.default_rng(5 + group)
+    n_ids = rows.shape[0]
+    filters = [rng.random(n_ids) < 0.2, (np.arange(n_ids) % 3) == 0]
+    engines = ["flat", "fp16", "fp8", "ivf_pq", "ivf_sq8"]
+    keys, fids, q = make_mix(160, rng, 64, engines)
+    with SearchBatcher.for_index(idx, max_wait_us=2000, max_batch_size=64, inflight=3,
+                                 group_by_params=group) as b:
+        fid_map = [b.add_filter(f) for f in filters]
+        sfids = [fid_map[f] if f >= 0 else -1 for f in fids]
+        # a burst: everything arrives at once, so the batches are mixed
+        ids, dist, status = b.replay(keys, q, np.zeros(len(keys), dtype=np.uint64), sfids)
+        s = b.serve_stats()
+    assert np.all(status == 0)
+    assert s["completed"] == len(keys) and s["avg_batch_size"] > 1.0
+    for i, key in enumerate(keys):
+        filt = filters[fids[i]] if fids[i] >= 0 else None
+        a_ids, a_dist = alone(idx, key, q[i], filt)
+        k = key.top_k
+        assert np.array_equal(ids[i, :k], a_ids[0]), (i, key)
+        assert np.array_equal(dist[i, :k], a_dist[0]), (i, key)
+        if filt is not None:
+            valid = ids[i, :k][ids[i, :k] != 0xFFFFFFFF]
+            assert np.all(filt[valid])
+        assert not np.isin(ids[i, :k], [3, 5, 6000, 6001, 4242]).any()
+
+
+def test_poisson_arrivals_report_latency(served):
+    from fvgb300.serve import BatchKey, SearchBatcher
+
+    idx, rows = served
+    rng = np.random.default_rng(9)
+    n = 400
+    gaps = rng.exponential(1e9 / 20000.0, n)  # 20k requests/s
+    arrivals = np.cumsum(gaps).astype(np.uint64)
+    keys = [BatchKey("ivf_sq8", 10, 16, 64) if i % 2 else BatchKey("fp16", 10) for i in range(n)]
+    q = gen_clustered(n, 64, 24, 77)
+    with SearchBatcher.for_index(idx, max_wait_us=200, max_batch_size=128, inflight=4) as b:
+        ids, _, status = b.replay(keys, q, arrivals)
+        s = b.serve_stats()
+    assert np.all(status == 0) and np.all(ids[:, 0] != 0xFFFFFFFF)
+    assert s["completed"] == n and s["qps"] > 0 and s["p99_us"] >= s["p50_us"] > 0
+
+
+def test_serving_survives_index_updates(served):
+    """Writers wait for the batches in flight; requests after an update see it."""
+    from fvgb300.serve import BatchKey, SearchBatcher
+
+    idx, rows = served
+    marker = np.full((1, 64), 40.0, dtype=np.float32)
+    with SearchBatcher.for_index(idx, max_wait_us=0, inflight=2) as b:
+        key = BatchKey("flat", 5)
+        before = b.search(key, marker[0])[0]
+        new_id = int(idx.add_vectors(marker)[0])
+        after = b.search(key, marker[0])[0]
+        assert after[0] == new_id and before[0] != new_id
+        idx.delete_ids([new_id])
+        assert b.search(key, marker[0])[0][0] != new_id
