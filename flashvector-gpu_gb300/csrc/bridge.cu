@@ -21,6 +21,42 @@
 
 namespace fv {
 
+// ------------------------------------------------------------- tuning
+namespace {
+struct Knob {
+  const char* key;
+  std::atomic<int64_t> value;
+};
+Knob g_knobs[] = {{"tc.prepass", {-1}}, {"tc.prepass_stride", {32}}, {"tc.prepass_margin", {3}}};
+}  // namespace
+
+bool tune_set(const char* key, int64_t value) {
+  for (auto& k : g_knobs)
+    if (std::strcmp(k.key, key) == 0) {
+      k.value.store(value, std::memory_order_relaxed);
+      return true;
+    }
+  return false;
+}
+
+bool tune_get(const char* key, int64_t* value) {
+  for (auto& k : g_knobs)
+    if (std::strcmp(k.key, key) == 0) {
+      *value = k.value.load(std::memory_order_relaxed);
+      return true;
+    }
+  return false;
+}
+
+int64_t tune_value(const char* key, int64_t dflt) {
+  int64_t v = dflt;
+  return tune_get(key, &v) ? v : dflt;
+}
+
+}  // namespace fv
+
+namespace fv {
+
 namespace {
 std::atomic<uint64_t> g_launches{0};
 
@@ -445,6 +481,16 @@ int cuda_bitonic_sort_test(const float* d_keys_in, const uint32_t* d_vals_in, fl
 
 // ----------------------------------------------------------- extensions
 const char* fv_version(void) { return "fvgb300 0.1 sm_103a"; }
+
+int fv_tune_set(const char* key, int64_t value) {
+  if (!key) return FV_ERR_NULL;
+  return fv::tune_set(key, value) ? 0 : FV_ERR_ARG;
+}
+
+int fv_tune_get(const char* key, int64_t* value) {
+  if (!key || !value) return FV_ERR_NULL;
+  return fv::tune_get(key, value) ? 0 : FV_ERR_ARG;
+}
 
 int fv_read_device_status(uint32_t* status) {
   if (!status) return FV_ERR_NULL;

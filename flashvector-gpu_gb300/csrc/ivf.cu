@@ -40,7 +40,8 @@ namespace fv {
 namespace {
 
 constexpr int IVF_THREADS = 256;
-constexpr uint32_t IVF_BUF = 1024;         // candidate buffer entries
+constexpr int IVF_ROWS = 4;                // postings per thread per round (loads issued together)
+constexpr uint32_t IVF_BUF = 2 * IVF_THREADS * IVF_ROWS;  // candidate buffer entries
 constexpr uint32_t MAX_SHORTLIST = 10240;  // reference clamp (ivf_rerank.cuh:12)
 
 enum IvfMode { IVF_PQ = 0, IVF_SQ8 = 1 };
@@ -84,10 +85,12 @@ __host__ __device__ __forceinline__ uint32_t ivf_clamps(uint32_t& top_k, uint32_
 
 struct IvfSmem {
   // [keys_pow2] u64 keys | LUT (PQ: m*256 f32) or residual+mins+scales (SQ8: 3*dim f32) | query (dim f32)
+  // | PQ: query residual to the probed centroid (dim f32)
   static size_t bytes(int mode, uint32_t keys_pow2, uint32_t dim, uint32_t m_pq) {
     size_t b = (size_t)keys_pow2 * 8;
     b += mode == IVF_PQ ? (size_t)m_pq * 256 * 4 : (size_t)3 * dim * 4;
     b += (size_t)dim * 4;
+    if (mode == IVF_PQ) b += (size_t)dim * 4;
     return b + 64;
   }
 };
@@ -108,6 +111,23 @@ __device__ __forceinline__ float adc_row(const float* __restrict__ lut, const ui
     }
   } else {
     for (uint32_t m = 0; m < m_pq; ++m) s = __fadd_rn(s, lut[m * 256 + __ldg(row + m)]);
+  }
+  return s;
+}
+
+// PQ: ADC of a code row already in registers (MW 16-byte words, m_pq = 16 MW),
+// sub-spaces added in order as adc_row does.
+template <int MW>
+__device__ __forceinline__ float adc_words(const float* __restrict__ lut, const uint4 (&w)[MW]) {
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < MW; ++j) {
+    const uint32_t ws[4] = {w[j].x, w[j].y, w[j].z, w[j].w};
+#pragma unroll
+    for (int b = 0; b < 16; ++b) {
+      const uint32_t c = (ws[b >> 2] >> ((b & 3) * 8)) & 0xFFu;
+      s = __fadd_rn(s, lut[(j * 16 + b) * 256 + c]);
+    }
   }
   return s;
 }
@@ -139,7 +159,9 @@ __device__ __forceinline__ float sq8_row(const float* __restrict__ qres, const f
   return s;
 }
 
-template <int MODE>
+// MODE: PQ or SQ8. MW > 0: PQ codes of 16 * MW bytes at 16-byte-aligned
+// rows (m_pq = 16, 32, 64), scanned by the register-prefetching loop.
+template <int MODE, int MW>
 __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   uint64_t* keys = reinterpret_cast<uint64_t*>(smem);
@@ -152,6 +174,8 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
   const bool vec16 = (a.code_bytes % 16u) == 0 && ((uintptr_t)a.codes % 16u) == 0;
   float* mins = tab + a.dim;      // SQ8 only
   float* scales = tab + 2 * a.dim;
+  float* qres = qs + a.dim;       // PQ only: q - centroid of the probed list
+  const bool cb4 = a.sub_dim == 4 && ((uintptr_t)a.codebooks % 16u) == 0;
 
   if (MODE == IVF_SQ8) {
     for (uint32_t d = tid; d < a.dim; d += IVF_THREADS) {
@@ -186,10 +210,12 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
 
     auto flush = [&]() {
       // keys[0, S) sorted shortlist, keys[S, S + cnt) new candidates
-      const uint32_t cnt = s_cnt;
-      for (uint32_t i = S + cnt + tid; i < a.keys_pow2; i += IVF_THREADS) keys[i] = kSentinelKey;
+      const uint32_t cnt = s_cnt;  // block-uniform (read after a barrier)
+      if (cnt == 0) return;
+      const uint32_t p2 = next_pow2_dev(S + cnt);  // sort only the occupied prefix
+      for (uint32_t i = S + cnt + tid; i < p2; i += IVF_THREADS) keys[i] = kSentinelKey;
       __syncthreads();
-      block_bitonic_sort(keys, a.keys_pow2);
+      block_bitonic_sort(keys, p2);
       if (tid == 0) {
         s_cnt = 0;
         s_tau = keys[S - 1];
@@ -202,17 +228,32 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
       if (l >= a.nlist) continue;  // uniform over the block
       const float* cent = a.centroids + (size_t)l * a.dim;
       if (MODE == IVF_PQ) {
+        // LUT[m][c] = sum_sd ((q - centroid) - codeword)^2 with fmaf in
+        // sub-dimension order; q - centroid is rounded once per dimension, as
+        // the reference's expression rounds it (ivf_pq_lookup.cu:150-162)
+        for (uint32_t d = tid; d < a.dim; d += IVF_THREADS) qres[d] = qs[d] - __ldg(cent + d);
+        __syncthreads();
         const uint32_t entries = a.m_pq * 256;
-        for (uint32_t e = tid; e < entries; e += IVF_THREADS) {
-          const uint32_t m = e >> 8, c = e & 255u;
-          const float* cb = a.codebooks + ((size_t)m * 256 + c) * a.sub_dim;
-          float s = 0.f;
-          for (uint32_t sd = 0; sd < a.sub_dim; ++sd) {
-            const uint32_t d = m * a.sub_dim + sd;
-            const float t = (qs[d] - __ldg(cent + d)) - __ldg(cb + sd);
-            s = fmaf(t, t, s);
+        if (cb4) {
+          const float4* cbv = reinterpret_cast<const float4*>(a.codebooks);
+#pragma unroll 4
+          for (uint32_t e = tid; e < entries; e += IVF_THREADS) {
+            const float4 w = __ldg(cbv + e);  // codeword (m, c) = row e of 4 floats
+            const float* r = qres + (e >> 8) * 4;
+            const float t0 = r[0] - w.x, t1 = r[1] - w.y, t2 = r[2] - w.z, t3 = r[3] - w.w;
+            tab[e] = fmaf(t3, t3, fmaf(t2, t2, fmaf(t1, t1, fmaf(t0, t0, 0.f))));
           }
-          tab[e] = s;
+        } else {
+          for (uint32_t e = tid; e < entries; e += IVF_THREADS) {
+            const uint32_t m = e >> 8, c = e & 255u;
+            const float* cb = a.codebooks + ((size_t)m * 256 + c) * a.sub_dim;
+            float s = 0.f;
+            for (uint32_t sd = 0; sd < a.sub_dim; ++sd) {
+              const float t = qres[m * a.sub_dim + sd] - __ldg(cb + sd);
+              s = fmaf(t, t, s);
+            }
+            tab[e] = s;
+          }
         }
       } else {
         for (uint32_t d = tid; d < a.dim; d += IVF_THREADS) tab[d] = qs[d] - __ldg(cent + d);
@@ -220,25 +261,57 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
       __syncthreads();
 
       const uint32_t beg = __ldg(a.offsets + l), end = __ldg(a.offsets + l + 1);
-      for (uint32_t base = beg; base < end; base += IVF_THREADS) {
-        const uint32_t i = base + tid;
-        if (i < end) {
-          const uint32_t vid = __ldg(a.vec_ids + i);
-          if (mask_allows(a.mask, vid) && filter_allows(qf, vid)) {
-            const uint8_t* row = a.codes + (size_t)(a.list_major ? i : vid) * a.code_bytes;
-            const float d = MODE == IVF_PQ ? adc_row(tab, row, a.m_pq, vec16)
-                                           : sq8_row(tab, mins, scales, row, a.dim, vec16);
-            if (d < kSentinelDist) {
-              const uint64_t key = make_key(d, vid);
-              if (key < s_tau) {
-                const uint32_t pos = atomicAdd(&s_cnt, 1u);
-                keys[S + pos] = key;
-              }
-            }
+      auto offer = [&](float d, uint32_t vid) {
+        if (d < kSentinelDist) {
+          const uint64_t key = make_key(d, vid);
+          if (key < s_tau) {
+            const uint32_t pos = atomicAdd(&s_cnt, 1u);
+            keys[S + pos] = key;
           }
         }
-        __syncthreads();
-        if (s_cnt > IVF_BUF - IVF_THREADS) flush();
+      };
+      if (MODE == IVF_PQ && MW > 0) {
+        // IVF_ROWS postings per thread per round: ids and code rows of all of
+        // them are loaded before any is scored, so a warp keeps several
+        // 16-byte loads in flight per lane
+        for (uint32_t base = beg; base < end; base += IVF_THREADS * IVF_ROWS) {
+          uint32_t vid[IVF_ROWS];
+          uint4 w[IVF_ROWS][MW > 0 ? MW : 1];
+#pragma unroll
+          for (int r = 0; r < IVF_ROWS; ++r) {
+            const uint32_t i = base + r * IVF_THREADS + tid;
+            vid[r] = i < end ? __ldg(a.vec_ids + i) : 0xFFFFFFFFu;
+          }
+#pragma unroll
+          for (int r = 0; r < IVF_ROWS; ++r) {
+            const uint32_t i = base + r * IVF_THREADS + tid;
+            const uint4* row = reinterpret_cast<const uint4*>(a.codes + (size_t)(a.list_major ? i : vid[r]) * (16u * MW));
+#pragma unroll
+            for (int j = 0; j < (MW > 0 ? MW : 1); ++j)
+              w[r][j] = i < end ? __ldg(row + j) : make_uint4(0u, 0u, 0u, 0u);
+          }
+#pragma unroll
+          for (int r = 0; r < IVF_ROWS; ++r) {
+            if (vid[r] != 0xFFFFFFFFu && mask_allows(a.mask, vid[r]) && filter_allows(qf, vid[r]))
+              offer(adc_words<(MW > 0 ? MW : 1)>(tab, w[r]), vid[r]);
+          }
+          __syncthreads();
+          if (s_cnt > IVF_BUF - IVF_THREADS * IVF_ROWS) flush();
+        }
+      } else {
+        for (uint32_t base = beg; base < end; base += IVF_THREADS) {
+          const uint32_t i = base + tid;
+          if (i < end) {
+            const uint32_t vid = __ldg(a.vec_ids + i);
+            if (mask_allows(a.mask, vid) && filter_allows(qf, vid)) {
+              const uint8_t* row = a.codes + (size_t)(a.list_major ? i : vid) * a.code_bytes;
+              offer(MODE == IVF_PQ ? adc_row(tab, row, a.m_pq, vec16) : sq8_row(tab, mins, scales, row, a.dim, vec16),
+                    vid);
+            }
+          }
+          __syncthreads();
+          if (s_cnt > IVF_BUF - IVF_THREADS) flush();
+        }
       }
       __syncthreads();  // the table is rebuilt for the next list
     }
@@ -338,7 +411,14 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
 
   const size_t smem = IvfSmem::bytes(mode, a.keys_pow2, L.dim, L.m_pq);
   if (smem > 227 * 1024) return FV_ERR_ARG;
-  auto kern = mode == IVF_PQ ? ivf_scan_kernel<IVF_PQ> : ivf_scan_kernel<IVF_SQ8>;
+  const bool rows16 = mode == IVF_PQ && ((uintptr_t)L.codes % 16u) == 0;
+  auto kern = ivf_scan_kernel<IVF_SQ8, 0>;
+  if (mode == IVF_PQ) {
+    kern = ivf_scan_kernel<IVF_PQ, 0>;
+    if (rows16 && L.m_pq == 16) kern = ivf_scan_kernel<IVF_PQ, 1>;
+    if (rows16 && L.m_pq == 32) kern = ivf_scan_kernel<IVF_PQ, 2>;
+    if (rows16 && L.m_pq == 64) kern = ivf_scan_kernel<IVF_PQ, 4>;
+  }
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
   int per_sm = 0;

@@ -35,6 +35,11 @@ struct QueryFilter {
   uint32_t reserved;
 };
 
+// Process-wide tuning knobs (fv_tune_set / fv_tune_get).
+bool tune_set(const char* key, int64_t value);
+bool tune_get(const char* key, int64_t* value);
+int64_t tune_value(const char* key, int64_t dflt);
+
 // Streaming-multiprocessor count of the current device (cached per device).
 int device_sm_count();
 
@@ -104,9 +109,9 @@ struct TcTables {
   uint32_t n, dim, padded_dim;
 };
 struct TcScanArgs;
-cudaError_t dispatch_tc_scan_fp16(int kl, int metric, const CUtensorMap& ta, const CUtensorMap& tb,
+cudaError_t dispatch_tc_scan_fp16(int kl, int groups, int metric, const CUtensorMap& ta, const CUtensorMap& tb,
                                   const TcScanArgs& a, uint32_t grid, cudaStream_t stream);
-cudaError_t dispatch_tc_scan_fp8(int kl, int metric, const CUtensorMap& ta, const CUtensorMap& tb,
+cudaError_t dispatch_tc_scan_fp8(int kl, int groups, int metric, const CUtensorMap& ta, const CUtensorMap& tb,
                                  const TcScanArgs& a, uint32_t grid, cudaStream_t stream);
 int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
                    const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream,

@@ -109,6 +109,9 @@ struct SelectArgs {
   float eps;
   GpuSearchResult* out;
   uint32_t* status;
+  const float* tau;          // per-query admission bound of the scan (null: none)
+  uint32_t* redo;            // set for a bounded query whose shortlist came up short
+  const uint32_t* only;      // process only the flagged queries (null: all)
 };
 
 constexpr int SEL_THREADS = 256;
@@ -123,6 +126,7 @@ __global__ void __launch_bounds__(SEL_THREADS) tc_select_kernel(SelectArgs s) {
   __shared__ int band_lo, band_hi;
   __shared__ int incomplete;
   const uint32_t q = blockIdx.x;
+  if (s.only && s.only[q] == 0u) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t total = s.lists * s.kl;
   const uint64_t* src = s.partial + (size_t)q * total;
@@ -142,6 +146,9 @@ __global__ void __launch_bounds__(SEL_THREADS) tc_select_kernel(SelectArgs s) {
   }
   __syncthreads();
   if (incomplete && threadIdx.x == 0) set_status(s.status, kStatusOverflow);
+  // a bounded scan admitted fewer than kp rows: the bound from the sample was
+  // below the query's kp-th distance, so the query is scanned again unbounded
+  if (s.redo && threadIdx.x == 0 && keys[kp - 1] == kSentinelKey && s.tau[q] < kSentinelDist) s.redo[q] = 1u;
 
   const float* qv = s.queries + (size_t)q * s.dim;
   if (s.vectors) {
@@ -203,6 +210,20 @@ __global__ void __launch_bounds__(SEL_THREADS) tc_select_kernel(SelectArgs s) {
     s.out[(size_t)q * s.k + r] = key_to_result(r < kp ? keys[r] : kSentinelKey, nullptr);
 }
 
+// Pre-pass result: per query, the distance of the r-th best key among the
+// sample's per-range heaps -- the query's admission bound for the full scan
+// (1e30, i.e. no bound, when the sample holds fewer than r admissible rows).
+__global__ void __launch_bounds__(128) tc_tau_kernel(const uint64_t* __restrict__ partial, uint32_t total,
+                                                     uint32_t pow2, uint32_t r, float* __restrict__ tau) {
+  extern __shared__ uint64_t keys[];
+  const uint32_t q = blockIdx.x;
+  const uint64_t* src = partial + (size_t)q * total;
+  for (uint32_t i = threadIdx.x; i < pow2; i += blockDim.x) keys[i] = i < total ? src[i] : kSentinelKey;
+  __syncthreads();
+  block_bitonic_sort(keys, pow2);
+  if (threadIdx.x == 0) tau[q] = (r <= total && keys[r - 1] != kSentinelKey) ? key_dist(keys[r - 1]) : kSentinelDist;
+}
+
 // cuTensorMapEncodeTiled resolved through the runtime, so the library does
 // not link libcuda (it must load on hosts without a driver).
 PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
@@ -245,37 +266,70 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   const uint32_t kblocks = (t.padded_dim + kb_elems - 1) / kb_elems;
   const uint32_t overfetch = opt.overfetch ? opt.overfetch : 4;
   const uint32_t shortlist = t.vectors ? std::min<uint32_t>(std::max(k, overfetch * k), 4096u) : k;
-  const uint32_t kl = std::min<uint32_t>(64u, shortlist);            // heap entries per (query, range)
-  const uint32_t kl_tmpl = std::min<uint32_t>(64u, (kl + 15) / 16 * 16);  // heap capacity (template)
+  // short K (at most two 64-element fp16 / 128-element fp8 blocks per tile):
+  // a tile costs the MMA little and the epilogue much, so two epilogue
+  // groups drain the two accumulator buffers in parallel
+  const int groups = kblocks <= 2 ? 2 : 1;
+  const uint32_t kl_cap = groups == 2 ? 48u : 64u;
+  const uint32_t kl = std::min<uint32_t>(kl_cap, shortlist);         // heap entries per (query, range, group)
+  const uint32_t kl_tmpl = std::min<uint32_t>(kl_cap, (kl + 15) / 16 * 16);  // heap capacity (template)
   const uint32_t nqb = (nq + TC_M - 1) / TC_M;
   const uint32_t ntiles = (t.n + TC_N - 1) / TC_N;
   const int sms = device_sm_count();
   uint32_t splits = opt.splits ? opt.splits : std::max<uint32_t>(1u, (uint32_t)sms / nqb);
   if (!opt.splits && shortlist > kl) {
-    // a (query, range) heap keeps kl keys: split the base so that each range
-    // holds, in expectation, a third of that share of the shortlist (a range
-    // that still overflows is reported through the status word)
-    splits = std::max<uint32_t>(splits, (3 * shortlist + kl - 1) / kl);
+    // a (query, range, group) heap keeps kl keys: split the base so that each
+    // heap holds, in expectation, a third of its share of the shortlist (a
+    // heap that still overflows is reported through the status word)
+    splits = std::max<uint32_t>(splits, (3 * shortlist + kl * groups - 1) / (kl * groups));
   }
   splits = std::max(1u, std::min(splits, ntiles));
   // the select kernel sorts lists*kl keys in shared memory: <= 16384
-  while (splits > 1 && next_pow2(splits * kl) > 16384u) --splits;
+  while (splits > 1 && next_pow2(splits * groups * kl) > 16384u) --splits;
   uint32_t tps = (ntiles + splits - 1) / splits;
   splits = (ntiles + tps - 1) / tps;
 
-  // scratch: prepared queries | ||q||^2 | q scales | partial heaps
+  // Sampled pre-pass (large shortlists only): the CTAs of a query cannot
+  // share a bound when the shortlist exceeds the per-range heap, so each
+  // range would insert ~kl (1 + ln(rows / kl)) keys per query. A scan of
+  // every stride-th tile gives each query its r-th best sampled distance,
+  // r = ceil(margin * shortlist / stride), an upper bound on its shortlist-th
+  // distance unless the sample is unlucky; the full scan then admits only
+  // rows within it. Queries whose bounded scan comes up short are scanned
+  // again without the bound (device-side, no host round trip).
+  const int64_t pp_knob = tune_value("tc.prepass", -1);
+  const uint32_t pstride = (uint32_t)std::max<int64_t>(2, tune_value("tc.prepass_stride", 32));
+  const uint32_t pmargin = (uint32_t)std::max<int64_t>(1, tune_value("tc.prepass_margin", 3));
+  const uint32_t pr = std::min<uint32_t>(kl_cap, (pmargin * shortlist + pstride - 1) / pstride);
+  const uint32_t psampled = (ntiles + pstride - 1) / pstride;
+  const bool prepass = pp_knob != 0 && shortlist > kl && (pp_knob == 1 || psampled >= 64u) && psampled > 0;
+  const uint32_t pkl_tmpl = std::min<uint32_t>(kl_cap, (pr + 15) / 16 * 16);
+  uint32_t psplits = std::max<uint32_t>(1u, std::min<uint32_t>((uint32_t)sms / nqb, psampled));
+  while (psplits > 1 && next_pow2(psplits * groups * pr) > 16384u) --psplits;
+  const uint32_t ptps = (psampled + psplits - 1) / psplits;
+  psplits = (psampled + ptps - 1) / ptps;
+
+  // scratch: prepared queries | ||q||^2 | q scales | partial heaps | slots
+  //          [| pre-pass heaps | tau | redo flags]
   const size_t q_bytes = align_up((size_t)nq * t.padded_dim * elem, 1024);
   const size_t qn_bytes = align_up((size_t)nq * 4, 256);
-  const size_t part_bytes = align_up((size_t)nq * splits * kl * 8, 256);
+  const size_t part_bytes = align_up((size_t)nq * splits * groups * kl * 8, 256);
   const uint32_t slot_stride = (kl + 3) / 4 * 4;
   const size_t slot_bytes = align_up((size_t)nq * slot_stride * 4, 256);
-  uint8_t* scratch = static_cast<uint8_t*>(scratch_get(stream, q_bytes + 2 * qn_bytes + part_bytes + slot_bytes));
+  const size_t ppart_bytes = prepass ? align_up((size_t)nq * psplits * groups * pr * 8, 256) : 0;
+  const size_t tau_bytes = prepass ? 2 * qn_bytes : 0;
+  uint8_t* scratch = static_cast<uint8_t*>(
+      scratch_get(stream, q_bytes + 2 * qn_bytes + part_bytes + slot_bytes + ppart_bytes + tau_bytes));
   if (!scratch) return (int)cudaErrorMemoryAllocation;
   void* qprep = scratch;
   float* qnorm = reinterpret_cast<float*>(scratch + q_bytes);
   float* qscale = reinterpret_cast<float*>(scratch + q_bytes + qn_bytes);
   uint64_t* partial = reinterpret_cast<uint64_t*>(scratch + q_bytes + 2 * qn_bytes);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(scratch + q_bytes + 2 * qn_bytes + part_bytes);
+  uint8_t* extra = scratch + q_bytes + 2 * qn_bytes + part_bytes + slot_bytes;
+  uint64_t* ppartial = prepass ? reinterpret_cast<uint64_t*>(extra) : nullptr;
+  float* tau = prepass ? reinterpret_cast<float*>(extra + ppart_bytes) : nullptr;
+  uint32_t* redo = prepass ? reinterpret_cast<uint32_t*>(extra + ppart_bytes + qn_bytes) : nullptr;
 
   {
     ProfScope ps(fp8 ? "tc_prep_queries_fp8" : "tc_prep_queries_fp16", stream);
@@ -299,30 +353,55 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   a.nq = nq;
   a.kblocks = kblocks;
   a.nqb = nqb;
-  a.splits = splits;
-  a.tiles_per_split = tps;
   a.xnorm = t.norms;
   a.xscale = t.scales;
   a.qnorm = qnorm;
   a.qscale = qscale;
   a.mask = mask;
-  a.partial = partial;
   a.tslot = tslot;
   a.tslot_stride = slot_stride;
-  a.kl = kl;
-  a.share = kl == shortlist ? 1u : 0u;
   a.status = status_word();
   a.filters = filters;
+  a.tile_stride = 1;
+  auto scan = [&](const TcScanArgs& args, int kl_t, uint32_t grid, const char* name) -> cudaError_t {
+    ProfScope ps(name, stream);
+    return fp8 ? dispatch_tc_scan_fp8(kl_t, groups, (int)metric, ta, tb, args, grid, stream)
+               : dispatch_tc_scan_fp16(kl_t, groups, (int)metric, ta, tb, args, grid, stream);
+  };
   cudaError_t e;
-  {
-    ProfScope ps(fp8 ? "tc_scan_fp8" : "tc_scan_fp16", stream);
-    e = fp8 ? dispatch_tc_scan_fp8((int)kl_tmpl, (int)metric, ta, tb, a, nqb * splits, stream)
-            : dispatch_tc_scan_fp16((int)kl_tmpl, (int)metric, ta, tb, a, nqb * splits, stream);
+  if (prepass) {
+    TcScanArgs p = a;
+    p.splits = psplits;
+    p.tiles_per_split = ptps;
+    p.partial = ppartial;
+    p.kl = pr;
+    p.share = 0;
+    p.tile_stride = pstride;
+    e = scan(p, (int)pkl_tmpl, nqb * psplits, fp8 ? "tc_prepass_fp8" : "tc_prepass_fp16");
+    if (e != cudaSuccess) return (int)e;
+    const uint32_t total = psplits * groups * pr, pow2 = next_pow2(total);
+    e = cudaFuncSetAttribute(tc_tau_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(pow2 * 8));
+    if (e != cudaSuccess) return (int)e;
+    {
+      ProfScope ps("tc_tau", stream);
+      tc_tau_kernel<<<nq, 128, pow2 * 8, stream>>>(ppartial, total, pow2, pr, tau);
+      note_launch();
+    }
+    e = cudaMemsetAsync(redo, 0, (size_t)nq * 4, stream);
+    if (e != cudaSuccess) return (int)e;
   }
+  a.splits = splits;
+  a.tiles_per_split = tps;
+  a.partial = partial;
+  a.kl = kl;
+  a.share = kl == shortlist ? 1u : 0u;
+  a.qbound = tau;
+  e = scan(a, (int)kl_tmpl, nqb * splits, fp8 ? "tc_scan_fp8" : "tc_scan_fp16");
   if (e != cudaSuccess) return (int)e;
 
-  SelectArgs s{partial, splits, kl, next_pow2(splits * kl), shortlist, k, queries, t.vectors, t.dim, (int)metric,
-               opt.boundary_fp64 ? 1u : 0u, 0.f, out, status_word()};
+  SelectArgs s{partial, splits * groups, kl, next_pow2(splits * groups * kl), shortlist, k, queries, t.vectors, t.dim,
+               (int)metric,
+               opt.boundary_fp64 ? 1u : 0u, 0.f, out, status_word(), tau, redo, nullptr};
   s.eps = opt.boundary_eps > 0.f ? opt.boundary_eps : (float)((t.dim + 31) / 32 + 5) * 2.0f * 5.960464477539063e-08f;
   const size_t sel_smem = (size_t)std::max(s.pow2, next_pow2(shortlist)) * 8;
   e = cudaFuncSetAttribute(tc_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sel_smem);
@@ -330,6 +409,23 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   {
     ProfScope ps("tc_select_rescore", stream);
     tc_select_kernel<<<nq, SEL_THREADS, sel_smem, stream>>>(s);
+    note_launch();
+  }
+  if (prepass) {
+    // queries whose bound was too tight: scanned again without it (blocks
+    // holding none of them exit at once), then selected again
+    TcScanArgs f = a;
+    f.qbound = nullptr;
+    f.active = redo;
+    f.share = 0;
+    e = scan(f, (int)kl_tmpl, nqb * splits, fp8 ? "tc_rescan_fp8" : "tc_rescan_fp16");
+    if (e != cudaSuccess) return (int)e;
+    SelectArgs r = s;
+    r.tau = nullptr;
+    r.redo = nullptr;
+    r.only = redo;
+    ProfScope ps("tc_select_rescore", stream);
+    tc_select_kernel<<<nq, SEL_THREADS, sel_smem, stream>>>(r);
     note_launch();
   }
   return (int)cudaGetLastError();

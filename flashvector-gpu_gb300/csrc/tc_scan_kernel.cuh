@@ -37,7 +37,9 @@ constexpr int TC_N = 256;                  // base rows per tile (MMA N)
 constexpr int KB_BYTES = 128;              // K bytes per stage row (one 128B swizzle atom)
 constexpr int A_STAGE = TC_M * KB_BYTES;   // 16 KB
 constexpr int B_STAGE = TC_N * KB_BYTES;   // 32 KB
-constexpr int SCAN_THREADS = 192;
+// threads of a scan CTA with G epilogue groups: warp 0 TMA, warp 1 MMA,
+// 4 epilogue warps per group
+__host__ __device__ constexpr int scan_threads(int G) { return 64 + 128 * G; }
 
 struct TcScanArgs {
   uint32_t n, nq, kblocks, nqb, splits, tiles_per_split;
@@ -53,16 +55,19 @@ struct TcScanArgs {
   uint32_t share;        // 1: the CTAs of a query share the slot bound (kl == shortlist)
   uint32_t* status;
   const QueryFilter* filters;  // per-query filters over slots (== logical ids), or null
+  const float* qbound;         // per-query admission bound (distance), or null
+  const uint32_t* active;      // per-query flags: only flagged queries are scanned (null: all)
+  uint32_t tile_stride;        // scan every tile_stride-th 256-row tile (a sample when > 1)
 };
 
-template <int KL, int STAGES>
+template <int KL, int STAGES, int G>
 struct ScanSmem {
   static constexpr size_t a_off = 0;
   static constexpr size_t b_off = a_off + (size_t)STAGES * A_STAGE;
   static constexpr size_t heap_off = b_off + (size_t)STAGES * B_STAGE;
-  static constexpr size_t col_off = heap_off + (size_t)KL * TC_M * 8;   // [4 warps][2][TC_N] floats
-  static constexpr size_t cmask_off = col_off + 4 * 2 * TC_N * 4;       // [4 warps][8] words
-  static constexpr size_t bar_off = cmask_off + 4 * 8 * 4;              // barriers
+  static constexpr size_t col_off = heap_off + (size_t)G * KL * TC_M * 8;  // [4G warps][2][TC_N] floats
+  static constexpr size_t cmask_off = col_off + 4 * G * 2 * TC_N * 4;      // [4G warps][8] words
+  static constexpr size_t bar_off = cmask_off + 4 * G * 8 * 4;          // barriers
   static constexpr size_t nbars = 2 * STAGES + 5;
   static constexpr size_t misc_off = bar_off + nbars * 8;
   static constexpr size_t bytes = misc_off + 16 + 1024;                 // + alignment slack
@@ -101,10 +106,14 @@ static __device__ __forceinline__ float select32(const float* v, int j) {
   return (j & 16) ? t[1] : t[0];
 }
 
-template <bool FP8, int KL, int STAGES, int METRIC>
-__global__ void __launch_bounds__(SCAN_THREADS, 1)
+// G epilogue groups: with G = 2 each group owns one of the two TMEM
+// accumulator buffers (tiles alternate between the groups) and keeps its
+// own heaps, which are dumped as separate lists (partial row split * G + g).
+template <bool FP8, int KL, int STAGES, int METRIC, int G>
+__global__ void __launch_bounds__(scan_threads(G), 1)
     tc_scan_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcScanArgs a) {
-  using L = ScanSmem<KL, STAGES>;
+  using L = ScanSmem<KL, STAGES, G>;
+  constexpr int SCAN_THREADS = scan_threads(G);
   extern __shared__ uint8_t smem_raw[];
   uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   uint8_t* sA = sm + L::a_off;
@@ -123,7 +132,17 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t qb = blockIdx.x % a.nqb, split = blockIdx.x / a.nqb;
-  const uint32_t ntiles = (a.n + TC_N - 1) / TC_N;
+  if (a.active) {
+    // a re-scan of flagged queries: a block holding none of them leaves at once
+    int any = 0;
+    for (int r = threadIdx.x; r < TC_M; r += SCAN_THREADS) {
+      const uint32_t q = qb * TC_M + r;
+      any |= (q < a.nq && a.active[q]) ? 1 : 0;
+    }
+    if (!__syncthreads_or(any)) return;
+  }
+  const uint32_t tstride = a.tile_stride ? a.tile_stride : 1u;
+  const uint32_t ntiles = ((a.n + TC_N - 1) / TC_N + tstride - 1) / tstride;
   const uint32_t t_begin = split * a.tiles_per_split;
   const uint32_t t_end = min(t_begin + a.tiles_per_split, ntiles);
   const uint32_t my_tiles = t_end > t_begin ? t_end - t_begin : 0;
@@ -135,7 +154,7 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
     }
     for (int b = 0; b < 2; ++b) {
       tc::mbar_init(&acc_full[b], 1);
-      tc::mbar_init(&acc_empty[b], 4);
+      tc::mbar_init(&acc_empty[b], 4);  // the 4 epilogue warps that drain buffer b
     }
     tc::mbar_init(mma_done, 1);
     *abort_flag = 0;
@@ -163,7 +182,7 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
       for (int s = 0; s < STAGES; ++s) issued_parity[s] = -1;
       bool ok = true;
       for (uint32_t i = 0; ok && i < my_tiles; ++i) {
-        const int32_t row_b = (int32_t)((t_begin + i) * TC_N);
+        const int32_t row_b = (int32_t)((t_begin + i) * tstride * TC_N);
         for (uint32_t kb = 0; kb < a.kblocks; ++kb) {
           if (!tc::mbar_wait(&empty[stage], phase ^ 1, abort_flag, a.status)) {
             ok = false;
@@ -225,17 +244,19 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
   } else {
     // --------------------------------------------------------- epilogue
     const int quad = warp & 3;                    // TMEM lane quadrant of this warp
+    const int grp = (warp - 2) >> 2;              // epilogue group
     const int row = quad * 32 + lane;             // query row in the block
     const uint32_t q = qb * TC_M + row;
-    const bool qvalid = q < a.nq;
-    uint64_t* h = heap + row;
+    const bool qvalid = q < a.nq && (a.active == nullptr || a.active[q] != 0u);
+    uint64_t* h = heap + (size_t)grp * KL * TC_M + row;
     const int kl = (int)a.kl;
     for (int i = 0; i < kl; ++i) h[i * TC_M] = kSentinelKey;
     const float qn = qvalid ? __ldg(a.qnorm + q) : 0.f;
     const QueryFilter qf = (a.filters && qvalid) ? load_filter(a.filters, q) : QueryFilter{nullptr, 0u, 0u};
     const float qs = (FP8 && qvalid) ? __ldg(a.qscale + q) : 1.f;
     float worst = kSentinelDist;  // this CTA's kl-th best distance (1e30 until the heap is full)
-    float bound = kSentinelDist;  // shared bound: max over the query's slots
+    // admission bound: the query's pre-pass bound, lowered by the shared slots
+    float bound = (a.qbound && qvalid) ? __ldg(a.qbound + q) : kSentinelDist;
     uint32_t* slots = (a.share && qvalid) ? a.tslot + (size_t)q * a.tslot_stride : nullptr;
 
     auto keep = [&](float dist, uint32_t slot) {
@@ -250,9 +271,9 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
     // wait on one another
     float* cb = colbuf + (warp - 2) * 2 * TC_N;
     uint32_t* cm = colmask + (warp - 2) * 8;
-    for (uint32_t i = 0; i < my_tiles; ++i) {
+    for (uint32_t i = (uint32_t)grp; i < my_tiles; i += G) {
       const uint32_t buf = i & 1, use = i >> 1;
-      const uint32_t v0 = (t_begin + i) * TC_N;
+      const uint32_t v0 = (t_begin + i) * tstride * TC_N;
       __syncwarp();
       for (int c = lane; c < TC_N; c += 32) {
         const uint32_t slot = v0 + c;
@@ -342,7 +363,7 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
       if (lane == 0) tc::mbar_arrive(&acc_empty[buf]);
     }
     if (qvalid) {
-      uint64_t* dst = a.partial + ((size_t)q * a.splits + split) * kl;
+      uint64_t* dst = a.partial + (((size_t)q * a.splits + split) * G + grp) * kl;
       for (int i = 0; i < kl; ++i) dst[i] = h[i * TC_M];
     }
   }
@@ -360,36 +381,48 @@ __global__ void __launch_bounds__(SCAN_THREADS, 1)
 }
 
 
-template <bool FP8, int KL, int STAGES, int METRIC>
+template <bool FP8, int KL, int STAGES, int METRIC, int G>
 cudaError_t launch_scan_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a, uint32_t grid,
                                cudaStream_t stream) {
-  using L = ScanSmem<KL, STAGES>;
-  auto kern = tc_scan_kernel<FP8, KL, STAGES, METRIC>;
+  using L = ScanSmem<KL, STAGES, G>;
+  static_assert(L::bytes <= 227 * 1024, "scan shared memory above the 227 KB per-CTA limit");
+  auto kern = tc_scan_kernel<FP8, KL, STAGES, METRIC, G>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes);
   if (e != cudaSuccess) return e;
-  kern<<<grid, SCAN_THREADS, L::bytes, stream>>>(ta, tb, a);
+  kern<<<grid, scan_threads(G), L::bytes, stream>>>(ta, tb, a);
   note_launch();
   return cudaGetLastError();
 }
 
+// groups == 2 (short K: one or two K blocks per tile, where the epilogue
+// rather than the MMA bounds a tile) halves the stage ring and caps the heap
+// at 48 entries so that two groups' heaps fit next to it.
 template <bool FP8, int METRIC>
-cudaError_t dispatch_scan_kl(int kl, const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a, uint32_t grid,
-                             cudaStream_t stream) {
+cudaError_t dispatch_scan_kl(int kl, int groups, const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a,
+                             uint32_t grid, cudaStream_t stream) {
+  if (groups == 2) {
+    switch (kl) {
+      case 16: return launch_scan_kernel<FP8, 16, 3, METRIC, 2>(ta, tb, a, grid, stream);
+      case 32: return launch_scan_kernel<FP8, 32, 2, METRIC, 2>(ta, tb, a, grid, stream);
+      default: return launch_scan_kernel<FP8, 48, 2, METRIC, 2>(ta, tb, a, grid, stream);
+    }
+  }
   switch (kl) {
-    case 16: return launch_scan_kernel<FP8, 16, 4, METRIC>(ta, tb, a, grid, stream);
-    case 32: return launch_scan_kernel<FP8, 32, 3, METRIC>(ta, tb, a, grid, stream);
-    case 48: return launch_scan_kernel<FP8, 48, 3, METRIC>(ta, tb, a, grid, stream);
-    default: return launch_scan_kernel<FP8, 64, 3, METRIC>(ta, tb, a, grid, stream);
+    case 16: return launch_scan_kernel<FP8, 16, 4, METRIC, 1>(ta, tb, a, grid, stream);
+    case 32: return launch_scan_kernel<FP8, 32, 3, METRIC, 1>(ta, tb, a, grid, stream);
+    case 48: return launch_scan_kernel<FP8, 48, 3, METRIC, 1>(ta, tb, a, grid, stream);
+    default: return launch_scan_kernel<FP8, 64, 3, METRIC, 1>(ta, tb, a, grid, stream);
   }
 }
 
 template <bool FP8>
-cudaError_t dispatch_scan(int kl, int metric, const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a,
-                          uint32_t grid, cudaStream_t stream) {
+cudaError_t dispatch_scan(int kl, int groups, int metric, const CUtensorMap& ta, const CUtensorMap& tb,
+                          const TcScanArgs& a, uint32_t grid, cudaStream_t stream) {
   switch (metric) {
-    case METRIC_INNER_PRODUCT: return dispatch_scan_kl<FP8, METRIC_INNER_PRODUCT>(kl, ta, tb, a, grid, stream);
-    case METRIC_COSINE: return dispatch_scan_kl<FP8, METRIC_COSINE>(kl, ta, tb, a, grid, stream);
-    default: return dispatch_scan_kl<FP8, METRIC_L2>(kl, ta, tb, a, grid, stream);
+    case METRIC_INNER_PRODUCT:
+      return dispatch_scan_kl<FP8, METRIC_INNER_PRODUCT>(kl, groups, ta, tb, a, grid, stream);
+    case METRIC_COSINE: return dispatch_scan_kl<FP8, METRIC_COSINE>(kl, groups, ta, tb, a, grid, stream);
+    default: return dispatch_scan_kl<FP8, METRIC_L2>(kl, groups, ta, tb, a, grid, stream);
   }
 }
 

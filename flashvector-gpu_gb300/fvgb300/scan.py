@@ -157,6 +157,35 @@ def fp8_search(table, queries, k, metric="l2", mask=None, opts=None, out=None, s
     return out
 
 
+def tune_set(key: str, value: int) -> None:
+    """Process-wide tuning knob (fv_tune_set): tc.prepass, tc.prepass_stride, tc.prepass_margin."""
+    call("fv_tune_set", key.encode(), int(value))
+
+
+def tune_get(key: str) -> int:
+    v = C.c_int64(0)
+    call("fv_tune_get", key.encode(), C.byref(v))
+    return v.value
+
+
+class tuned:
+    """Context manager that sets knobs and restores them on exit."""
+
+    def __init__(self, **knobs):
+        self.knobs = {k.replace("_", ".", 1): v for k, v in knobs.items()}
+        self.saved = {}
+
+    def __enter__(self):
+        for k, v in self.knobs.items():
+            self.saved[k] = tune_get(k)
+            tune_set(k, v)
+        return self
+
+    def __exit__(self, *exc):
+        for k, v in self.saved.items():
+            tune_set(k, v)
+
+
 def profile_enable(on: bool = True) -> None:
     call("fv_profile_enable", 1 if on else 0)
 

@@ -262,6 +262,18 @@ uint64_t fv_launch_count(void);
  * (JSON, NUL-terminated) into buf and clears the record. */
 int fv_profile_enable(int on);
 int fv_profile_summary(char* buf, size_t len);
+/* Process-wide tuning knobs (no reference counterpart). Keys:
+ *   "tc.prepass"        -1 automatic (default), 0 off, 1 on where it applies:
+ *                       tensor-core scans whose shortlist exceeds the 64-entry
+ *                       per-range heap first scan a strided sample of the
+ *                       base for a per-query admission bound
+ *   "tc.prepass_stride" sample stride in 256-row tiles (default 32)
+ *   "tc.prepass_margin" sampled rank = ceil(margin * shortlist / stride)
+ *                       (default 3)
+ * Unknown keys return FV_ERR_ARG. Values apply to launches issued after the
+ * call. */
+int fv_tune_set(const char* key, int64_t value);
+int fv_tune_get(const char* key, int64_t* value);
 /* Installs a caller-owned device buffer as the scratch arena of `stream`
  * (kernels that need scratch then never allocate on that stream; a call
  * needing more than `bytes` fails with cudaErrorMemoryAllocation).

@@ -51,3 +51,17 @@ def test_struct_layouts_match_reference():
     assert ctypes.sizeof(_lib.Fp16GpuTables) == 3 * 8 + 3 * 4 + 4
     assert [f[0] for f in _lib.IvfPqGpuTables._fields_][:6] == [
         "d_centroids", "d_pq_codebooks", "d_pq_codes", "d_ivf_offsets", "d_ivf_vec_ids", "d_vectors"]
+
+
+def test_tune_knobs_roundtrip(built_lib):
+    """fv_tune_set / fv_tune_get (host only)."""
+    import pytest
+    from fvgb300 import scan
+    from fvgb300._lib import FvError
+
+    assert scan.tune_get("tc.prepass") == -1
+    with scan.tuned(tc_prepass_stride=16):
+        assert scan.tune_get("tc.prepass_stride") == 16
+    assert scan.tune_get("tc.prepass_stride") == 32
+    with pytest.raises(FvError):
+        scan.tune_set("no.such.knob", 1)

@@ -254,3 +254,29 @@ def test_fp8_rescored_recall(cuda, oracle_mod, k):
     rec = check_rescored(oracle_mod, base, queries, ids, dist, "l2", k)
     assert rec >= 0.99, rec
     assert scan.device_status() == 0
+
+
+@pytest.mark.parametrize("fp8", [False, True])
+def test_sampled_prepass_gives_the_unbounded_answer(cuda, oracle_mod, fp8):
+    """k = 100 (a 400-entry shortlist, above the 64-entry range heap): the
+    scan bounded by the sampled pre-pass returns exactly what the unbounded
+    scan returns, also when the bound is made too tight on purpose (stride
+    64, margin 1: many queries fall back to the device-side re-scan)."""
+    from fvgb300 import scan
+
+    torch = cuda
+    base = unit_mixture(300_000, 96, 512, 0.5, 21)
+    queries = unit_mixture(300, 96, 512, 0.5, 22)
+    t = (scan.Fp8Table if fp8 else scan.Fp16Table)(torch.from_numpy(base).cuda())
+    q = torch.from_numpy(queries).cuda()
+    search = scan.fp8_search if fp8 else scan.fp16_search
+    with scan.tuned(tc_prepass=0):
+        ref = res_np(search(t, q, 100, "l2"))
+    for knobs in ({"tc_prepass": 1}, {"tc_prepass": 1, "tc_prepass_stride": 64, "tc_prepass_margin": 1}):
+        with scan.tuned(**knobs):
+            got = res_np(search(t, q, 100, "l2"))
+        assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1]), knobs
+    assert scan.device_status() == 0
+    rec = check_rescored(oracle_mod, base, queries[:40], ref[0][:40], ref[1][:40], "l2", 100)
+    assert rec >= 0.99
+
