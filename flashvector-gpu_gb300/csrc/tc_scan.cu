@@ -255,6 +255,29 @@ bool encode_tmap(CUtensorMap* m, const void* ptr, bool fp8, uint64_t inner_elems
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// One CTA per SM at a time: a grid of nqb * splits CTAs runs in
+// ceil(nqb * splits / sms) waves, the last one possibly part-empty. Among
+// split counts in [s_min, 2 s_min] (within the tile count and the select
+// kernel's 16,384-key sort), take the smallest whose waves are at least
+// 1% fuller than those of every smaller candidate.
+uint32_t fill_waves(uint32_t s_min, uint32_t nqb, uint32_t ntiles, uint32_t sms, uint32_t keys_per_split) {
+  auto fullness = [&](uint32_t s) {
+    const uint64_t ctas = (uint64_t)nqb * s, waves = (ctas + sms - 1) / sms;
+    return (double)ctas / (double)(waves * sms);
+  };
+  uint32_t best = s_min;
+  double best_f = fullness(s_min);
+  for (uint32_t s = s_min + 1; s <= 2 * s_min && s <= ntiles; ++s) {
+    if (next_pow2(s * keys_per_split) > 16384u) break;
+    const double f = fullness(s);
+    if (f > best_f + 0.01) {
+      best = s;
+      best_f = f;
+    }
+  }
+  return best;
+}
+
 }  // namespace
 
 int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
@@ -284,6 +307,7 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
     splits = std::max<uint32_t>(splits, (3 * shortlist + kl * groups - 1) / (kl * groups));
   }
   splits = std::max(1u, std::min(splits, ntiles));
+  if (!opt.splits) splits = fill_waves(splits, nqb, ntiles, (uint32_t)sms, groups * kl);
   // the select kernel sorts lists*kl keys in shared memory: <= 16384
   while (splits > 1 && next_pow2(splits * groups * kl) > 16384u) --splits;
   uint32_t tps = (ntiles + splits - 1) / splits;
@@ -305,6 +329,7 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   const bool prepass = pp_knob != 0 && shortlist > kl && (pp_knob == 1 || psampled >= 64u) && psampled > 0;
   const uint32_t pkl_tmpl = std::min<uint32_t>(kl_cap, (pr + 15) / 16 * 16);
   uint32_t psplits = std::max<uint32_t>(1u, std::min<uint32_t>((uint32_t)sms / nqb, psampled));
+  psplits = fill_waves(psplits, nqb, psampled, (uint32_t)sms, groups * pr);
   while (psplits > 1 && next_pow2(psplits * groups * pr) > 16384u) --psplits;
   const uint32_t ptps = (psampled + psplits - 1) / psplits;
   psplits = (psampled + ptps - 1) / ptps;
@@ -314,7 +339,7 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   const size_t q_bytes = align_up((size_t)nq * t.padded_dim * elem, 1024);
   const size_t qn_bytes = align_up((size_t)nq * 4, 256);
   const size_t part_bytes = align_up((size_t)nq * splits * groups * kl * 8, 256);
-  const uint32_t slot_stride = (kl + 3) / 4 * 4;
+  const uint32_t slot_stride = ((prepass ? std::max(kl, pr) : kl) + 3) / 4 * 4;
   const size_t slot_bytes = align_up((size_t)nq * slot_stride * 4, 256);
   const size_t ppart_bytes = prepass ? align_up((size_t)nq * psplits * groups * pr * 8, 256) : 0;
   const size_t tau_bytes = prepass ? 2 * qn_bytes : 0;
@@ -334,12 +359,15 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   {
     ProfScope ps(fp8 ? "tc_prep_queries_fp8" : "tc_prep_queries_fp16", stream);
     const uint32_t blocks = (nq * 32 + 255) / 256;
+    // the shared-bound slots serve the scan that shares a bound: the main
+    // scan when its heap holds the whole shortlist, else the pre-pass
+    const uint32_t slot_kl = prepass ? pr : kl;
     if (fp8)
       tc_prep_queries_kernel<true><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm, qscale,
-                                                               tslot, kl, slot_stride);
+                                                               tslot, slot_kl, slot_stride);
     else
       tc_prep_queries_kernel<false><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm,
-                                                                qscale, tslot, kl, slot_stride);
+                                                                qscale, tslot, slot_kl, slot_stride);
     note_launch();
   }
 
@@ -375,7 +403,7 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
     p.tiles_per_split = ptps;
     p.partial = ppartial;
     p.kl = pr;
-    p.share = 0;
+    p.share = 1;  // the pre-pass heap holds its whole "shortlist" (pr keys)
     p.tile_stride = pstride;
     e = scan(p, (int)pkl_tmpl, nqb * psplits, fp8 ? "tc_prepass_fp8" : "tc_prepass_fp16");
     if (e != cudaSuccess) return (int)e;

@@ -73,6 +73,30 @@ struct ScanSmem {
   static constexpr size_t bytes = misc_off + 16 + 1024;                 // + alignment slack
 };
 
+// Sift `key` down from position i of a max-heap of kl keys stored with
+// stride TC_M (one heap per query row of the block).
+static __device__ __forceinline__ void heap_down(uint64_t* h, int kl, int i, uint64_t key) {
+  while (true) {
+    int l = 2 * i + 1;
+    if (l >= kl) break;
+    uint64_t cv = h[l * TC_M];
+    int c = l;
+    if (l + 1 < kl) {
+      uint64_t rv = h[(l + 1) * TC_M];
+      if (rv > cv) { cv = rv; c = l + 1; }
+    }
+    if (cv <= key) break;
+    h[i * TC_M] = cv;
+    i = c;
+  }
+  h[i * TC_M] = key;
+}
+
+// Turns kl unordered keys into a max-heap (bottom-up).
+static __device__ __noinline__ void heap_build(uint64_t* h, int kl) {
+  for (int i = kl / 2 - 1; i >= 0; --i) heap_down(h, kl, i, h[i * TC_M]);
+}
+
 static __device__ __noinline__ void heap_sift(uint64_t* h, int kl, uint64_t key) {
   // replace the root of a max-heap stored with stride TC_M
   int i = 0;
@@ -259,39 +283,67 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
     float bound = (a.qbound && qvalid) ? __ldg(a.qbound + q) : kSentinelDist;
     uint32_t* slots = (a.share && qvalid) ? a.tslot + (size_t)q * a.tslot_stride : nullptr;
 
+    // Until kl keys are held the heap is an unordered list (appends cost
+    // one store); on the kl-th key it is heapified once and from then on a
+    // key replaces the root. The kept set is the same either way.
+    int fill = 0;
     auto keep = [&](float dist, uint32_t slot) {
-      heap_sift(h, kl, make_key(dist, slot));
-      const uint64_t root = h[0];
-      worst = root == kSentinelKey ? kSentinelDist : key_dist(root);
+      const uint64_t key = make_key(dist, slot);
+      if (fill < kl) {
+        h[fill * TC_M] = key;
+        if (++fill == kl) {
+          heap_build(h, kl);
+          worst = key_dist(h[0]);
+        }
+      } else {
+        heap_sift(h, kl, key);
+        worst = key_dist(h[0]);
+      }
       if (slots) atomicMin(slots + __umulhi(slot * 2654435761u, (uint32_t)kl), float_order(dist));
     };
 
-    // per-warp copy of the current tile's column data (norms, fp8 scales,
+    // per-warp copy of the current tile's column data (norms, fp8 factors,
     // mask words): staged by the warp itself, so the epilogue warps never
-    // wait on one another
+    // wait on one another. The global loads for tile i + G are issued into
+    // registers while tile i is processed (lane l holds columns l + 32 r).
     float* cb = colbuf + (warp - 2) * 2 * TC_N;
     uint32_t* cm = colmask + (warp - 2) * 8;
+    float pre_n[TC_N / 32], pre_s[TC_N / 32];
+    uint32_t pre_m = 0;
+    auto prefetch = [&](uint32_t tile) {
+      const uint32_t v0n = (t_begin + tile) * tstride * TC_N;
+#pragma unroll
+      for (int r = 0; r < TC_N / 32; ++r) {
+        const uint32_t slot = v0n + lane + 32 * r;
+        const bool in = slot < a.n;
+        pre_n[r] = (METRIC != METRIC_INNER_PRODUCT && in) ? __ldg(a.xnorm + slot) : 0.f;
+        // per-column factor of the scaled dot: -2 xs (L2), -xs (IP), xs (cosine)
+        const float xs = (FP8 && in) ? __ldg(a.xscale + slot) : 0.f;
+        pre_s[r] = METRIC == METRIC_L2 ? -2.0f * xs : (METRIC == METRIC_INNER_PRODUCT ? -xs : xs);
+      }
+      pre_m = 0;
+      if (lane < 8) {
+        const uint32_t c0 = v0n + lane * 32;
+        if (c0 < a.n) {
+          const uint32_t cnt = min(32u, a.n - c0);
+          pre_m = cnt == 32 ? 0xFFFFFFFFu : ((1u << cnt) - 1u);
+          if (a.mask) pre_m &= __ldg(a.mask + (c0 >> 5));
+        }
+      }
+    };
+    if ((uint32_t)grp < my_tiles) prefetch((uint32_t)grp);
     for (uint32_t i = (uint32_t)grp; i < my_tiles; i += G) {
       const uint32_t buf = i & 1, use = i >> 1;
       const uint32_t v0 = (t_begin + i) * tstride * TC_N;
       __syncwarp();
-      for (int c = lane; c < TC_N; c += 32) {
-        const uint32_t slot = v0 + c;
-        const bool in = slot < a.n;
-        if (METRIC != METRIC_INNER_PRODUCT) cb[c] = in ? __ldg(a.xnorm + slot) : 0.f;
-        if (FP8) cb[TC_N + c] = in ? __ldg(a.xscale + slot) : 0.f;
+#pragma unroll
+      for (int r = 0; r < TC_N / 32; ++r) {
+        if (METRIC != METRIC_INNER_PRODUCT) cb[lane + 32 * r] = pre_n[r];
+        if (FP8) cb[TC_N + lane + 32 * r] = pre_s[r];
       }
-      if (lane < 8) {
-        const uint32_t c0 = v0 + lane * 32;
-        uint32_t w = 0;
-        if (c0 < a.n) {
-          const uint32_t cnt = min(32u, a.n - c0);
-          w = cnt == 32 ? 0xFFFFFFFFu : ((1u << cnt) - 1u);
-          if (a.mask) w &= __ldg(a.mask + (c0 >> 5));
-        }
-        cm[lane] = w;
-      }
+      if (lane < 8) cm[lane] = pre_m;
       __syncwarp();
+      if (i + G < my_tiles) prefetch(i + G);
       // the shared bound, loaded before the accumulator wait hides its latency
       uint32_t smax = 0;
       if (slots)
@@ -318,20 +370,46 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
         tc::tmem_wait_ld(ra);
         tc::reg_fence(rb);
         if (mw == 0ull) continue;
-        // exact per-column distances (the expressions the insertion test
-        // uses); v[0..32) columns c0.., v[32..64) columns c0+32..
+        // per-column values v, v[0..32) columns c0.., v[32..64) columns
+        // c0+32..; the distance is D(v): L2  D(v) = max(0, ||q||^2 + v) with
+        // v = ||x||^2 - 2 <q, x> (the query's norm is added after the
+        // minimum, D being monotone), IP  D(v) = v = -<q, x>, cosine the
+        // full expression. FP8 dots carry the per-query and per-row scales.
         float v[64];
+        if (METRIC == METRIC_COSINE) {
 #pragma unroll
-        for (int j = 0; j < 64; ++j) {
-          float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
-          if (FP8) dot = dot * (qs * cb[TC_N + c0 + j]);
-          if (METRIC == METRIC_INNER_PRODUCT)
-            v[j] = -dot;
-          else if (METRIC == METRIC_COSINE)
+          for (int j = 0; j < 64; ++j) {
+            float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
+            if (FP8) dot = dot * (qs * cb[TC_N + c0 + j]);
             v[j] = 1.0f - dot / (sqrtf(qn * cb[c0 + j]) + 1e-8f);
-          else
-            v[j] = fmaxf(0.f, fmaf(-2.0f, dot, qn + cb[c0 + j]));
+          }
+        } else {
+          const float4* nb = reinterpret_cast<const float4*>(cb + c0);
+          const float4* sb = reinterpret_cast<const float4*>(cb + TC_N + c0);
+#pragma unroll
+          for (int j4 = 0; j4 < 16; ++j4) {
+            const float4 n4 = METRIC == METRIC_L2 ? nb[j4] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 s4 = FP8 ? sb[j4] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float nv[4] = {n4.x, n4.y, n4.z, n4.w};
+            const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const int j = 4 * j4 + e;
+              const float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
+              if (FP8)
+                v[j] = METRIC == METRIC_L2 ? fmaf(dot * qs, sv[e], nv[e]) : (dot * qs) * sv[e];
+              else
+                v[j] = METRIC == METRIC_L2 ? fmaf(-2.0f, dot, nv[e]) : -dot;
+            }
+          }
         }
+        auto D = [&](float x) { return METRIC == METRIC_L2 ? fmaxf(0.f, qn + x) : x; };
+        // admission threshold in the v domain: every v whose distance could
+        // enter (D(v) < worst and D(v) <= bound) has v <= thr (for L2 the
+        // subtraction of the query norm is padded by a relative slack, so
+        // thr errs on the admitting side; exact tests follow)
+        const float w = fminf(worst, bound);
+        const float thr = METRIC == METRIC_L2 ? (w - qn) + 1e-6f * (fabsf(w) + fabsf(qn)) + 1e-30f : w;
         // pairwise minima, then a min tree: a 64-column batch whose minimum
         // cannot enter is skipped whole (the common case once warm)
         float m1[32], m[16];
@@ -340,20 +418,20 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
 #pragma unroll
         for (int j = 0; j < 16; ++j) m[j] = fminf(m1[j], m1[j + 16]);
 #pragma unroll
-        for (int w = 8; w > 0; w >>= 1)
+        for (int t = 8; t > 0; t >>= 1)
 #pragma unroll
-          for (int j = 0; j < w; ++j) m[j] = fminf(m[j], m[j + w]);
-        if (!(m[0] < worst && m[0] <= bound)) continue;
-        // pairs (j, j+32) that may enter, walked lane-parallel
+          for (int j = 0; j < t; ++j) m[j] = fminf(m[j], m[j + t]);
+        if (!(m[0] <= thr)) continue;
+        // pairs (j, j+32) that may hold a candidate, walked lane-parallel
         uint32_t pass = 0;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) pass |= (uint32_t)(m1[j] < worst && m1[j] <= bound) << j;
+        for (int j = 0; j < 32; ++j) pass |= (uint32_t)(m1[j] <= thr) << j;
         pass &= (uint32_t)mw | (uint32_t)(mw >> 32);
         while (pass) {
           const int j = __ffs(pass) - 1;
           pass &= pass - 1;
-          const float dlo = select32(v, j);
-          const float dhi = select32(v + 32, j);
+          const float dlo = D(select32(v, j));
+          const float dhi = D(select32(v + 32, j));
           if (((mw >> j) & 1ull) && dlo < worst && dlo <= bound) keep(dlo, v0 + c0 + j);
           if (((mw >> (j + 32)) & 1ull) && dhi < worst && dhi <= bound) keep(dhi, v0 + c0 + j + 32);
         }
@@ -363,6 +441,13 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
       if (lane == 0) tc::mbar_arrive(&acc_empty[buf]);
     }
     if (qvalid) {
+      // entry 0 of a dumped list is its largest key (the select kernel tests
+      // it for overflow): a full heap has it there already; a list that never
+      // filled gets one of its sentinels moved there
+      if (fill > 0 && fill < kl) {
+        h[fill * TC_M] = h[0];
+        h[0] = kSentinelKey;
+      }
       uint64_t* dst = a.partial + (((size_t)q * a.splits + split) * G + grp) * kl;
       for (int i = 0; i < kl; ++i) dst[i] = h[i * TC_M];
     }
