@@ -21,6 +21,7 @@
 //             memory max-heap. No distance matrix ever reaches HBM.
 // A CTA scans a contiguous range of base tiles; the per-(query, range)
 // heaps are merged by tc_select_kernel, which also rescoring in fp32.
+#include <cmath>
 #include <cuda_fp16.h>
 #include <cuda_fp8.h>
 #include <cudaTypedefs.h>
@@ -35,7 +36,8 @@ namespace {
 // ---------------------------------------------------------------------------
 // Query preparation: fp32 -> fp16 (round to nearest even, as the reference
 // converts queries: ivf_quant_lookup.cu:953) or fp32 -> e4m3 with a per-query
-// scale amax/448; ||q||^2 with fmaf in dimension order (:922-928).
+// scale amax/448; ||q||^2 of the fp32 query (the reference's :922-928, here
+// summed across the warp: it only enters the scan's approximate distance).
 // One warp per query.
 // ---------------------------------------------------------------------------
 template <bool FP8>
@@ -50,10 +52,14 @@ __global__ void __launch_bounds__(256) tc_prep_queries_kernel(const float* __res
   const float* src = q + (size_t)qi * dim;
   // shared-bound slots: empty (all ones) for the kl used, 0 for the padding
   for (uint32_t s = lane; s < stride; s += 32) tslot[(size_t)qi * stride + s] = s < kl ? 0xFFFFFFFFu : 0u;
-  if (lane == 0) {
+  {
+    // ||q||^2 of the scan's approximate distance (L2 and cosine); the exact
+    // fp32 rescore recomputes distances in the reference's order
     float s = 0.f;
-    for (uint32_t d = 0; d < dim; ++d) s = fmaf(src[d], src[d], s);
-    qnorm[qi] = s;
+    for (uint32_t d = lane; d < dim; d += 32) s = fmaf(src[d], src[d], s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) qnorm[qi] = s;
   }
   if (FP8) {
     float amax = 0.f;
@@ -255,6 +261,24 @@ bool encode_tmap(CUtensorMap* m, const void* ptr, bool fp8, uint64_t inner_elems
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// Sampled rank for the pre-pass bound. A sample of every stride-th tile
+// holds each of a query's top (shortlist - 1) rows with probability
+// 1 / stride, so the number of them in the sample is about Poisson(lambda =
+// shortlist / stride); the sample's r-th best distance is below the query's
+// shortlist-th distance (and the query needs the re-scan) only when that
+// count reaches r. Returns the smallest r whose Poisson tail P(X >= r) is
+// below `tail`.
+uint32_t poisson_rank(double lambda, double tail) {
+  double term = std::exp(-lambda), cdf = 0.0;
+  uint32_t r = 0;
+  while (1.0 - cdf >= tail && r < 4096) {
+    cdf += term;
+    ++r;
+    term *= lambda / r;
+  }
+  return r;
+}
+
 // One CTA per SM at a time: a grid of nqb * splits CTAs runs in
 // ceil(nqb * splits / sms) waves, the last one possibly part-empty. Among
 // split counts in [s_min, 2 s_min] (within the tile count and the select
@@ -299,7 +323,12 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   const uint32_t nqb = (nq + TC_M - 1) / TC_M;
   const uint32_t ntiles = (t.n + TC_N - 1) / TC_N;
   const int sms = device_sm_count();
-  uint32_t splits = opt.splits ? opt.splits : std::max<uint32_t>(1u, (uint32_t)sms / nqb);
+  // CTA pairs (cta_group::2) for long rows: two query blocks share each
+  // base tile, each SM streaming half of it
+  const int64_t pair_knob = tune_value("tc.pair", -1);
+  const bool pair = groups == 1 && pair_knob != 0;
+  const uint32_t nqb_grid = pair ? 2 * ((nqb + 1) / 2) : nqb;  // CTAs per split
+  uint32_t splits = opt.splits ? opt.splits : std::max<uint32_t>(1u, (uint32_t)sms / nqb_grid);
   if (!opt.splits && shortlist > kl) {
     // a (query, range, group) heap keeps kl keys: split the base so that each
     // heap holds, in expectation, a third of its share of the shortlist (a
@@ -307,29 +336,35 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
     splits = std::max<uint32_t>(splits, (3 * shortlist + kl * groups - 1) / (kl * groups));
   }
   splits = std::max(1u, std::min(splits, ntiles));
-  if (!opt.splits) splits = fill_waves(splits, nqb, ntiles, (uint32_t)sms, groups * kl);
+  if (!opt.splits) splits = fill_waves(splits, nqb_grid, ntiles, (uint32_t)sms, groups * kl);
   // the select kernel sorts lists*kl keys in shared memory: <= 16384
   while (splits > 1 && next_pow2(splits * groups * kl) > 16384u) --splits;
   uint32_t tps = (ntiles + splits - 1) / splits;
   splits = (ntiles + tps - 1) / tps;
 
-  // Sampled pre-pass (large shortlists only): the CTAs of a query cannot
-  // share a bound when the shortlist exceeds the per-range heap, so each
-  // range would insert ~kl (1 + ln(rows / kl)) keys per query. A scan of
-  // every stride-th tile gives each query its r-th best sampled distance,
-  // r = ceil(margin * shortlist / stride), an upper bound on its shortlist-th
-  // distance unless the sample is unlucky; the full scan then admits only
+  // Sampled pre-pass: the CTAs of a query cannot share a bound when the
+  // shortlist exceeds the per-range heap, so each range would insert
+  // ~kl (1 + ln(rows / kl)) keys per query. A scan of every stride-th tile
+  // gives each query its r-th best sampled distance (r from the Poisson tail
+  // below, or ceil(margin * shortlist / stride) when the margin knob is
+  // set), an upper bound on its shortlist-th distance unless the sample is
+  // unlucky (probability < 1e-7 per query); the full scan then admits only
   // rows within it. Queries whose bounded scan comes up short are scanned
   // again without the bound (device-side, no host round trip).
   const int64_t pp_knob = tune_value("tc.prepass", -1);
   const uint32_t pstride = (uint32_t)std::max<int64_t>(2, tune_value("tc.prepass_stride", 32));
-  const uint32_t pmargin = (uint32_t)std::max<int64_t>(1, tune_value("tc.prepass_margin", 3));
-  const uint32_t pr = std::min<uint32_t>(kl_cap, (pmargin * shortlist + pstride - 1) / pstride);
+  const int64_t pmargin = tune_value("tc.prepass_margin", 0);
+  const uint32_t pr = std::max<uint32_t>(
+      1u, std::min<uint32_t>(kl_cap, pmargin > 0 ? (uint32_t)((pmargin * shortlist + pstride - 1) / pstride)
+                                                 : poisson_rank((double)shortlist / pstride, 1e-7)));
   const uint32_t psampled = (ntiles + pstride - 1) / pstride;
-  const bool prepass = pp_knob != 0 && shortlist > kl && (pp_knob == 1 || psampled >= 64u) && psampled > 0;
+  // automatic: bases of >= 64 sampled tiles (the main scan then uses the
+  // pre-pass bound instead of the cross-CTA shared one); forced on (knob 1):
+  // any base
+  const bool prepass = psampled > 0 && (pp_knob == 1 || (pp_knob != 0 && psampled >= 64u));
   const uint32_t pkl_tmpl = std::min<uint32_t>(kl_cap, (pr + 15) / 16 * 16);
-  uint32_t psplits = std::max<uint32_t>(1u, std::min<uint32_t>((uint32_t)sms / nqb, psampled));
-  psplits = fill_waves(psplits, nqb, psampled, (uint32_t)sms, groups * pr);
+  uint32_t psplits = std::max<uint32_t>(1u, std::min<uint32_t>((uint32_t)sms / nqb_grid, psampled));
+  psplits = fill_waves(psplits, nqb_grid, psampled, (uint32_t)sms, groups * pr);
   while (psplits > 1 && next_pow2(psplits * groups * pr) > 16384u) --psplits;
   const uint32_t ptps = (psampled + psplits - 1) / psplits;
   psplits = (psampled + ptps - 1) / ptps;
@@ -371,9 +406,10 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
     note_launch();
   }
 
-  CUtensorMap ta, tb;
+  CUtensorMap ta, tb, tb_half;
   if (!encode_tmap(&ta, qprep, fp8, t.padded_dim, nq, (uint64_t)t.padded_dim * elem, TC_M) ||
-      !encode_tmap(&tb, t.base, fp8, t.padded_dim, t.n, (uint64_t)t.padded_dim * elem, TC_N))
+      !encode_tmap(&tb, t.base, fp8, t.padded_dim, t.n, (uint64_t)t.padded_dim * elem, TC_N) ||
+      (pair && !encode_tmap(&tb_half, t.base, fp8, t.padded_dim, t.n, (uint64_t)t.padded_dim * elem, TC_N / 2)))
     return FV_ERR_ARG;
 
   TcScanArgs a{};
@@ -391,10 +427,15 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   a.status = status_word();
   a.filters = filters;
   a.tile_stride = 1;
-  auto scan = [&](const TcScanArgs& args, int kl_t, uint32_t grid, const char* name) -> cudaError_t {
+  // use_pair: the CTA-pair variant (not for the re-scan of flagged queries,
+  // whose blocks leave independently)
+  auto scan = [&](const TcScanArgs& args, int kl_t, uint32_t splits_n, const char* name, bool use_pair) -> cudaError_t {
     ProfScope ps(name, stream);
-    return fp8 ? dispatch_tc_scan_fp8(kl_t, groups, (int)metric, ta, tb, args, grid, stream)
-               : dispatch_tc_scan_fp16(kl_t, groups, (int)metric, ta, tb, args, grid, stream);
+    const int g = use_pair ? -1 : groups;
+    const uint32_t grid = (use_pair ? nqb_grid : nqb) * splits_n;
+    const CUtensorMap& b = use_pair ? tb_half : tb;
+    return fp8 ? dispatch_tc_scan_fp8(kl_t, g, (int)metric, ta, b, args, grid, stream)
+               : dispatch_tc_scan_fp16(kl_t, g, (int)metric, ta, b, args, grid, stream);
   };
   cudaError_t e;
   if (prepass) {
@@ -405,7 +446,7 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
     p.kl = pr;
     p.share = 1;  // the pre-pass heap holds its whole "shortlist" (pr keys)
     p.tile_stride = pstride;
-    e = scan(p, (int)pkl_tmpl, nqb * psplits, fp8 ? "tc_prepass_fp8" : "tc_prepass_fp16");
+    e = scan(p, (int)pkl_tmpl, psplits, fp8 ? "tc_prepass_fp8" : "tc_prepass_fp16", pair);
     if (e != cudaSuccess) return (int)e;
     const uint32_t total = psplits * groups * pr, pow2 = next_pow2(total);
     e = cudaFuncSetAttribute(tc_tau_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(pow2 * 8));
@@ -422,9 +463,9 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   a.tiles_per_split = tps;
   a.partial = partial;
   a.kl = kl;
-  a.share = kl == shortlist ? 1u : 0u;
+  a.share = (kl == shortlist && !prepass) ? 1u : 0u;
   a.qbound = tau;
-  e = scan(a, (int)kl_tmpl, nqb * splits, fp8 ? "tc_scan_fp8" : "tc_scan_fp16");
+  e = scan(a, (int)kl_tmpl, splits, fp8 ? "tc_scan_fp8" : "tc_scan_fp16", pair);
   if (e != cudaSuccess) return (int)e;
 
   SelectArgs s{partial, splits * groups, kl, next_pow2(splits * groups * kl), shortlist, k, queries, t.vectors, t.dim,
@@ -446,7 +487,7 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
     f.qbound = nullptr;
     f.active = redo;
     f.share = 0;
-    e = scan(f, (int)kl_tmpl, nqb * splits, fp8 ? "tc_rescan_fp8" : "tc_rescan_fp16");
+    e = scan(f, (int)kl_tmpl, splits, fp8 ? "tc_rescan_fp8" : "tc_rescan_fp16", false);
     if (e != cudaSuccess) return (int)e;
     SelectArgs r = s;
     r.tau = nullptr;

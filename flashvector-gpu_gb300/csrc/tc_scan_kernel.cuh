@@ -60,11 +60,13 @@ struct TcScanArgs {
   uint32_t tile_stride;        // scan every tile_stride-th 256-row tile (a sample when > 1)
 };
 
-template <int KL, int STAGES, int G>
+// PAIR: a CTA of a cta_group::2 pair holds half of each 256-row base tile.
+template <int KL, int STAGES, int G, bool PAIR = false>
 struct ScanSmem {
+  static constexpr size_t b_stage = PAIR ? B_STAGE / 2 : B_STAGE;
   static constexpr size_t a_off = 0;
   static constexpr size_t b_off = a_off + (size_t)STAGES * A_STAGE;
-  static constexpr size_t heap_off = b_off + (size_t)STAGES * B_STAGE;
+  static constexpr size_t heap_off = b_off + (size_t)STAGES * b_stage;
   static constexpr size_t col_off = heap_off + (size_t)G * KL * TC_M * 8;  // [4G warps][2][TC_N] floats
   static constexpr size_t cmask_off = col_off + 4 * G * 2 * TC_N * 4;      // [4G warps][8] words
   static constexpr size_t bar_off = cmask_off + 4 * G * 8 * 4;          // barriers
@@ -133,10 +135,20 @@ static __device__ __forceinline__ float select32(const float* v, int j) {
 // G epilogue groups: with G = 2 each group owns one of the two TMEM
 // accumulator buffers (tiles alternate between the groups) and keeps its
 // own heaps, which are dumped as separate lists (partial row split * G + g).
-template <bool FP8, int KL, int STAGES, int METRIC, int G>
+//
+// PAIR: the CTA is one of a cluster of two (a cta_group::2 pair) sharing the
+// same base range: CTA r holds query block 2p + r and rows [128 r, 128 r +
+// 128) of every 256-row tile; the even CTA issues M=256 MMAs whose 128
+// accumulator lanes land in each CTA's TMEM, so each SM streams 16 KB of
+// base per K block instead of 32 KB and the ring gets deeper. Both CTAs'
+// TMA loads count on the even CTA's full barriers; the even CTA's commits
+// are multicast to both CTAs' barriers; the odd CTA's epilogue arrives on
+// the even CTA's accumulator barriers.
+template <bool FP8, int KL, int STAGES, int METRIC, int G, bool PAIR>
 __global__ void __launch_bounds__(scan_threads(G), 1)
     tc_scan_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcScanArgs a) {
-  using L = ScanSmem<KL, STAGES, G>;
+  using L = ScanSmem<KL, STAGES, G, PAIR>;
+  constexpr uint32_t b_stage = (uint32_t)L::b_stage;
   constexpr int SCAN_THREADS = scan_threads(G);
   extern __shared__ uint8_t smem_raw[];
   uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -155,8 +167,17 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
   volatile uint32_t* abort_flag = tmem_slot + 1;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t qb = blockIdx.x % a.nqb, split = blockIdx.x / a.nqb;
-  if (a.active) {
+  uint32_t qb, split, rank = 0;
+  if constexpr (PAIR) {
+    rank = tc::cluster_ctarank();
+    const uint32_t c = blockIdx.x >> 1, npairs = (a.nqb + 1) / 2;
+    qb = 2 * (c % npairs) + rank;
+    split = c / npairs;
+  } else {
+    qb = blockIdx.x % a.nqb;
+    split = blockIdx.x / a.nqb;
+  }
+  if (!PAIR && a.active) {
     // a re-scan of flagged queries: a block holding none of them leaves at once
     int any = 0;
     for (int r = threadIdx.x; r < TC_M; r += SCAN_THREADS) {
@@ -178,17 +199,21 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
     }
     for (int b = 0; b < 2; ++b) {
       tc::mbar_init(&acc_full[b], 1);
-      tc::mbar_init(&acc_empty[b], 4);  // the 4 epilogue warps that drain buffer b
+      tc::mbar_init(&acc_empty[b], PAIR ? 8 : 4);  // the epilogue warps (of both CTAs) that drain buffer b
     }
     tc::mbar_init(mma_done, 1);
     *abort_flag = 0;
     tc::fence_mbar_init();
   }
   if (warp == 1) {
-    tc::tmem_alloc(tmem_slot, 512);
+    if constexpr (PAIR)
+      tc::tmem_alloc_pair(tmem_slot, 512);
+    else
+      tc::tmem_alloc(tmem_slot, 512);
     tc::tc_fence_before();
   }
   __syncthreads();
+  if constexpr (PAIR) tc::cluster_sync();  // both CTAs' barriers exist before either signals the other's
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
@@ -212,10 +237,19 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
             ok = false;
             break;
           }
-          tc::mbar_arrive_expect_tx(&full[stage], A_STAGE + B_STAGE);
-          tc::tma_load_2d(sA + stage * A_STAGE, &tmA, &full[stage], (int32_t)(kb * kb_elems), (int32_t)(qb * TC_M),
-                          pol_a);
-          tc::tma_load_2d(sB + stage * B_STAGE, &tmB, &full[stage], (int32_t)(kb * kb_elems), row_b, pol_b);
+          if constexpr (PAIR) {
+            const uint32_t fb = tc::mapa(tc::smem_addr(&full[stage]), 0);  // the even CTA's full barrier
+            if (rank == 0) tc::mbar_arrive_expect_tx(&full[stage], 2 * (A_STAGE + b_stage));
+            tc::tma_load_2d_pair(sA + stage * A_STAGE, &tmA, fb, (int32_t)(kb * kb_elems), (int32_t)(qb * TC_M),
+                                 pol_a);
+            tc::tma_load_2d_pair(sB + stage * b_stage, &tmB, fb, (int32_t)(kb * kb_elems),
+                                 row_b + (int32_t)(rank * (TC_N / 2)), pol_b);
+          } else {
+            tc::mbar_arrive_expect_tx(&full[stage], A_STAGE + B_STAGE);
+            tc::tma_load_2d(sA + stage * A_STAGE, &tmA, &full[stage], (int32_t)(kb * kb_elems), (int32_t)(qb * TC_M),
+                            pol_a);
+            tc::tma_load_2d(sB + stage * B_STAGE, &tmB, &full[stage], (int32_t)(kb * kb_elems), row_b, pol_b);
+          }
           issued_parity[stage] = (int32_t)phase;
           if (++stage == STAGES) {
             stage = 0;
@@ -224,17 +258,20 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
         }
       }
       // drain: every copy issued must have landed before the CTA may exit
-      // (normally they all have; after an abort this waits a bounded time)
+      // (normally they all have; after an abort this waits a bounded time).
+      // A pair's copies all count on the even CTA's barriers, which it drains.
       uint32_t no_abort = 0;
+      if (!PAIR || rank == 0) {
 #pragma unroll
-      for (int s = 0; s < STAGES; ++s)
-        if (issued_parity[s] >= 0)
-          tc::mbar_wait(&full[s], (uint32_t)issued_parity[s], &no_abort, a.status, 100000000ull);
+        for (int s = 0; s < STAGES; ++s)
+          if (issued_parity[s] >= 0)
+            tc::mbar_wait(&full[s], (uint32_t)issued_parity[s], &no_abort, a.status, 100000000ull);
+      }
     }
   } else if (warp == 1) {
     // ------------------------------------------------------- MMA issuer
-    if (lane == 0) {
-      constexpr uint32_t idesc = tc::idesc_f32acc(0, 0, TC_M, TC_N);
+    if (lane == 0 && (!PAIR || rank == 0)) {
+      constexpr uint32_t idesc = tc::idesc_f32acc(0, 0, PAIR ? 2 * TC_M : TC_M, TC_N);
       uint32_t stage = 0, phase = 0;
       bool ok = true;
       for (uint32_t i = 0; ok && i < my_tiles; ++i) {
@@ -249,21 +286,36 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
           }
           tc::tc_fence_after();
           const uint32_t a_base = tc::smem_addr(sA + stage * A_STAGE);
-          const uint32_t b_base = tc::smem_addr(sB + stage * B_STAGE);
+          const uint32_t b_base = tc::smem_addr(sB + stage * b_stage);
 #pragma unroll
           for (uint32_t kk = 0; kk < 4; ++kk) {
-            tc::mma<FP8>(d_tmem, tc::sdesc_k_sw128(a_base + kk * 32), tc::sdesc_k_sw128(b_base + kk * 32), idesc,
-                         (kb | kk) != 0);
+            if constexpr (PAIR)
+              tc::mma_pair<FP8>(d_tmem, tc::sdesc_k_sw128(a_base + kk * 32), tc::sdesc_k_sw128(b_base + kk * 32),
+                                idesc, (kb | kk) != 0);
+            else
+              tc::mma<FP8>(d_tmem, tc::sdesc_k_sw128(a_base + kk * 32), tc::sdesc_k_sw128(b_base + kk * 32), idesc,
+                           (kb | kk) != 0);
           }
-          tc::mma_commit(&empty[stage]);
+          if constexpr (PAIR)
+            tc::mma_commit_pair(&empty[stage], 3);
+          else
+            tc::mma_commit(&empty[stage]);
           if (++stage == STAGES) {
             stage = 0;
             phase ^= 1;
           }
         }
-        if (ok) tc::mma_commit(&acc_full[buf]);
+        if (ok) {
+          if constexpr (PAIR)
+            tc::mma_commit_pair(&acc_full[buf], 3);
+          else
+            tc::mma_commit(&acc_full[buf]);
+        }
       }
-      tc::mma_commit(mma_done);
+      if constexpr (PAIR)
+        tc::mma_commit_pair(mma_done, 3);
+      else
+        tc::mma_commit(mma_done);
     }
   } else {
     // --------------------------------------------------------- epilogue
@@ -438,7 +490,12 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
       }
       tc::tc_fence_before();
       __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&acc_empty[buf]);
+      if (lane == 0) {
+        if (PAIR && rank != 0)
+          tc::mbar_arrive_cluster(tc::mapa(tc::smem_addr(&acc_empty[buf]), 0));
+        else
+          tc::mbar_arrive(&acc_empty[buf]);
+      }
     }
     if (qvalid) {
       // entry 0 of a dumped list is its largest key (the select kernel tests
@@ -461,19 +518,43 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
     tc::mbar_wait(mma_done, 0, &no_abort, a.status, 100000000ull);
     __syncwarp();
     tc::tc_fence_after();
-    tc::tmem_dealloc(tmem, 512);
+    if constexpr (PAIR)
+      tc::tmem_dealloc_pair(tmem, 512);
+    else
+      tc::tmem_dealloc(tmem, 512);
   }
+  // a pair's CTAs read each other's shared memory (MMA operands, barriers):
+  // neither leaves before the other is done
+  if constexpr (PAIR) tc::cluster_sync();
 }
 
 
-template <bool FP8, int KL, int STAGES, int METRIC, int G>
+template <bool FP8, int KL, int STAGES, int METRIC, int G, bool PAIR = false>
 cudaError_t launch_scan_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a, uint32_t grid,
                                cudaStream_t stream) {
-  using L = ScanSmem<KL, STAGES, G>;
+  using L = ScanSmem<KL, STAGES, G, PAIR>;
   static_assert(L::bytes <= 227 * 1024, "scan shared memory above the 227 KB per-CTA limit");
-  auto kern = tc_scan_kernel<FP8, KL, STAGES, METRIC, G>;
+  auto kern = tc_scan_kernel<FP8, KL, STAGES, METRIC, G, PAIR>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes);
   if (e != cudaSuccess) return e;
+  if constexpr (PAIR) {
+    // grid = 2 CTAs per (query-block pair, split), clusters of two
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid, 1, 1);
+    cfg.blockDim = dim3(scan_threads(G), 1, 1);
+    cfg.dynamicSmemBytes = L::bytes;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, kern, ta, tb, a);
+    note_launch();
+    return e;
+  }
   kern<<<grid, scan_threads(G), L::bytes, stream>>>(ta, tb, a);
   note_launch();
   return cudaGetLastError();
@@ -481,10 +562,21 @@ cudaError_t launch_scan_kernel(const CUtensorMap& ta, const CUtensorMap& tb, con
 
 // groups == 2 (short K: one or two K blocks per tile, where the epilogue
 // rather than the MMA bounds a tile) halves the stage ring and caps the heap
-// at 48 entries so that two groups' heaps fit next to it.
+// at 48 entries so that two groups' heaps fit next to it. groups == -1
+// selects the CTA-pair variant (grid = 2 CTAs per cluster).
 template <bool FP8, int METRIC>
 cudaError_t dispatch_scan_kl(int kl, int groups, const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a,
                              uint32_t grid, cudaStream_t stream) {
+  if (groups == -1) {
+    // cta_group::2 pairs (one epilogue group): 16 KB of base per stage frees
+    // room for 4-6 stages
+    switch (kl) {
+      case 16: return launch_scan_kernel<FP8, 16, 6, METRIC, 1, true>(ta, tb, a, grid, stream);
+      case 32: return launch_scan_kernel<FP8, 32, 5, METRIC, 1, true>(ta, tb, a, grid, stream);
+      case 48: return launch_scan_kernel<FP8, 48, 5, METRIC, 1, true>(ta, tb, a, grid, stream);
+      default: return launch_scan_kernel<FP8, 64, 4, METRIC, 1, true>(ta, tb, a, grid, stream);
+    }
+  }
   if (groups == 2) {
     switch (kl) {
       case 16: return launch_scan_kernel<FP8, 16, 3, METRIC, 2>(ta, tb, a, grid, stream);

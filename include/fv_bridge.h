@@ -268,8 +268,13 @@ int fv_profile_summary(char* buf, size_t len);
  *                       per-range heap first scan a strided sample of the
  *                       base for a per-query admission bound
  *   "tc.prepass_stride" sample stride in 256-row tiles (default 32)
- *   "tc.prepass_margin" sampled rank = ceil(margin * shortlist / stride)
- *                       (default 3)
+ *   "tc.prepass_margin" 0 (default): the sampled rank r is the smallest
+ *                       with P(Poisson(shortlist / stride) >= r) < 1e-7;
+ *                       m > 0: r = ceil(m * shortlist / stride)
+ *   "tc.pair"           -1 automatic (default), 0 off, 1 on: tensor-core scans
+ *                       of long rows (more than two K blocks) run on CTA
+ *                       pairs (cta_group::2), each SM streaming half of
+ *                       every base tile
  * Unknown keys return FV_ERR_ARG. Values apply to launches issued after the
  * call. */
 int fv_tune_set(const char* key, int64_t value);

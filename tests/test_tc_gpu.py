@@ -280,3 +280,25 @@ def test_sampled_prepass_gives_the_unbounded_answer(cuda, oracle_mod, fp8):
     rec = check_rescored(oracle_mod, base, queries[:40], ref[0][:40], ref[1][:40], "l2", 100)
     assert rec >= 0.99
 
+
+
+@pytest.mark.parametrize("fp8", [False, True])
+@pytest.mark.parametrize("n,dim,nq,k", [(70_001, 768, 300, 10), (20_000, 384, 129, 100), (5_000, 200, 1, 16)])
+def test_cta_pair_scan_matches_single_cta(cuda, fp8, n, dim, nq, k):
+    """The cta_group::2 pair variant (two SMs per 256-row tile) returns
+    exactly what the one-SM kernel returns: odd query-block counts, partial
+    last tiles, the pre-pass path (k = 100) and a single query."""
+    from fvgb300 import scan
+
+    torch = cuda
+    base = unit_mixture(n, dim, 128, 0.4, n + dim)
+    queries = unit_mixture(nq, dim, 128, 0.4, nq + 1)
+    t = (scan.Fp8Table if fp8 else scan.Fp16Table)(torch.from_numpy(base).cuda())
+    q = torch.from_numpy(queries).cuda()
+    search = scan.fp8_search if fp8 else scan.fp16_search
+    with scan.tuned(tc_pair=0):
+        ref = res_np(search(t, q, k, "l2"))
+    with scan.tuned(tc_pair=1, tc_prepass=1 if k == 100 else -1):
+        got = res_np(search(t, q, k, "l2"))
+    assert scan.device_status() == 0
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
