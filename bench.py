@@ -55,7 +55,8 @@ def parse_args():
     ap.add_argument("--dim", type=int, default=None)
     ap.add_argument("--batch", type=int, default=None)
     ap.add_argument("--k", type=int, default=None)
-    ap.add_argument("--overfetch", type=int, default=4)
+    ap.add_argument("--overfetch", type=int, default=4, help="fp16_ip: shortlist = overfetch x k")
+    ap.add_argument("--overfetch-fp8", type=int, default=None, help="fp8_l2: over-fetch (default: autotuned)")
     ap.add_argument("--nprobe", type=str, default="8,32,128", help="ivf_pq: comma-separated nprobe sweep")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -526,7 +527,10 @@ def run_workload(a, world, rank, local):
         qb = [qpool[:a.batch].contiguous(), qpool[a.batch:].contiguous()]
         table = scan.Fp8Table(base)
         out = scan.empty_results(a.batch, a.k, dev)
-        opts = scan.options(overfetch=a.overfetch, boundary_fp64=1)
+        # over-fetch 0: the committed autotuner's value for this shape
+        fp8_overfetch = 0 if a.overfetch_fp8 is None else a.overfetch_fp8
+        opts = scan.options(overfetch=fp8_overfetch, boundary_fp64=1)
+        tuned_knobs = scan.tune_lookup("fp8", "l2", a.dim, a.n, a.batch, a.k)
         step = lambda i, qq=None: scan.fp8_search(table, qb[i % 2] if qq is None else qq, a.k, "l2",  # noqa: E731
                                                    opts=opts, out=out)
         for i in range(max(3, a.warmup)):
@@ -590,8 +594,10 @@ def run_workload(a, world, rank, local):
             cdt = time.perf_counter() - t0
             cpu = {"value": threads / cdt, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"{threads} queries, exact fp32 search of the full base, {cdt:.1f} s"}
-        cfg = {"workload": "fp8 e4m3 flat L2 scan (per-row scales) + fp32 rescore (4k over-fetch) + fp64 boundary",
-               "N": a.n, "dim": a.dim, "batch": a.batch, "k": a.k, "overfetch": a.overfetch,
+        eff_overfetch = fp8_overfetch or (tuned_knobs or {}).get("overfetch") or 4
+        cfg = {"workload": "fp8 e4m3 flat L2 scan (per-row scales) + fp32 rescore (autotuned over-fetch) + fp64 "
+                           "boundary", "N": a.n, "dim": a.dim, "batch": a.batch, "k": a.k, "overfetch": eff_overfetch,
+               "autotuned": tuned_knobs,
                "mixture": "16384 comps, N(0,1) means, sigma 0.5",
                "l2": "inputs larger than L2 (0.96 GB fp8 base streamed per step)"}
         _line(a, world, qps, UNIT, dev_s,

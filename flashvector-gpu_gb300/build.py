@@ -25,7 +25,7 @@ LIB = PKG / "fvgb300" / "libfvgb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "-Xptxas", "-warn-spills", f"-I{ROOT / 'include'}"]
+              "-Xptxas", "-warn-spills", f"-I{ROOT / 'include'}", f"-I{PKG / '_build'}"]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", f"-I{ROOT / 'include'}", "-I/usr/local/cuda/include"]
 
 
@@ -36,8 +36,31 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
+TUNING = PKG / "tuning" / "gb300.json"
+TUNE_INC = OBJ / "tuning_table.inc"
+METRICS = {"l2": 0, "cosine": 1, "ip": 2}
+
+
+def _tuning_table() -> None:
+    """tuning/gb300.json (committed autotuner results) -> _build/tuning_table.inc,
+    one TuneEntry initialiser per entry (see csrc/tc_scan.cu)."""
+    import json
+
+    lines = []
+    if TUNING.exists():
+        for e in json.loads(TUNING.read_text()).get("entries", []):
+            k = e["knobs"]
+            lines.append("    {%d, %d, %du, %du, %dull, %dull, %du, %du, %du, %du, %d, %d, %d, %d},"
+                         % (1 if e["precision"] == "fp8" else 0, METRICS[e["metric"]], e["dim"][0], e["dim"][1],
+                            e["n"][0], e["n"][1], e["nq"][0], e["nq"][1], e["k"][0], e["k"][1], k.get("pair", -1),
+                            k.get("prepass", -1), k.get("stride", 0), k.get("overfetch", 0)))
+    text = "// generated by build.py from tuning/gb300.json\n" + "\n".join(lines) + ("\n" if lines else "")
+    if not TUNE_INC.exists() or TUNE_INC.read_text() != text:
+        TUNE_INC.write_text(text)
+
+
 def _headers() -> list[Path]:
-    return list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
+    return list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h")) + [TUNE_INC]
 
 
 def _stale(src: Path, obj: Path, newest_header: float) -> bool:
@@ -49,6 +72,7 @@ def _stale(src: Path, obj: Path, newest_header: float) -> bool:
 
 def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -> Path:
     OBJ.mkdir(exist_ok=True)
+    _tuning_table()
     nvcc = _nvcc()
     newest = max((h.stat().st_mtime for h in _headers()), default=0.0)
     cmds = []

@@ -27,7 +27,8 @@ struct Knob {
   const char* key;
   std::atomic<int64_t> value;
 };
-Knob g_knobs[] = {{"tc.prepass", {-1}}, {"tc.prepass_stride", {32}}, {"tc.prepass_margin", {0}}, {"tc.pair", {-1}}};
+Knob g_knobs[] = {{"tc.prepass", {-1}}, {"tc.prepass_stride", {0}}, {"tc.prepass_margin", {0}}, {"tc.pair", {-1}},
+                  {"tc.table", {1}}};
 }  // namespace
 
 bool tune_set(const char* key, int64_t value) {

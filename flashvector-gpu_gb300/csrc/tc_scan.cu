@@ -261,6 +261,35 @@ bool encode_tmap(CUtensorMap* m, const void* ptr, bool fp8, uint64_t inner_elems
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// ---------------------------------------------------------------------------
+// Committed autotuner results (flashvector-gpu_gb300/tuning/gb300.json,
+// compiled in by build.py as tuning_table.inc): per shape range, the CTA-pair
+// choice, the pre-pass choice and stride, and the over-fetch that reached
+// recall@10 >= 0.99 fastest on this GPU. Explicit knobs (fv_tune_set) and
+// explicit scan options take precedence; "tc.table" = 0 ignores the table.
+// ---------------------------------------------------------------------------
+struct TuneEntry {
+  int fp8, metric;
+  uint32_t dim_lo, dim_hi;
+  uint64_t n_lo, n_hi;
+  uint32_t nq_lo, nq_hi, k_lo, k_hi;
+  int pair, prepass, stride, overfetch;
+};
+const TuneEntry kTuneTable[] = {
+#include "tuning_table.inc"
+    {-1, -1, 0, 0, 0, 0, 0, 0, 0, 0, -1, -1, 0, 0}};
+
+const TuneEntry* tune_lookup(bool fp8, int metric, uint32_t dim, uint64_t n, uint32_t nq, uint32_t k) {
+  if (tune_value("tc.table", 1) == 0) return nullptr;
+  for (const TuneEntry& e : kTuneTable) {
+    if (e.fp8 < 0) break;
+    if (e.fp8 == (fp8 ? 1 : 0) && e.metric == metric && dim >= e.dim_lo && dim <= e.dim_hi && n >= e.n_lo &&
+        n <= e.n_hi && nq >= e.nq_lo && nq <= e.nq_hi && k >= e.k_lo && k <= e.k_hi)
+      return &e;
+  }
+  return nullptr;
+}
+
 // Sampled rank for the pre-pass bound. A sample of every stride-th tile
 // holds each of a query's top (shortlist - 1) rows with probability
 // 1 / stride, so the number of them in the sample is about Poisson(lambda =
@@ -311,7 +340,8 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   const uint32_t elem = fp8 ? 1 : 2;
   const uint32_t kb_elems = fp8 ? 128 : 64;
   const uint32_t kblocks = (t.padded_dim + kb_elems - 1) / kb_elems;
-  const uint32_t overfetch = opt.overfetch ? opt.overfetch : 4;
+  const TuneEntry* te = tune_lookup(fp8, (int)metric, t.dim, t.n, nq, k);
+  const uint32_t overfetch = opt.overfetch ? opt.overfetch : (te && te->overfetch > 0 ? (uint32_t)te->overfetch : 4u);
   const uint32_t shortlist = t.vectors ? std::min<uint32_t>(std::max(k, overfetch * k), 4096u) : k;
   // short K (at most two 64-element fp16 / 128-element fp8 blocks per tile):
   // a tile costs the MMA little and the epilogue much, so two epilogue
@@ -325,7 +355,8 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   const int sms = device_sm_count();
   // CTA pairs (cta_group::2) for long rows: two query blocks share each
   // base tile, each SM streaming half of it
-  const int64_t pair_knob = tune_value("tc.pair", -1);
+  int64_t pair_knob = tune_value("tc.pair", -1);
+  if (pair_knob < 0 && te && te->pair >= 0) pair_knob = te->pair;
   const bool pair = groups == 1 && pair_knob != 0;
   const uint32_t nqb_grid = pair ? 2 * ((nqb + 1) / 2) : nqb;  // CTAs per split
   uint32_t splits = opt.splits ? opt.splits : std::max<uint32_t>(1u, (uint32_t)sms / nqb_grid);
@@ -351,8 +382,11 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   // unlucky (probability < 1e-7 per query); the full scan then admits only
   // rows within it. Queries whose bounded scan comes up short are scanned
   // again without the bound (device-side, no host round trip).
-  const int64_t pp_knob = tune_value("tc.prepass", -1);
-  const uint32_t pstride = (uint32_t)std::max<int64_t>(2, tune_value("tc.prepass_stride", 32));
+  int64_t pp_knob = tune_value("tc.prepass", -1);
+  if (pp_knob < 0 && te && te->prepass >= 0) pp_knob = te->prepass;
+  int64_t stride_knob = tune_value("tc.prepass_stride", 0);
+  if (stride_knob <= 0) stride_knob = (te && te->stride > 0) ? te->stride : 32;
+  const uint32_t pstride = (uint32_t)std::max<int64_t>(2, stride_knob);
   const int64_t pmargin = tune_value("tc.prepass_margin", 0);
   const uint32_t pr = std::max<uint32_t>(
       1u, std::min<uint32_t>(kl_cap, pmargin > 0 ? (uint32_t)((pmargin * shortlist + pstride - 1) / pstride)
@@ -501,3 +535,16 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
 }
 
 }  // namespace fv
+
+extern "C" int fv_tune_lookup(int fp8, MetricType metric, uint32_t dim, uint64_t num_vectors, uint32_t num_queries,
+                              uint32_t top_k, int32_t* out_knobs) {
+  if (!out_knobs) return FV_ERR_NULL;
+  const fv::TuneEntry* e = fv::tune_lookup(fp8 != 0, (int)metric, dim, num_vectors, num_queries, top_k);
+  if (!e) return FV_ERR_ARG;
+  out_knobs[0] = e->pair;
+  out_knobs[1] = e->prepass;
+  out_knobs[2] = e->stride;
+  out_knobs[3] = e->overfetch;
+  return 0;
+}
+

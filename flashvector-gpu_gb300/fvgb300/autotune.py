@@ -1,0 +1,175 @@
+"""Autotuner of the tensor-core scans; its results are committed to
+flashvector-gpu_gb300/tuning/gb300.json and compiled into libfvgb300 by
+build.py, where launch_tc_scan consults them for calls of a matching shape.
+
+For each benchmark shape it sweeps
+  * tc.pair          one-SM CTAs or cta_group::2 pairs (long rows only),
+  * tc.prepass       sampled pre-pass bound on / off, and its stride,
+  * over-fetch       the fp32-rescored shortlist = over-fetch x k,
+times each configuration (CUDA events around the whole search call, median
+of several runs, after warm-up) and measures recall@10 and recall@k against
+an fp64 exact search on a query subsample. The chosen configuration is the
+fastest whose recall@10 and recall@k are both >= the target (0.99); the
+pair / pre-pass / stride knobs never change the answer (the tests check
+this), the over-fetch can.
+
+    python -m fvgb300.autotune [--shapes all|fp16|fp8] [--out tuning/gb300.json]
+
+Data: the seeded synthetic mixtures of the benchmark configurations
+(fvgb300.datasets), queries fresh draws from the same mixture.
+"""
+from __future__ import annotations
+
+import argparse
+import dataclasses
+import json
+import statistics
+import time
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parents[1]
+DEFAULT_OUT = PKG / "tuning" / "gb300.json"
+
+# precision, metric, N, dim, queries, k, mixture name, mask fraction (0 = no
+# mask), over-fetch values to try: the fp16 inner-product configuration fixes
+# a 4k over-fetch, the fp8 one tunes it
+SHAPES = {
+    "fp16_ip_1M_q1024_k10": ("fp16", "ip", 1_000_000, 768, 1024, 10, "FP16_IP_UNIT", 0.5, (4,)),
+    "fp16_ip_1M_q1024_k100": ("fp16", "ip", 1_000_000, 768, 1024, 100, "FP16_IP_UNIT", 0.5, (4,)),
+    "fp16_ip_1M_q64_k10": ("fp16", "ip", 1_000_000, 768, 64, 10, "FP16_IP_UNIT", 0.5, (4,)),
+    "fp16_ip_1M_q1_k10": ("fp16", "ip", 1_000_000, 768, 1, 10, "FP16_IP_UNIT", 0.5, (4,)),
+    "fp8_l2_10M_q10000_k100": ("fp8", "l2", 10_000_000, 96, 10_000, 100, "FP8_L2", 0.0, (4, 3, 2)),
+}
+
+
+def _ranges(n, dim, nq, k):
+    """The shape range an entry applies to: dimension within 1.5x, base size
+    within 4x, batch within 2x (batches of 1-16 queries form one range),
+    k within 2x."""
+    nq_range = [1, 16] if nq <= 16 else [nq // 2, nq * 2]
+    return {"dim": [max(1, int(dim / 1.5)), int(dim * 1.5)], "n": [max(1, n // 4), n * 4],
+            "nq": nq_range, "k": [max(1, k // 2), min(256, k * 2)]}
+
+
+def _candidates(precision, dim, overfetches):
+    long_rows = (dim + (127 if precision == "fp8" else 63)) // (128 if precision == "fp8" else 64) > 2
+    pairs = [1, 0] if long_rows else [0]
+    prepasses = [(0, 0), (1, 16), (1, 32), (1, 64)]
+    for overfetch in overfetches:
+        for pair in pairs:
+            for prepass, stride in prepasses:
+                yield {"pair": pair, "prepass": prepass, "stride": stride, "overfetch": overfetch}
+
+
+def tune_shape(name, spec, runs=5, nsub=100, target=0.99, log=print):
+    import torch
+
+    from . import datasets, scan
+
+    precision, metric, n, dim, nq, k, mix_name, mask_frac, overfetches = spec
+    dev = torch.device("cuda", 0)
+    mix = dataclasses.replace(getattr(datasets, mix_name), dim=dim)
+    base = datasets.sample_torch(mix, n, seed=11, stream=0, device=dev)
+    queries = datasets.sample_torch(mix, nq, seed=11, stream=1, device=dev).contiguous()
+    table = (scan.Fp8Table if precision == "fp8" else scan.Fp16Table)(base)
+    search = scan.fp8_search if precision == "fp8" else scan.fp16_search
+    mask = allowed = None
+    if mask_frac > 0:
+        words = datasets.bernoulli_mask_words(n, mask_frac, seed=1)
+        mask = torch.from_numpy(words.view(np.int32)).to(dev)
+        allowed = torch.from_numpy(datasets.unpack_words(words, n)).to(dev)
+    truth = _fp64_topk(base, queries[:nsub], k, metric, allowed)
+    out = scan.empty_results(nq, k, dev)
+    stream = torch.cuda.current_stream()
+    results = []
+    for cand in _candidates(precision, dim, overfetches):
+        knobs = {"tc_table": 0, "tc_pair": cand["pair"], "tc_prepass": cand["prepass"],
+                 "tc_prepass_stride": cand["stride"] or 32}
+        opts = scan.options(overfetch=cand["overfetch"], boundary_fp64=1)
+        with scan.tuned(**knobs):
+            for _ in range(2):
+                search(table, queries, k, metric, mask=mask, opts=opts, out=out)
+            torch.cuda.synchronize()
+            times = []
+            for _ in range(runs):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                search(table, queries, k, metric, mask=mask, opts=opts, out=out)
+                e1.record(stream)
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1))
+        res = out.cpu().numpy()
+        ids = res[..., 0].view(np.uint32)
+        r10 = _recall(ids[:nsub, :10], truth[:, :10])
+        rk = _recall(ids[:nsub], truth)
+        ms = statistics.median(times)
+        results.append({**cand, "ms": ms, "qps": nq / (ms / 1e3), "recall_at_10": r10, "recall_at_k": rk})
+        log(f"{name} {cand} {ms:.3f} ms recall@10 {r10:.4f} recall@{k} {rk:.4f}")
+    ok = [r for r in results if r["recall_at_10"] >= target and r["recall_at_k"] >= target]
+    best = min(ok or results, key=lambda r: r["ms"])
+    default = next(r for r in results if r["overfetch"] == 4 and r["prepass"] == 0 and r["pair"] == 0)
+    return {"name": name, "precision": precision, "metric": metric, **_ranges(n, dim, nq, k),
+            "shape": {"n": n, "dim": dim, "nq": nq, "k": k, "mask_fraction": mask_frac},
+            "knobs": {"pair": best["pair"], "prepass": best["prepass"], "stride": best["stride"],
+                      "overfetch": best["overfetch"]},
+            "measured": {"ms": best["ms"], "qps": best["qps"], "recall_at_10": best["recall_at_10"],
+                         "recall_at_k": best["recall_at_k"], "untuned_ms": default["ms"],
+                         "recall_target": target, "candidates": len(results)}}
+
+
+def _fp64_topk(base, queries, k, metric, allowed, chunk=500_000):
+    import torch
+
+    q64 = queries.double()
+    best_d = best_i = None
+    for c in range(0, base.shape[0], chunk):
+        x = base[c:c + chunk].double()
+        if metric == "l2":
+            d = (q64 * q64).sum(1, keepdim=True) + (x * x).sum(1)[None, :] - 2.0 * (q64 @ x.T)
+        else:
+            d = -(q64 @ x.T)
+        if allowed is not None:
+            d = d.masked_fill(~allowed[None, c:c + chunk], float("inf"))
+        tv, ti = torch.topk(d, min(k, d.shape[1]), dim=1, largest=False)
+        ti = ti + c
+        if best_d is None:
+            best_d, best_i = tv, ti
+        else:
+            best_d, o = torch.topk(torch.cat([best_d, tv], 1), k, dim=1, largest=False)
+            best_i = torch.cat([best_i, ti], 1).gather(1, o)
+    return best_i.cpu().numpy()
+
+
+def _recall(ids, truth):
+    k = truth.shape[1]
+    return float(sum(len(set(ids[i, :k].tolist()) & set(truth[i].tolist())) for i in range(truth.shape[0]))
+                 / (truth.shape[0] * k))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--shapes", default="all", help="all, fp16, fp8 or a comma-separated list of shape names")
+    ap.add_argument("--out", default=str(DEFAULT_OUT))
+    ap.add_argument("--runs", type=int, default=5)
+    a = ap.parse_args(argv)
+    import torch
+
+    names = list(SHAPES) if a.shapes == "all" else [s for s in SHAPES if s.startswith(a.shapes)] \
+        if a.shapes in ("fp16", "fp8") else a.shapes.split(",")
+    entries = [tune_shape(nm, SHAPES[nm], runs=a.runs) for nm in names]
+    out = Path(a.out)
+    prev = json.loads(out.read_text()) if out.exists() else {"entries": []}
+    keep = [e for e in prev.get("entries", []) if e.get("name") not in {x["name"] for x in entries}]
+    doc = {"device": torch.cuda.get_device_name(0), "date": time.strftime("%Y-%m-%d"),
+           "method": "fastest configuration with recall@10 and recall@k >= target vs fp64 exact search "
+                     "(median of CUDA-event times around the whole search call)",
+           "entries": keep + entries}
+    out.parent.mkdir(parents=True, exist_ok=True)
+    out.write_text(json.dumps(doc, indent=1) + "\n")
+    print(f"wrote {len(doc['entries'])} entries to {out}")
+
+
+if __name__ == "__main__":
+    main()

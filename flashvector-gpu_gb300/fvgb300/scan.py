@@ -168,6 +168,15 @@ def tune_get(key: str) -> int:
     return v.value
 
 
+def tune_lookup(precision: str, metric: str, dim: int, n: int, nq: int, k: int):
+    """The committed autotuner knobs the library applies to this shape, or None."""
+    out = (C.c_int32 * 4)()
+    code = _lib.lib().fv_tune_lookup(1 if precision == "fp8" else 0, _metric(metric), dim, n, nq, k, out)
+    if code != 0:
+        return None
+    return {"pair": out[0], "prepass": out[1], "stride": out[2], "overfetch": out[3]}
+
+
 class tuned:
     """Context manager that sets knobs and restores them on exit."""
 

@@ -267,7 +267,8 @@ int fv_profile_summary(char* buf, size_t len);
  *                       tensor-core scans whose shortlist exceeds the 64-entry
  *                       per-range heap first scan a strided sample of the
  *                       base for a per-query admission bound
- *   "tc.prepass_stride" sample stride in 256-row tiles (default 32)
+ *   "tc.prepass_stride" sample stride in 256-row tiles (0 automatic: the
+ *                       tuned value, else 32)
  *   "tc.prepass_margin" 0 (default): the sampled rank r is the smallest
  *                       with P(Poisson(shortlist / stride) >= r) < 1e-7;
  *                       m > 0: r = ceil(m * shortlist / stride)
@@ -275,10 +276,18 @@ int fv_profile_summary(char* buf, size_t len);
  *                       of long rows (more than two K blocks) run on CTA
  *                       pairs (cta_group::2), each SM streaming half of
  *                       every base tile
+ *   "tc.table"          1 (default): knobs left automatic and a zero
+ *                       over-fetch take the committed autotuner results
+ *                       for the call's shape (tuning/gb300.json); 0: ignore
  * Unknown keys return FV_ERR_ARG. Values apply to launches issued after the
  * call. */
 int fv_tune_set(const char* key, int64_t value);
 int fv_tune_get(const char* key, int64_t* value);
+/* The committed autotuner entry a tensor-core scan of this shape uses
+ * (fp8: 0 fp16 rows, 1 e4m3 rows): out_knobs[4] = {pair, prepass, stride,
+ * overfetch}. FV_ERR_ARG when no entry applies (or "tc.table" is 0). */
+int fv_tune_lookup(int fp8, MetricType metric, uint32_t dim, uint64_t num_vectors, uint32_t num_queries,
+                   uint32_t top_k, int32_t* out_knobs);
 /* Installs a caller-owned device buffer as the scratch arena of `stream`
  * (kernels that need scratch then never allocate on that stream; a call
  * needing more than `bytes` fails with cudaErrorMemoryAllocation).

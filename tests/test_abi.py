@@ -60,8 +60,32 @@ def test_tune_knobs_roundtrip(built_lib):
     from fvgb300._lib import FvError
 
     assert scan.tune_get("tc.prepass") == -1
+    assert scan.tune_get("tc.table") == 1
     with scan.tuned(tc_prepass_stride=16):
         assert scan.tune_get("tc.prepass_stride") == 16
-    assert scan.tune_get("tc.prepass_stride") == 32
+    assert scan.tune_get("tc.prepass_stride") == 0
     with pytest.raises(FvError):
         scan.tune_set("no.such.knob", 1)
+
+
+def test_committed_tuning_table_is_compiled_in(built_lib):
+    """Every entry of tuning/gb300.json is what the library applies to its
+    own shape (the table build.py compiles in), and nothing applies to a
+    shape outside every range."""
+    import json
+
+    from conftest import ROOT
+    from fvgb300 import scan
+
+    doc = json.loads((ROOT / "flashvector-gpu_gb300" / "tuning" / "gb300.json").read_text())
+    assert doc["entries"]
+    for e in doc["entries"]:
+        sh = e["shape"]
+        got = scan.tune_lookup(e["precision"], e["metric"], sh["dim"], sh["n"], sh["nq"], sh["k"])
+        assert got == {k: e["knobs"][k] for k in ("pair", "prepass", "stride", "overfetch")}, e["name"]
+        assert e["measured"]["recall_at_10"] >= e["measured"]["recall_target"]
+    assert scan.tune_lookup("fp16", "cosine", 7, 100, 3, 5) is None
+    with scan.tuned(tc_table=0):
+        sh = doc["entries"][0]["shape"]
+        assert scan.tune_lookup(doc["entries"][0]["precision"], doc["entries"][0]["metric"], sh["dim"], sh["n"],
+                                sh["nq"], sh["k"]) is None
