@@ -40,8 +40,7 @@ namespace fv {
 namespace {
 
 constexpr int IVF_THREADS = 256;
-constexpr int IVF_ROWS = 4;                // postings per thread per round (loads issued together)
-constexpr uint32_t IVF_BUF = 2 * IVF_THREADS * IVF_ROWS;  // candidate buffer entries
+constexpr uint32_t IVF_BUF = 1536;         // candidate buffer entries (>= 1.5 rounds of 1,024 postings)
 constexpr uint32_t MAX_SHORTLIST = 10240;  // reference clamp (ivf_rerank.cuh:12)
 
 enum IvfMode { IVF_PQ = 0, IVF_SQ8 = 1 };
@@ -160,8 +159,9 @@ __device__ __forceinline__ float sq8_row(const float* __restrict__ qres, const f
 }
 
 // MODE: PQ or SQ8. MW > 0: PQ codes of 16 * MW bytes at 16-byte-aligned
-// rows (m_pq = 16, 32, 64), scanned by the register-prefetching loop.
-template <int MODE, int MW>
+// rows (m_pq = 16, 32, 64), scanned by the register-prefetching loop with R
+// postings per thread per round, software-pipelined across rounds (PIPE).
+template <int MODE, int MW, int R = 4, bool PIPE = false>
 __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   uint64_t* keys = reinterpret_cast<uint64_t*>(smem);
@@ -271,32 +271,67 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
         }
       };
       if (MODE == IVF_PQ && MW > 0) {
-        // IVF_ROWS postings per thread per round: ids and code rows of all of
-        // them are loaded before any is scored, so a warp keeps several
-        // 16-byte loads in flight per lane
-        for (uint32_t base = beg; base < end; base += IVF_THREADS * IVF_ROWS) {
-          uint32_t vid[IVF_ROWS];
-          uint4 w[IVF_ROWS][MW > 0 ? MW : 1];
+        // R postings per thread per round: ids and code rows of all of them
+        // are loaded before any is scored. PIPE: the next round's loads are
+        // issued before this round is scored, and its mask / filter words
+        // after, so global-load latency overlaps the LUT arithmetic.
+        constexpr int MWW = MW > 0 ? MW : 1;
+        constexpr uint32_t step = IVF_THREADS * R;
+        auto issue = [&](uint32_t b0, uint32_t (&v)[R], uint4 (&c)[R][MWW]) {
 #pragma unroll
-          for (int r = 0; r < IVF_ROWS; ++r) {
-            const uint32_t i = base + r * IVF_THREADS + tid;
-            vid[r] = i < end ? __ldg(a.vec_ids + i) : 0xFFFFFFFFu;
+          for (int r = 0; r < R; ++r) {
+            const uint32_t i = b0 + r * IVF_THREADS + tid;
+            v[r] = i < end ? __ldg(a.vec_ids + i) : 0xFFFFFFFFu;
           }
 #pragma unroll
-          for (int r = 0; r < IVF_ROWS; ++r) {
-            const uint32_t i = base + r * IVF_THREADS + tid;
-            const uint4* row = reinterpret_cast<const uint4*>(a.codes + (size_t)(a.list_major ? i : vid[r]) * (16u * MW));
+          for (int r = 0; r < R; ++r) {
+            const uint32_t i = b0 + r * IVF_THREADS + tid;
+            const uint4* row = reinterpret_cast<const uint4*>(a.codes + (size_t)(a.list_major ? i : v[r]) * (16u * MW));
 #pragma unroll
-            for (int j = 0; j < (MW > 0 ? MW : 1); ++j)
-              w[r][j] = i < end ? __ldg(row + j) : make_uint4(0u, 0u, 0u, 0u);
+            for (int j = 0; j < MWW; ++j) c[r][j] = i < end ? __ldg(row + j) : make_uint4(0u, 0u, 0u, 0u);
           }
+        };
+        auto admit = [&](const uint32_t (&v)[R], bool (&o)[R]) {
 #pragma unroll
-          for (int r = 0; r < IVF_ROWS; ++r) {
-            if (vid[r] != 0xFFFFFFFFu && mask_allows(a.mask, vid[r]) && filter_allows(qf, vid[r]))
-              offer(adc_words<(MW > 0 ? MW : 1)>(tab, w[r]), vid[r]);
+          for (int r = 0; r < R; ++r)
+            o[r] = v[r] != 0xFFFFFFFFu && mask_allows(a.mask, v[r]) && filter_allows(qf, v[r]);
+        };
+        uint32_t vid[R];
+        uint4 w[R][MWW];
+        bool ok[R];
+        if (PIPE && beg < end) {
+          issue(beg, vid, w);
+          admit(vid, ok);
+        }
+        for (uint32_t base = beg; base < end; base += step) {
+          if (PIPE) {
+            uint32_t vn[R];
+            uint4 wn[R][MWW];
+            bool okn[R];
+            const bool more = base + step < end;  // uniform over the block
+            if (more) issue(base + step, vn, wn);
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+              if (ok[r]) offer(adc_words<MWW>(tab, w[r]), vid[r]);
+            if (more) {
+              admit(vn, okn);
+#pragma unroll
+              for (int r = 0; r < R; ++r) {
+                vid[r] = vn[r];
+                ok[r] = okn[r];
+#pragma unroll
+                for (int j = 0; j < MWW; ++j) w[r][j] = wn[r][j];
+              }
+            }
+          } else {
+            issue(base, vid, w);
+            admit(vid, ok);
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+              if (ok[r]) offer(adc_words<MWW>(tab, w[r]), vid[r]);
           }
           __syncthreads();
-          if (s_cnt > IVF_BUF - IVF_THREADS * IVF_ROWS) flush();
+          if (s_cnt > IVF_BUF - step) flush();
         }
       } else {
         for (uint32_t base = beg; base < end; base += IVF_THREADS) {
@@ -412,12 +447,17 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   const size_t smem = IvfSmem::bytes(mode, a.keys_pow2, L.dim, L.m_pq);
   if (smem > 227 * 1024) return FV_ERR_ARG;
   const bool rows16 = mode == IVF_PQ && ((uintptr_t)L.codes % 16u) == 0;
+  // "ivf.pipeline": 1 software-pipelines the PQ list scan (2 postings per
+  // thread per round, next round's loads in flight while scoring). Off by
+  // default: its 78 registers allow 3 CTAs per SM where the plain loop
+  // (60 registers, 4 postings per round) runs 4, which measured 7% faster.
+  const bool pipe = tune_value("ivf.pipeline", 0) != 0;
   auto kern = ivf_scan_kernel<IVF_SQ8, 0>;
   if (mode == IVF_PQ) {
     kern = ivf_scan_kernel<IVF_PQ, 0>;
-    if (rows16 && L.m_pq == 16) kern = ivf_scan_kernel<IVF_PQ, 1>;
-    if (rows16 && L.m_pq == 32) kern = ivf_scan_kernel<IVF_PQ, 2>;
-    if (rows16 && L.m_pq == 64) kern = ivf_scan_kernel<IVF_PQ, 4>;
+    if (rows16 && L.m_pq == 16) kern = pipe ? ivf_scan_kernel<IVF_PQ, 1, 2, true> : ivf_scan_kernel<IVF_PQ, 1>;
+    if (rows16 && L.m_pq == 32) kern = pipe ? ivf_scan_kernel<IVF_PQ, 2, 2, true> : ivf_scan_kernel<IVF_PQ, 2>;
+    if (rows16 && L.m_pq == 64) kern = pipe ? ivf_scan_kernel<IVF_PQ, 4, 2, true> : ivf_scan_kernel<IVF_PQ, 4>;
   }
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;

@@ -279,6 +279,9 @@ int fv_profile_summary(char* buf, size_t len);
  *   "tc.table"          1 (default): knobs left automatic and a zero
  *                       over-fetch take the committed autotuner results
  *                       for the call's shape (tuning/gb300.json); 0: ignore
+ *   "ivf.pipeline"      0 (default): the IVF-PQ list scan loads and scores
+ *                       4 postings per thread per round; 1: 2 per round
+ *                       with the next round's loads in flight
  * Unknown keys return FV_ERR_ARG. Values apply to launches issued after the
  * call. */
 int fv_tune_set(const char* key, int64_t value);
