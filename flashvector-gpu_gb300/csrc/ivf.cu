@@ -68,7 +68,34 @@ struct IvfArgs {
   GpuSearchResult* out;
   uint32_t* status;
   uint32_t keys_pow2;             // pow2(largest shortlist + IVF_BUF)
+  uint32_t items_per_q;           // G: a query's probed postings are cut into G ranges
+  uint64_t* partial;              // G > 1: [nq * G][part_stride] sorted shortlists of the ranges
+  uint32_t part_stride;           // >= every query's shortlist
 };
+
+// Rerank of a query's shortlist keys[0, S) (sorted, sentinels last) with the
+// reference's warp-order fp32 distance, sort, and the query's top k into
+// out[q][0, top_k) (sentinels past k). Block-collective.
+__device__ void ivf_finish_query(const IvfArgs& a, uint64_t* keys, uint32_t q, uint32_t S, uint32_t kq,
+                                 bool do_rerank, const float* qv) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (do_rerank) {
+    for (uint32_t c = warp; c < S; c += IVF_THREADS / 32) {
+      const uint64_t key = keys[c];
+      if (key == kSentinelKey) continue;
+      const uint32_t vid = key_slot(key);
+      if (vid >= a.num_vectors) continue;
+      const float d = warp_metric_distance(qv, a.vectors + (size_t)vid * a.dim, a.dim, lane, (MetricType)a.metric);
+      if (lane == 0) keys[c] = make_key(d, vid);
+    }
+    const uint32_t p2 = next_pow2_dev(S);
+    for (uint32_t i = S + tid; i < p2; i += IVF_THREADS) keys[i] = kSentinelKey;
+    __syncthreads();
+    block_bitonic_sort(keys, p2);
+  }
+  for (uint32_t r = tid; r < a.top_k; r += IVF_THREADS)
+    a.out[(size_t)q * a.top_k + r] = key_to_result(r < S && r < kq ? keys[r] : kSentinelKey, nullptr);
+}
 
 // The reference's clamps (ivf_pq_lookup.cu:351-362) for one query: returns
 // the shortlist length; top_k and nprobe are clamped in place.
@@ -184,12 +211,15 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
     }
   }
 
+  __shared__ unsigned long long s_total;
+  const uint32_t G = a.items_per_q;
   while (true) {
     __syncthreads();
     if (tid == 0) s_q = atomicAdd(a.work, 1u);
     __syncthreads();
-    const uint32_t q = s_q;
-    if (q >= a.nq) break;
+    const uint32_t item = s_q;
+    if (item >= a.nq * G) break;
+    const uint32_t q = item / G, g = item % G;
     uint32_t kq = a.q_topk ? __ldg(a.q_topk + q) : a.top_k;
     uint32_t npq = a.q_nprobe ? __ldg(a.q_nprobe + q) : a.nprobe;
     const uint32_t rrq = a.q_rerank ? __ldg(a.q_rerank + q) : a.rerank_k;
@@ -205,8 +235,19 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
     if (tid == 0) {
       s_cnt = 0;
       s_tau = kSentinelKey;
+      unsigned long long total = 0;
+      if (G > 1)
+        for (uint32_t p = 0; p < npq; ++p) {
+          const uint32_t l = a.probes[(size_t)q * a.nprobe + p].id;
+          if (l < a.nlist) total += __ldg(a.offsets + l + 1) - __ldg(a.offsets + l);
+        }
+      s_total = total;
     }
     __syncthreads();
+    // this item's range of the query's probed postings (lists in probe order)
+    const uint64_t lo = G > 1 ? s_total * g / G : 0ull;
+    const uint64_t hi = G > 1 ? s_total * (g + 1) / G : ~0ull;
+    uint64_t cum = 0;
 
     auto flush = [&]() {
       // keys[0, S) sorted shortlist, keys[S, S + cnt) new candidates
@@ -226,6 +267,11 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
     for (uint32_t p = 0; p < npq; ++p) {
       const uint32_t l = a.probes[(size_t)q * a.nprobe + p].id;
       if (l >= a.nlist) continue;  // uniform over the block
+      const uint32_t lbeg = __ldg(a.offsets + l), llen = __ldg(a.offsets + l + 1) - lbeg;
+      const uint64_t s0 = max(lo, cum), s1 = min(hi, cum + llen);
+      const uint64_t at = cum;
+      cum += llen;
+      if (s0 >= s1) continue;  // uniform: the list lies outside this item's range
       const float* cent = a.centroids + (size_t)l * a.dim;
       if (MODE == IVF_PQ) {
         // LUT[m][c] = sum_sd ((q - centroid) - codeword)^2 with fmaf in
@@ -260,7 +306,7 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
       }
       __syncthreads();
 
-      const uint32_t beg = __ldg(a.offsets + l), end = __ldg(a.offsets + l + 1);
+      const uint32_t beg = lbeg + (uint32_t)(s0 - at), end = lbeg + (uint32_t)(s1 - at);
       auto offer = [&](float d, uint32_t vid) {
         if (d < kSentinelDist) {
           const uint64_t key = make_key(d, vid);
@@ -351,24 +397,38 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
       __syncthreads();  // the table is rebuilt for the next list
     }
     flush();
-
-    if (do_rerank) {
-      for (uint32_t c = warp; c < S; c += IVF_THREADS / 32) {
-        const uint64_t key = keys[c];
-        if (key == kSentinelKey) continue;
-        const uint32_t vid = key_slot(key);
-        if (vid >= a.num_vectors) continue;
-        const float d = warp_metric_distance(qv, a.vectors + (size_t)vid * a.dim, a.dim, lane, (MetricType)a.metric);
-        if (lane == 0) keys[c] = make_key(d, vid);
-      }
-      const uint32_t p2 = next_pow2_dev(S);
-      for (uint32_t i = S + tid; i < p2; i += IVF_THREADS) keys[i] = kSentinelKey;
-      __syncthreads();
-      block_bitonic_sort(keys, p2);
+    if (G > 1) {
+      // a range's shortlist goes to the merge kernel
+      uint64_t* dst = a.partial + (size_t)item * a.part_stride;
+      for (uint32_t i = tid; i < S; i += IVF_THREADS) dst[i] = keys[i];
+      continue;
     }
-    for (uint32_t r = tid; r < a.top_k; r += IVF_THREADS)
-      a.out[(size_t)q * a.top_k + r] = key_to_result(r < S && r < kq ? keys[r] : kSentinelKey, nullptr);
+    ivf_finish_query(a, keys, q, S, kq, do_rerank, qv);
   }
+}
+
+// G > 1: one CTA per query merges the G range shortlists (top S of their
+// union, by key), reranks and writes the top k -- the same answer as one
+// range holding every posting.
+__global__ void __launch_bounds__(IVF_THREADS) ivf_merge_kernel(IvfArgs a) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  uint64_t* keys = reinterpret_cast<uint64_t*>(smem);
+  const uint32_t q = blockIdx.x, G = a.items_per_q;
+  uint32_t kq = a.q_topk ? __ldg(a.q_topk + q) : a.top_k;
+  uint32_t npq = a.q_nprobe ? __ldg(a.q_nprobe + q) : a.nprobe;
+  const uint32_t rrq = a.q_rerank ? __ldg(a.q_rerank + q) : a.rerank_k;
+  const uint32_t S = ivf_clamps(kq, npq, rrq, a.nlist);
+  kq = min(kq, a.top_k);
+  const bool do_rerank = rrq != 1u && a.vectors != nullptr;
+  const uint32_t total = G * S, p2 = next_pow2_dev(total);
+  for (uint32_t i = threadIdx.x; i < p2; i += IVF_THREADS) {
+    uint64_t v = kSentinelKey;
+    if (i < total) v = a.partial[((size_t)q * G + i / S) * a.part_stride + i % S];
+    keys[i] = v;
+  }
+  __syncthreads();
+  block_bitonic_sort(keys, p2);
+  ivf_finish_query(a, keys, q, S, kq, do_rerank, a.queries + (size_t)q * a.dim);
 }
 
 __global__ void relayout_codes_kernel(const uint8_t* __restrict__ by_id, const uint32_t* __restrict__ vec_ids,
@@ -396,14 +456,29 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   if (nprobe > (uint32_t)kMaxTopK) return FV_ERR_ARG;  // coarse selection keeps <= 256 lists
   if (mode == IVF_PQ && (L.sub_dim == 0 || L.m_pq * L.sub_dim > L.dim)) return FV_ERR_ARG;
 
-  // scratch: coarse heaps | probes | work counter
+  // Work items: with fewer queries than ~4 CTAs per SM, each query's probed
+  // postings are cut into G equal ranges (a Zipf-giant list spreads over G
+  // CTAs); each range keeps its own shortlist and ivf_merge_kernel joins
+  // them. "ivf.split": -1 automatic, 0 / 1 never, G > 1 force G.
+  const uint32_t sms = (uint32_t)device_sm_count();
+  const int64_t split_knob = tune_value("ivf.split", -1);
+  uint32_t G = 1;
+  if (split_knob > 1)
+    G = (uint32_t)split_knob;
+  else if (split_knob < 0 && L.nq < 4 * sms)
+    G = (4 * sms + L.nq - 1) / L.nq;
+  G = std::max(1u, std::min<uint32_t>(std::min(G, 64u), 16384u / next_pow2(shortlist)));
+
+  // scratch: coarse heaps | probes | range shortlists | work counter
   const FlatPlan cp = plan_flat_f32(L.nlist, L.nq, nprobe, 0);
   const size_t coarse_bytes = align256(cp.scratch_bytes);
   const size_t probe_bytes = align256((size_t)L.nq * nprobe * sizeof(GpuSearchResult));
-  uint8_t* scratch = static_cast<uint8_t*>(scratch_get(stream, coarse_bytes + probe_bytes + 256));
+  const size_t part_bytes = G > 1 ? align256((size_t)L.nq * G * shortlist * 8) : 0;
+  uint8_t* scratch = static_cast<uint8_t*>(scratch_get(stream, coarse_bytes + probe_bytes + part_bytes + 256));
   if (!scratch) return (int)cudaErrorMemoryAllocation;
   GpuSearchResult* probes = reinterpret_cast<GpuSearchResult*>(scratch + coarse_bytes);
-  uint32_t* work = reinterpret_cast<uint32_t*>(scratch + coarse_bytes + probe_bytes);
+  uint64_t* partial = G > 1 ? reinterpret_cast<uint64_t*>(scratch + coarse_bytes + probe_bytes) : nullptr;
+  uint32_t* work = reinterpret_cast<uint32_t*>(scratch + coarse_bytes + probe_bytes + part_bytes);
 
   int rc = launch_flat_f32_planned(cp, L.centroids, nullptr, L.nlist, L.dim, L.queries, L.nq, nprobe, METRIC_L2,
                                    nullptr, probes, true, cp.scratch_bytes ? scratch : nullptr, stream);
@@ -443,6 +518,9 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   a.out = L.out;
   a.status = status_word();
   a.keys_pow2 = next_pow2(shortlist + IVF_BUF);
+  a.items_per_q = G;
+  a.partial = partial;
+  a.part_stride = shortlist;
 
   const size_t smem = IvfSmem::bytes(mode, a.keys_pow2, L.dim, L.m_pq);
   if (smem > 227 * 1024) return FV_ERR_ARG;
@@ -463,10 +541,18 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   if (e != cudaSuccess) return (int)e;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, IVF_THREADS, smem);
-  const uint32_t grid = std::max(1u, std::min<uint32_t>(L.nq, (uint32_t)(std::max(1, per_sm) * device_sm_count())));
+  const uint32_t grid = std::max(1u, std::min<uint32_t>(L.nq * G, (uint32_t)(std::max(1, per_sm) * sms)));
   {
     ProfScope ps(mode == IVF_PQ ? "ivf_pq_scan" : "ivf_sq8_scan", stream);
     kern<<<grid, IVF_THREADS, smem, stream>>>(a);
+    note_launch();
+  }
+  if (G > 1) {
+    const size_t msmem = (size_t)next_pow2(G * shortlist) * 8;
+    e = cudaFuncSetAttribute(ivf_merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msmem);
+    if (e != cudaSuccess) return (int)e;
+    ProfScope ps("ivf_merge", stream);
+    ivf_merge_kernel<<<L.nq, IVF_THREADS, msmem, stream>>>(a);
     note_launch();
   }
   return (int)cudaGetLastError();

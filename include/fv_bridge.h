@@ -282,6 +282,10 @@ int fv_profile_summary(char* buf, size_t len);
  *   "ivf.pipeline"      0 (default): the IVF-PQ list scan loads and scores
  *                       4 postings per thread per round; 1: 2 per round
  *                       with the next round's loads in flight
+ *   "ivf.split"         -1 (default): batches of fewer than 4 queries per
+ *                       SM cut each query's probed postings into G equal
+ *                       ranges scanned by separate CTAs and merged (same
+ *                       answer); 0 or 1: never; G > 1: always G ranges
  * Unknown keys return FV_ERR_ARG. Values apply to launches issued after the
  * call. */
 int fv_tune_set(const char* key, int64_t value);

@@ -143,3 +143,34 @@ def test_ivf_clamps_and_noops(cuda, oracle_mod, e2e_case):
     assert _lib.lib().cuda_ivf_pq_search_batch(C.byref(table.struct), C.c_void_p(1), 0, 10, 4, 0, 0, None,
                                                C.c_void_p(1), None) == 0
     assert _lib.lib().cuda_ivf_pq_search_batch(None, None, 1, 10, 4, 0, 0, None, None, None) == -1
+
+
+@pytest.mark.parametrize("mode", ["pq", "sq8"])
+@pytest.mark.parametrize("split", [0, 2, 7, 33])
+def test_ivf_posting_ranges_give_the_same_answer(cuda, oracle_mod, mode, split):
+    """A query's probed postings cut into G ranges (separate CTAs, merged
+    shortlists) answer exactly as one CTA per query, and as the oracle; a
+    skewed base puts most postings in one list, so ranges cut through it."""
+    from fvgb300 import scan
+
+    rng = np.random.default_rng(77)
+    # one tight cluster of 5,000 rows (k-means leaves it in one list) and 40
+    # small far-apart clusters
+    big = (rng.standard_normal((1, 32)) + np.float32(0.01) * rng.standard_normal((5000, 32))).astype(np.float32)
+    centers = rng.uniform(-10, 10, size=(40, 32)).astype(np.float32)
+    rest = (centers[np.arange(1000) % 40] + np.float32(0.05) * rng.standard_normal((1000, 32))).astype(np.float32)
+    x = np.vstack([big, rest]).astype(np.float32)
+    x = x[rng.permutation(x.shape[0])]
+    t = oracle_mod.build_ivf(x, nlist=16, m_pq=8, iters=10, seed=3)
+    lens = np.diff(t["offsets"].astype(np.int64))
+    assert lens.max() > 0.5 * x.shape[0]
+    q = x[rng.integers(0, x.shape[0], 12)] + np.float32(0.001)
+    words = (rng.random(x.shape[0]) < 0.7)
+    from fvgb300.datasets import pack_bools
+
+    mask = pack_bools(words)
+    with scan.tuned(ivf_split=split):
+        ids, dist = run(cuda, t, x, q, mode, 20, 6, 64, mask=mask, list_major=True)
+    fn = oracle_mod.ivf_pq_search if mode == "pq" else oracle_mod.ivf_sq_search
+    assert_same(ids, dist, fn(t, x, q, 20, 6, 64, mask=mask))
+    assert np.all(words[ids[ids != 0xFFFFFFFF]])
