@@ -746,6 +746,38 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind):
     for i in range(a.steps):
         idx.batch_search_ivf_mode(hq, a.batch, a.k, head, rerank, "pq", words)
     e2e_s = time.perf_counter() - t0
+    # CPU baseline: the oracle's restatement of the reference's IVF-PQ search
+    # (coarse probe, residual LUT, ADC, shortlist, warp-order rerank) on the
+    # host cores, over the engine's own tables, for a bounded query sample
+    cpu = None
+    if not a.no_cpu_baseline and rank == 0:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
+
+        oracle.build()
+        threads = os.cpu_count() or 1
+        t = {"nlist": nlist}
+        for key, (table, shape, dt) in {"centroids": (0, (nlist, a.dim), np.float32),
+                                        "codebooks": (1, (m_pq, 256, a.dim // m_pq), np.float32),
+                                        "pq_codes": (2, (a.n, m_pq), np.uint8), "offsets": (6, (nlist + 1,), np.uint32),
+                                        "vec_ids": (7, (a.n,), np.uint32)}.items():
+            arr = np.zeros(shape, dtype=dt)
+            _lib.call("fv_index_export_ivf", idx._h, table, arr.ctypes.data_as(C.c_void_p), arr.nbytes)
+            t[key] = arr
+        rows_np = rows.cpu().numpy()
+        qs_np = q[:threads].cpu().numpy()
+        t0 = time.perf_counter()
+        oracle.ivf_pq_search(t, rows_np, qs_np, a.k, head, rerank, mask=words, threads=threads)
+        per = (time.perf_counter() - t0) / qs_np.shape[0]
+        nsamp = int(max(threads, min(a.batch, a.cpu_seconds / max(per, 1e-9)))) // threads * threads
+        qs_np = q[:nsamp].cpu().numpy()
+        t0 = time.perf_counter()
+        ref_out = oracle.ivf_pq_search(t, rows_np, qs_np, a.k, head, rerank, mask=words, threads=threads)
+        cdt = time.perf_counter() - t0
+        same = bool(np.array_equal(ref_out["id"], out.cpu().numpy()[:nsamp, :, 0].view(np.uint32)))
+        cpu = {"value": nsamp / cdt, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{nsamp} queries, the reference's IVF-PQ search restated (nprobe {head}, rerank {rerank}) "
+                         f"over the engine's tables, {cdt:.1f} s; ids equal to the GPU's: {same}"}
     h = sweep[head]
     kname = "ivf_pq_scan"
     kms = prof[kname]["ms"] / prof[kname]["launches"]
@@ -761,7 +793,7 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind):
            "l2": "inputs larger than L2 (320 MB of codes + 40 MB ids)"}
     _line(a, world, h["qps"], UNIT, h["ms_per_batch"] * a.steps / 1e3,
           {"value": a.batch * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": a.batch * a.dim * 4 + words.nbytes,
-           "d2h_bytes_per_step": a.batch * a.k * 8}, h["launches"], roof, _kernels(prof), None, None, "f32+u8", cfg,
+           "d2h_bytes_per_step": a.batch * a.k * 8}, h["launches"], roof, _kernels(prof), None, cpu, "f32+u8", cfg,
           recall_at_10=h["recall_at_10"], recall_sample=nsub, nprobe_sweep=sweep)
 
 
