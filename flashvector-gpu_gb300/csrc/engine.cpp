@@ -30,12 +30,15 @@
 #include <memory>
 #include <mutex>
 #include <shared_mutex>
+#include <string>
+#include <type_traits>
 #include <unordered_set>
 #include <vector>
 
 #include "../../include/fv_bridge.h"
 #include "engine.h"
 #include "kernels.h"
+#include "snapshot.h"
 
 namespace fv {
 
@@ -202,6 +205,8 @@ class Index {
     }
   }
   int launch_batch(const BatchLaunch& b, cudaStream_t s);
+  int load_snapshot(const snap::File& f, std::string* error);
+  int save_snapshot(const char* path, std::string* error);
   uint32_t dim() const { return cfg_.dim; }
   int metric() const { return (int)cfg_.metric; }
   bool built() const { return built_; }
@@ -709,6 +714,322 @@ int Index::search(const FvSearchParams& p, const float* q, uint32_t nq, bool dev
   return 0;
 }
 
+// ------------------------------------------------------------ snapshots
+// The reference's FLSHVEC1 file (persistence.rs, index.rs:845-1260) read
+// into the engine's device tables, and written from them.
+//
+// Load: sections are copied to the GPU straight from the read-only mapping
+// (page-locked in place when the driver allows, so the copies are DMA from
+// the page cache). Slots whose logical id differs from the slot index
+// (logical_ids not the identity) are placed at their logical ids, so the
+// engine keeps slot == logical id; never-assigned ids in between become
+// invalid slots. Tables the file lacks or that this engine adds are built on
+// the GPU: fp16 rows when the file has none of this padding, fp8 rows, and
+// the list-major IVF code copies.
+//
+// Save: every section the reference's loader requires is written, the
+// graph and RaBitQ ones (outside this engine) empty, so the reference can
+// open the file and serve the flat / fp16 / IVF paths from it.
+namespace {
+// Page-locks the mapping for the duration of a load (copies from it are then
+// DMA); on destruction waits for the stream's copies before unlocking.
+struct HostRegistration {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  bool ok = false;
+  HostRegistration(const void* ptr, size_t bytes, cudaStream_t stream) : s(stream) {
+    if (bytes == 0) return;
+    p = const_cast<void*>(ptr);
+    ok = cudaHostRegister(p, bytes, cudaHostRegisterReadOnly) == cudaSuccess;
+    if (!ok) cudaGetLastError();  // clear: the copies fall back to staged transfers
+  }
+  ~HostRegistration() {
+    cudaStreamSynchronize(s);
+    if (ok) cudaHostUnregister(p);
+  }
+};
+
+template <class T>
+int upload(DevBuf<T>& dst, const uint8_t* src, uint64_t bytes, cudaStream_t s) {
+  int rc = dst.alloc(bytes / sizeof(T));
+  if (!rc && bytes) rc = (int)cudaMemcpyAsync(dst.p, src, bytes, cudaMemcpyHostToDevice, s);
+  return rc;
+}
+}  // namespace
+
+int Index::load_snapshot(const snap::File& f, std::string* error) {
+  std::unique_lock<std::shared_mutex> lk(state_mu_);
+  wait_unpinned();
+  const snap::Manifest& m = f.manifest();
+  auto fail = [&](const std::string& why) {
+    if (error) *error = why;
+    return FV_ERR_ARG;
+  };
+  const uint32_t dim = cfg_.dim;
+  const uint64_t n = m.num_vectors;
+  if (n == 0 || n >= 0xFFFFFFFFull) return fail("snapshot holds no vectors (or more than 2^32 - 1)");
+  uint64_t b = 0;
+  const uint8_t* vecs = f.section("vectors", &b);
+  if (!vecs || b != n * dim * 4) return fail("vectors section missing or not num_vectors x dim f32");
+  cudaStream_t s = streams_[0]->s;
+  HostRegistration reg(f.base(), f.size(), s);
+
+  // logical ids: slot -> logical id (identity when absent)
+  std::vector<uint32_t> lid;
+  uint64_t lb = 0;
+  if (const uint8_t* p = f.section("logical_ids", &lb)) {
+    if (lb != n * 4) return fail("logical_ids section is not num_vectors u32");
+    lid.assign(reinterpret_cast<const uint32_t*>(p), reinterpret_cast<const uint32_t*>(p) + n);
+  }
+  bool identity = true;
+  uint64_t nslots = n;
+  for (uint64_t i = 0; i < lid.size(); ++i) {
+    identity = identity && lid[i] == i;
+    nslots = std::max<uint64_t>(nslots, (uint64_t)lid[i] + 1);
+  }
+  if (!identity && nslots > std::max<uint64_t>(4 * n, n + 4096))
+    return fail("logical ids too sparse to place at their own slots (more than 4x the row count)");
+  // inv[logical] = slot, n = no row (zero / invalid)
+  std::vector<uint32_t> inv;
+  DevBuf<uint32_t> d_inv;
+  if (!identity) {
+    inv.assign(nslots, (uint32_t)n);
+    for (uint64_t i = 0; i < n; ++i) {
+      if (inv[lid[i]] != (uint32_t)n) return fail("duplicate logical id in logical_ids");
+      inv[lid[i]] = (uint32_t)i;
+    }
+    int rc = d_inv.alloc(nslots);
+    if (!rc) rc = (int)cudaMemcpyAsync(d_inv.p, inv.data(), nslots * 4, cudaMemcpyHostToDevice, s);
+    if (rc) return rc;
+  }
+  // a table of n rows -> the engine's nslots rows at logical positions
+  auto place_rows = [&](const uint8_t* src, uint64_t row_bytes, auto& dst) -> int {
+    using T = typename std::remove_reference<decltype(*dst.p)>::type;
+    if (identity) return upload(dst, src, n * row_bytes, s);
+    DevBuf<uint8_t> tmp;
+    int rc = upload(tmp, src, n * row_bytes, s);
+    if (!rc) rc = dst.alloc(nslots * row_bytes / sizeof(T));
+    if (!rc) rc = launch_gather_row_bytes(tmp.p, d_inv.p, (uint32_t)nslots, (uint32_t)row_bytes, (uint32_t)n, dst.p, s);
+    if (!rc) rc = (int)cudaStreamSynchronize(s);  // tmp is freed on return
+    return rc;
+  };
+  int rc = place_rows(vecs, (uint64_t)dim * 4, vectors_);
+  if (rc) return rc;
+  n_ = (uint32_t)nslots;
+
+  // validity words over slots -> over logical ids (tombstoned and unassigned
+  // ids invalid)
+  std::vector<uint32_t> slot_valid((n + 31) / 32, 0xFFFFFFFFu);
+  uint64_t vb = 0;
+  if (const uint8_t* p = f.section("main_valid_words", &vb)) {
+    if (vb < slot_valid.size() * 4) return fail("main_valid_words shorter than num_vectors bits");
+    std::memcpy(slot_valid.data(), p, slot_valid.size() * 4);
+  }
+  main_valid_.assign((nslots + 31) / 32, 0u);
+  tombstones_.clear();
+  for (uint64_t i = 0; i < n; ++i) {
+    const uint32_t l = identity ? (uint32_t)i : lid[i];
+    if ((slot_valid[i >> 5] >> (i & 31)) & 1u)
+      main_valid_[l >> 5] |= 1u << (l & 31);
+    else
+      tombstones_.insert(l);
+  }
+  uint64_t tb = 0;
+  if (const uint8_t* p = f.section("tombstones", &tb)) {
+    const uint32_t* t = reinterpret_cast<const uint32_t*>(p);
+    for (uint64_t i = 0; i < tb / 4; ++i) tombstones_.insert(t[i]);
+  }
+  rc = valid_words_.alloc(main_valid_.size());
+  if (!rc) rc = (int)cudaMemcpyAsync(valid_words_.p, main_valid_.data(), main_valid_.size() * 4,
+                                     cudaMemcpyHostToDevice, s);
+  if (rc) return rc;
+
+  // fp16 rows: the file's when padded as this engine pads, else encoded here
+  pd16_ = pd8_ = 0;
+  if (cfg_.build_flags & FV_BUILD_FP16) {
+    const uint32_t pd = (dim + 15) / 16 * 16;
+    uint64_t hb = 0, nb = 0;
+    const uint8_t* h = f.section("vectors_fp16", &hb);
+    const uint8_t* nr = f.section("vec_norms_sq", &nb);
+    pd16_ = pd;
+    if (h && nr && m.fp16_padded_dim == pd && hb == n * pd * 2 && nb == n * 4) {
+      rc = place_rows(h, (uint64_t)pd * 2, fp16_);
+      if (!rc) rc = place_rows(nr, 4, norms16_);
+    } else {
+      rc = fp16_.alloc((size_t)n_ * pd);
+      if (!rc) rc = norms16_.alloc(n_);
+      if (!rc) rc = launch_encode_fp16(vectors_.p, n_, dim, pd, fp16_.p, norms16_.p, s);
+    }
+    if (rc) return rc;
+  }
+  if (cfg_.build_flags & FV_BUILD_FP8) {
+    pd8_ = (dim + 15) / 16 * 16;
+    rc = fp8_.alloc((size_t)n_ * pd8_);
+    if (!rc) rc = fp8_scales_.alloc(n_);
+    if (!rc) rc = fp8_norms_.alloc(n_);
+    if (!rc) rc = launch_encode_fp8(vectors_.p, n_, dim, pd8_, fp8_.p, fp8_scales_.p, fp8_norms_.p, s);
+    if (rc) return rc;
+  }
+
+  // IVF tables (ids in the lists are slots: mapped to logical ids)
+  nlist_ = 0;
+  uint64_t cb = 0, ob = 0, ib = 0;
+  const uint8_t* cent = f.section("ivf_centroids", &cb);
+  const uint8_t* offs = f.section("ivf_offsets", &ob);
+  const uint8_t* vids = f.section("ivf_vec_ids", &ib);
+  if (m.nlist && cent && offs && vids && cb == (uint64_t)m.nlist * dim * 4 && ob == ((uint64_t)m.nlist + 1) * 4 &&
+      ib == n * 4) {
+    nlist_ = m.nlist;
+    rc = upload(centroids_, cent, cb, s);
+    if (!rc) rc = upload(offsets_, offs, ob, s);
+    DevBuf<uint32_t> slot_ids;  // list order, slots (for the list-major copies)
+    if (!rc) rc = upload(slot_ids, vids, ib, s);
+    std::vector<uint32_t> mapped(reinterpret_cast<const uint32_t*>(vids), reinterpret_cast<const uint32_t*>(vids) + n);
+    for (auto& v : mapped) {
+      if (v >= n) return fail("ivf_vec_ids holds a slot beyond num_vectors");
+      if (!identity) v = lid[v];
+    }
+    if (!rc) rc = vec_ids_.alloc(n);
+    if (!rc) rc = (int)cudaMemcpyAsync(vec_ids_.p, mapped.data(), n * 4, cudaMemcpyHostToDevice, s);
+    if (!rc) rc = (int)cudaStreamSynchronize(s);  // `mapped` is freed on return
+    if (rc) return rc;
+    uint64_t bb = 0, pb = 0;
+    const uint8_t* books = f.section("pq_codebooks", &bb);
+    const uint8_t* pcodes = f.section("pq_codes", &pb);
+    const uint32_t mq = m.m_pq;
+    if (mq && dim % mq == 0 && books && pcodes && bb == (uint64_t)mq * 256 * (dim / mq) * 4 && pb == n * mq) {
+      rc = upload(codebooks_, books, bb, s);
+      DevBuf<uint8_t> by_slot;
+      if (!rc) rc = upload(by_slot, pcodes, pb, s);
+      if (!rc) rc = pq_codes_lm_.alloc(n * mq);
+      if (!rc) rc = launch_relayout_codes(by_slot.p, slot_ids.p, (uint32_t)n, mq, pq_codes_lm_.p, s);
+      if (!rc) rc = place_rows(pcodes, mq, pq_codes_);
+      if (!rc) rc = (int)cudaStreamSynchronize(s);
+      if (rc) return rc;
+    }
+    uint64_t mb = 0, sb = 0, qb = 0;
+    const uint8_t* mins = f.section("sq_mins", &mb);
+    const uint8_t* scales = f.section("sq_scales", &sb);
+    const uint8_t* scodes = f.section("sq_codes", &qb);
+    if (mins && scales && scodes && mb == (uint64_t)dim * 4 && sb == (uint64_t)dim * 4 && qb == n * dim) {
+      rc = upload(sq_mins_, mins, mb, s);
+      if (!rc) rc = upload(sq_scales_, scales, sb, s);
+      DevBuf<uint8_t> by_slot;
+      if (!rc) rc = upload(by_slot, scodes, qb, s);
+      if (!rc) rc = sq_codes_lm_.alloc(n * dim);
+      if (!rc) rc = launch_relayout_codes(by_slot.p, slot_ids.p, (uint32_t)n, dim, sq_codes_lm_.p, s);
+      if (!rc) rc = place_rows(scodes, dim, sq_codes_);
+      if (!rc) rc = (int)cudaStreamSynchronize(s);
+      if (rc) return rc;
+    }
+  }
+
+  // live-insert buffer
+  delta_.vectors.clear();
+  delta_.ids.clear();
+  delta_.live.clear();
+  uint64_t dvb = 0, dib = 0;
+  const uint8_t* dv = f.section("delta_vectors", &dvb);
+  const uint8_t* di = f.section("delta_ids", &dib);
+  uint32_t next = m.next_logical_id;
+  next = std::max<uint32_t>(next, (uint32_t)nslots);
+  if (dv && di && dib > 0) {
+    const uint64_t len = dib / 4;
+    if (dvb != len * dim * 4) return fail("delta_vectors does not match delta_ids");
+    delta_.vectors.assign(reinterpret_cast<const float*>(dv), reinterpret_cast<const float*>(dv) + len * dim);
+    delta_.ids.assign(reinterpret_cast<const uint32_t*>(di), reinterpret_cast<const uint32_t*>(di) + len);
+    size_t cap = 256;
+    while (cap < len) cap <<= 1;
+    rc = delta_.d_vectors.alloc(cap * dim);
+    if (!rc) rc = delta_.d_ids.alloc(cap);
+    if (!rc) rc = delta_.d_mask.alloc((cap + 31) / 32);
+    if (!rc) rc = delta_.d_live.alloc((cap + 31) / 32);
+    if (rc) return rc;
+    delta_.capacity = cap;
+    delta_.live.assign((len + 31) / 32, 0u);
+    for (uint64_t i = 0; i < len; ++i) {
+      if (!tombstones_.count(delta_.ids[i])) delta_.live[i >> 5] |= 1u << (i & 31);
+      next = std::max<uint32_t>(next, delta_.ids[i] + 1);
+    }
+    rc = (int)cudaMemcpyAsync(delta_.d_vectors.p, delta_.vectors.data(), len * dim * 4, cudaMemcpyHostToDevice, s);
+    if (!rc) rc = (int)cudaMemcpyAsync(delta_.d_ids.p, delta_.ids.data(), len * 4, cudaMemcpyHostToDevice, s);
+    if (!rc) rc = upload_delta_live(s);
+    if (rc) return rc;
+  }
+  next_id_ = next;
+  rc = (int)cudaStreamSynchronize(s);
+  if (rc) return rc;
+  built_ = true;
+  return 0;
+}
+
+int Index::save_snapshot(const char* path, std::string* error) {
+  std::shared_lock<std::shared_mutex> lk(state_mu_);
+  if (!built_) {
+    if (error) *error = "index not built";
+    return FV_ERR_ARG;
+  }
+  const uint32_t dim = cfg_.dim;
+  auto d2h = [](const auto& buf, auto& host) -> int {
+    host.resize(buf.n);
+    return buf.n ? (int)cudaMemcpy(host.data(), buf.p, buf.bytes(), cudaMemcpyDeviceToHost) : 0;
+  };
+  std::vector<float> vecs, cent, books, mins, scales, norms;
+  std::vector<uint16_t> f16;
+  std::vector<uint8_t> pq, sq;
+  std::vector<uint32_t> offs, vids;
+  int rc = d2h(vectors_, vecs);
+  if (!rc) rc = d2h(centroids_, cent);
+  if (!rc) rc = d2h(codebooks_, books);
+  if (!rc) rc = d2h(pq_codes_, pq);
+  if (!rc) rc = d2h(offsets_, offs);
+  if (!rc) rc = d2h(vec_ids_, vids);
+  if (!rc) rc = d2h(sq_mins_, mins);
+  if (!rc) rc = d2h(sq_scales_, scales);
+  if (!rc) rc = d2h(sq_codes_, sq);
+  if (!rc) rc = d2h(fp16_, f16);
+  if (!rc) rc = d2h(norms16_, norms);
+  if (rc) return rc;
+  std::vector<uint32_t> ids(n_);
+  for (uint32_t i = 0; i < n_; ++i) ids[i] = i;
+  std::vector<uint32_t> tomb(tombstones_.begin(), tombstones_.end());
+  std::sort(tomb.begin(), tomb.end());
+
+  snap::Manifest m;
+  m.version = 1;
+  m.dim = dim;
+  m.max_elements = n_;
+  m.nlist = nlist_;
+  m.m_pq = codebooks_.n ? cfg_.m_pq : 0;
+  m.metric = cfg_.metric;
+  m.num_vectors = n_;
+  m.fp16_padded_dim = fp16_.n ? pd16_ : 0;
+  m.next_logical_id = next_id_;
+  auto sec = [](const char* name, const char* dtype, const auto& v) {
+    using T = typename std::decay<decltype(v[0])>::type;
+    return snap::OutSection{name, dtype, (uint64_t)v.size(), v.data(), (uint64_t)v.size() * sizeof(T)};
+  };
+  const std::vector<uint32_t> none_u32;
+  const std::vector<float> none_f32;
+  std::vector<snap::OutSection> out = {
+      sec("vectors", "f32", vecs),          sec("logical_ids", "u32", ids),
+      sec("main_valid_words", "u32", main_valid_), sec("hnsw_adjacency", "u32", none_u32),
+      sec("hnsw_degrees", "u32", none_u32), sec("cagra_adjacency", "u32", none_u32),
+      sec("ivf_centroids", "f32", cent),    sec("pq_codebooks", "f32", books),
+      sec("pq_codes", "u8", pq),            sec("ivf_offsets", "u32", offs),
+      sec("ivf_vec_ids", "u32", vids),      sec("sq_mins", "f32", mins),
+      sec("sq_scales", "f32", scales),      sec("sq_codes", "u8", sq),
+      sec("rabitq_signs", "f32", none_f32), sec("rabitq_centroids", "f32", none_f32),
+      sec("rabitq_bits", "u32", none_u32),  sec("rabitq_meta", "f32", none_f32),
+      sec("vectors_fp16", "u16", f16),      sec("vec_norms_sq", "f32", norms)};
+  if (!tomb.empty()) out.push_back(sec("tombstones", "u32", tomb));
+  if (delta_.len()) {
+    out.push_back(sec("delta_vectors", "f32", delta_.vectors));
+    out.push_back(sec("delta_ids", "u32", delta_.ids));
+  }
+  return snap::write(path, m, out, error);
+}
+
 // ------------------------------------------------------- served batches
 // One heterogeneous batch on the caller's stream, with the semantics of
 // search() for every query taken alone: the main scan (shared validity
@@ -958,5 +1279,66 @@ int fv_index_export_ivf(FvIndex* index, uint32_t table, void* host_out, size_t b
   if (!index) return FV_ERR_NULL;
   return index->impl.export_ivf(table, host_out, bytes);
 }
+
+namespace {
+thread_local std::string g_snapshot_error;
+}
+
+int fv_index_save_snapshot(FvIndex* index, const char* path) {
+  if (!index || !path) return FV_ERR_NULL;
+  g_snapshot_error.clear();
+  return index->impl.save_snapshot(path, &g_snapshot_error);
+}
+
+int fv_index_load_snapshot(const char* path, const FvIndexConfig* config, FvIndex** out) {
+  if (!path || !out) return FV_ERR_NULL;
+  g_snapshot_error.clear();
+  fv::snap::File f;
+  int rc = f.open(path, &g_snapshot_error);
+  if (rc) return rc;
+  const fv::snap::Manifest& m = f.manifest();
+  if (m.dim == 0 || m.dim > 4096 || m.metric > 2) {
+    g_snapshot_error = "snapshot config out of range";
+    return FV_ERR_ARG;
+  }
+  FvIndexConfig c{};
+  if (config) c = *config;
+  c.dim = m.dim;
+  c.metric = m.metric;
+  c.nlist = m.nlist;
+  c.m_pq = m.m_pq;
+  if (c.build_flags == 0) c.build_flags = FV_BUILD_FP16 | FV_BUILD_IVF_PQ | FV_BUILD_IVF_SQ8;
+  FvIndex* idx = nullptr;
+  try {
+    idx = new FvIndex(c);
+  } catch (...) {
+    return FV_ERR_NOMEM;
+  }
+  rc = idx->impl.load_snapshot(f, &g_snapshot_error);
+  if (rc) {
+    delete idx;
+    return rc;
+  }
+  *out = idx;
+  return 0;
+}
+
+int fv_snapshot_inspect(const char* path, char* manifest_json, size_t len, size_t* needed) {
+  if (!path) return FV_ERR_NULL;
+  g_snapshot_error.clear();
+  fv::snap::File f;
+  const int rc = f.open(path, &g_snapshot_error);
+  if (rc) return rc;
+  const std::string j = fv::snap::manifest_to_json(f.manifest());
+  if (needed) *needed = j.size() + 1;
+  if (manifest_json && len) {
+    const size_t c = std::min(len - 1, j.size());
+    std::memcpy(manifest_json, j.data(), c);
+    manifest_json[c] = 0;
+  }
+  return 0;
+}
+
+const char* fv_snapshot_error(void) { return g_snapshot_error.c_str(); }
 
 }  // extern "C"

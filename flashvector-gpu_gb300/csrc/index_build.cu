@@ -206,6 +206,30 @@ __global__ void gather_rows_kernel(const float* __restrict__ x, const uint32_t* 
   }
 }
 
+// out row i = in row rows[i], or zeros when rows[i] == zero_row; rows of
+// `words` 32-bit words (snapshot loads that place slots at logical ids)
+__global__ void gather_word_rows_kernel(const uint32_t* __restrict__ in, const uint32_t* __restrict__ rows,
+                                        uint32_t count, uint32_t words, uint32_t zero_row,
+                                        uint32_t* __restrict__ out) {
+  const uint64_t total = (uint64_t)count * words;
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = e / words, w = e % words;
+    const uint32_t r = rows[i];
+    out[e] = r == zero_row ? 0u : in[(uint64_t)r * words + w];
+  }
+}
+
+__global__ void gather_byte_rows_kernel(const uint8_t* __restrict__ in, const uint32_t* __restrict__ rows,
+                                        uint32_t count, uint32_t row_bytes, uint32_t zero_row,
+                                        uint8_t* __restrict__ out) {
+  const uint64_t total = (uint64_t)count * row_bytes;
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = e / row_bytes, b = e % row_bytes;
+    const uint32_t r = rows[i];
+    out[e] = r == zero_row ? (uint8_t)0 : in[(uint64_t)r * row_bytes + b];
+  }
+}
+
 __global__ void fill_f32_kernel(float* p, size_t n, float v) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
 }
@@ -289,6 +313,21 @@ int launch_gather_rows(const float* x, const uint32_t* rows, uint32_t count, uin
                        cudaStream_t stream) {
   if (count == 0) return 0;
   gather_rows_kernel<<<grid_for((uint64_t)count * dim), 256, 0, stream>>>(x, rows, count, dim, out);
+  note_launch();
+  return (int)cudaGetLastError();
+}
+
+int launch_gather_row_bytes(const void* in, const uint32_t* rows, uint32_t count, uint32_t row_bytes,
+                            uint32_t zero_row, void* out, cudaStream_t stream) {
+  if (count == 0 || row_bytes == 0) return 0;
+  if (row_bytes % 4 == 0 && (uintptr_t)in % 4 == 0 && (uintptr_t)out % 4 == 0) {
+    const uint32_t words = row_bytes / 4;
+    gather_word_rows_kernel<<<grid_for((uint64_t)count * words), 256, 0, stream>>>(
+        static_cast<const uint32_t*>(in), rows, count, words, zero_row, static_cast<uint32_t*>(out));
+  } else {
+    gather_byte_rows_kernel<<<grid_for((uint64_t)count * row_bytes), 256, 0, stream>>>(
+        static_cast<const uint8_t*>(in), rows, count, row_bytes, zero_row, static_cast<uint8_t*>(out));
+  }
   note_launch();
   return (int)cudaGetLastError();
 }

@@ -171,6 +171,9 @@ int launch_sq8_encode(const float* r, uint32_t n, uint32_t dim, const float* min
 int launch_gather_rows(const float* x, const uint32_t* rows, uint32_t count, uint32_t dim, float* out,
                        cudaStream_t stream);
 int launch_fill_f32(float* p, size_t n, float v, cudaStream_t stream);
+// out row i = in row rows[i] (rows of row_bytes bytes), zeros where rows[i] == zero_row
+int launch_gather_row_bytes(const void* in, const uint32_t* rows, uint32_t count, uint32_t row_bytes,
+                            uint32_t zero_row, void* out, cudaStream_t stream);
 
 // reduced-precision table encoders (encode.cu)
 int launch_encode_fp16(const float* x, uint32_t n, uint32_t dim, uint32_t pd, uint16_t* out, float* norms,

@@ -145,6 +145,10 @@ SIGNATURES = {
     "fv_index_info": (I32, [P, P]),
     "fv_index_ivf_tables": (I32, [P, P, P, P]),
     "fv_index_export_ivf": (I32, [P, U32, P, SZ]),
+    "fv_index_save_snapshot": (I32, [P, C.c_char_p]),
+    "fv_index_load_snapshot": (I32, [C.c_char_p, P, P]),
+    "fv_snapshot_inspect": (I32, [C.c_char_p, C.c_char_p, SZ, P]),
+    "fv_snapshot_error": (C.c_char_p, []),
     "fv_graph_begin": (I32, [P]),
     "fv_graph_end": (I32, [P, P]),
     "fv_graph_launch": (I32, [P, P]),

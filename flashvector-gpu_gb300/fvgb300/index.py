@@ -136,6 +136,29 @@ class GpuVectorIndex:
              out.ctypes.data_as(C.c_void_p))
         return out[..., 0].copy(), out[..., 1].view(np.float32).copy()
 
+    # --------------------------------------------------------- snapshots
+    def save_snapshot(self, path) -> None:
+        """GpuVectorIndex::save_snapshot (index.rs:845-1031): a FLSHVEC1 file."""
+        code = _lib.lib().fv_index_save_snapshot(self._h, str(path).encode())
+        if code != 0:
+            raise _lib.FvError(f"fv_index_save_snapshot ({_lib.lib().fv_snapshot_error().decode()})", code)
+
+    @classmethod
+    def load_snapshot(cls, path, config: IndexConfig | None = None) -> "GpuVectorIndex":
+        """GpuVectorIndex::load_snapshot (index.rs:1033-1260). The file sets dim,
+        metric, nlist and m_pq; `config` may add build flags (FP8) and streams."""
+        h = C.c_void_p()
+        c = config.to_c() if config is not None else None
+        code = _lib.lib().fv_index_load_snapshot(str(path).encode(), None if c is None else C.byref(c), C.byref(h))
+        if code != 0:
+            raise _lib.FvError(f"fv_index_load_snapshot ({_lib.lib().fv_snapshot_error().decode()})", code)
+        obj = cls.__new__(cls)
+        obj._h = h
+        inf = obj.info()
+        obj.config = IndexConfig(dim=inf["dim"], nlist=inf["nlist"], m_pq=inf["m_pq"], metric=inf["metric"],
+                                 build_flags=config.build_flags if config else BUILD_FP16 | BUILD_IVF_PQ | BUILD_IVF_SQ8)
+        return obj
+
     # ------------------------------------------------------------ status
     def metrics(self) -> dict:
         s = _lib.FvLatencyStats()
@@ -178,3 +201,16 @@ class GpuVectorIndex:
             call("fv_index_export_ivf", self._h, table, a.ctypes.data_as(C.c_void_p), a.nbytes)
             out[key] = a
         return out
+
+
+def snapshot_manifest(path) -> dict:
+    """The manifest of a FLSHVEC1 snapshot (no GPU needed)."""
+    import json
+
+    need = C.c_size_t(0)
+    code = _lib.lib().fv_snapshot_inspect(str(path).encode(), None, 0, C.byref(need))
+    if code != 0:
+        raise _lib.FvError(f"fv_snapshot_inspect ({_lib.lib().fv_snapshot_error().decode()})", code)
+    buf = C.create_string_buffer(need.value)
+    call("fv_snapshot_inspect", str(path).encode(), buf, need.value, None)
+    return json.loads(buf.value.decode())

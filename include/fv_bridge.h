@@ -223,6 +223,23 @@ int fv_index_ivf_tables(FvIndex* index, IvfPqGpuTables* pq, IvfSqGpuTables* sq, 
  * 7 list ids. */
 int fv_index_export_ivf(FvIndex* index, uint32_t table, void* host_out, size_t bytes);
 
+/* Snapshots in the reference's FLSHVEC1 format (persistence.rs:1-200,
+ * GpuVectorIndex::save_snapshot / load_snapshot, index.rs:845-1260).
+ * save: every section the reference's loader requires (the graph and
+ * RaBitQ sections it does not serve from this engine are written empty).
+ * load: the file's dim / metric / nlist / m_pq; `config` (optional)
+ * supplies build_flags (FV_BUILD_FP8 adds an fp8 table built on the GPU;
+ * fp16 rows are taken from the file when padded as this engine pads, else
+ * encoded), streams and seed. Sections are copied to the GPU from a
+ * read-only mapping of the file; rows whose logical id differs from their
+ * slot are placed at their logical id. fv_snapshot_inspect (no GPU
+ * needed) writes the manifest as JSON; fv_snapshot_error describes the last
+ * failure of these calls on this thread. */
+int fv_index_save_snapshot(FvIndex* index, const char* path);
+int fv_index_load_snapshot(const char* path, const FvIndexConfig* config, FvIndex** out);
+int fv_snapshot_inspect(const char* path, char* manifest_json, size_t len, size_t* needed);
+const char* fv_snapshot_error(void);
+
 /* ---- CUDA graphs -------------------------------------------------------
  * Capture the library calls issued on `stream` between fv_graph_begin and
  * fv_graph_end into one replayable graph (the steady-state search of a fixed
