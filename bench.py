@@ -43,10 +43,12 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="fp16_ip", choices=["fp16_ip", "fp8_l2", "ivf_pq", "flat_f32", "serve"],
+    ap.add_argument("--workload", default="fp16_ip",
+                    choices=["fp16_ip", "fp8_l2", "ivf_pq", "ivf_rabitq", "flat_f32", "serve"],
                     help="fp16_ip (default, the headline): 1M x 768 fp16 IP scan + rescore; fp8_l2: 10M x 96 fp8 "
                          "L2 scan + rescore vs the exact fp32 scan; ivf_pq: 10M x 128 IVF-PQ over Zipf-skewed "
-                         "lists; flat_f32: 100k x 128 exact fp32 L2 scan; serve: continuous batching over a "
+                         "lists; ivf_rabitq: the same rows and lists as IVF-RaBitQ; flat_f32: 100k x 128 exact "
+                         "fp32 L2 scan; serve: continuous batching over a "
                          "1M x 768 fp16 flat index + IVF-SQ8 (nlist 4096) under Poisson arrivals")
     ap.add_argument("--rates", type=str, default="5000,20000,50000,100000,200000",
                     help="serve: offered request rates (requests/s)")
@@ -57,12 +59,13 @@ def parse_args():
     ap.add_argument("--k", type=int, default=None)
     ap.add_argument("--overfetch", type=int, default=4, help="fp16_ip: shortlist = overfetch x k")
     ap.add_argument("--overfetch-fp8", type=int, default=None, help="fp8_l2: over-fetch (default: autotuned)")
-    ap.add_argument("--nprobe", type=str, default="8,32,128", help="ivf_pq: comma-separated nprobe sweep")
+    ap.add_argument("--nprobe", type=str, default="8,32,128", help="ivf_pq / ivf_rabitq: comma-separated nprobe sweep")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     a = ap.parse_args()
     defaults = {"fp16_ip": (1_000_000, 768, 1024, 10), "fp8_l2": (10_000_000, 96, 10_000, 100),
-                "ivf_pq": (10_000_000, 128, 10_000, 10), "flat_f32": (100_000, 128, 1000, 10),
+                "ivf_pq": (10_000_000, 128, 10_000, 10), "ivf_rabitq": (10_000_000, 128, 10_000, 10),
+                "flat_f32": (100_000, 128, 1000, 10),
                 "serve": (1_000_000, 768, 1024, 10)}[a.workload]
     a.n = a.n or defaults[0]
     a.dim = a.dim or defaults[1]
@@ -607,8 +610,8 @@ def run_workload(a, world, rank, local):
               fp32_exact_scan={"value": f32_qps, "unit": UNIT, "steps": f32_steps, "speedup_fp8_over_fp32": qps / f32_qps})
         return
 
-    if a.workload == "ivf_pq":
-        run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind)
+    if a.workload in ("ivf_pq", "ivf_rabitq"):
+        run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind, a.workload[4:])
         return
     if a.workload == "serve":
         run_serve(a, world, rank, local, dev, peaks, peak_kind)
@@ -661,19 +664,25 @@ def zipf_ivf_data(n, dim, nlist, seed, device):
     return rows, c_dev, queries, sizes
 
 
-def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind):
+def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind, mode="pq"):
+    """mode "pq": IVF-PQ (m_pq 32); "rabitq": IVF-RaBitQ on the same rows
+    (P = 128 sign bits + 16-byte meta per row), same lists, rerank and mask."""
     import ctypes as C
 
     import numpy as np
     import torch
 
     from fvgb300 import _lib, datasets, scan
-    from fvgb300.index import BUILD_IVF_PQ, GpuVectorIndex, IndexConfig
+    from fvgb300.index import BUILD_IVF_PQ, BUILD_IVF_RABITQ, GpuVectorIndex, IndexConfig
 
     nlist, m_pq, rerank = 16384, 32, 400
+    rq = mode == "rabitq"
+    P = _lib.lib().fv_rabitq_padded_dim(a.dim)
+    row_bytes = P // 8 + 16 if rq else m_pq  # bytes per posting besides its 4-byte id
     t_build = time.perf_counter()
     rows, centers, qgen, gen_sizes = zipf_ivf_data(a.n, a.dim, nlist, 3, dev)
-    idx = GpuVectorIndex(IndexConfig(dim=a.dim, nlist=nlist, m_pq=m_pq, metric="l2", build_flags=BUILD_IVF_PQ,
+    idx = GpuVectorIndex(IndexConfig(dim=a.dim, nlist=nlist, m_pq=m_pq, metric="l2",
+                                     build_flags=BUILD_IVF_RABITQ if rq else BUILD_IVF_PQ,
                                      kmeans_iters_given=2, train_rows=min(a.n, 4 * nlist * 64), pq_iters=10, seed=3))
     idx.build_device(rows, centers)
     torch.cuda.synchronize()
@@ -684,7 +693,12 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind):
     hist = {"max": int(lens.max()), "p50": int(np.median(lens)), "p99": int(np.percentile(lens, 99)),
             "lists_at_or_below_64": int((lens <= 64).sum()), "empty": int((lens == 0).sum()),
             "generated_max": int(gen_sizes.max())}
-    pq, sq, opt = idx.ivf_tables()
+    if rq:
+        tab, opt = idx.rabitq_tables()
+        fn_name = "fv_ivf_rabitq_search_ex"
+    else:
+        tab, _, opt = idx.ivf_tables()
+        fn_name = "fv_ivf_pq_search_ex"
     q = qgen(a.batch, 4242).contiguous()
     words = datasets.bernoulli_mask_words(a.n, 0.10, seed=3)
     mask = torch.from_numpy(words.view(np.int32)).to(dev)
@@ -692,7 +706,7 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind):
     out = scan.empty_results(a.batch, a.k, dev)
 
     def search(nprobe, qq=q):
-        _lib.call("fv_ivf_pq_search_ex", C.byref(pq), C.byref(opt), C.c_void_p(qq.data_ptr()), a.batch, a.k, nprobe,
+        _lib.call(fn_name, C.byref(tab), C.byref(opt), C.c_void_p(qq.data_ptr()), a.batch, a.k, nprobe,
                   rerank, 0, C.c_void_p(mask.data_ptr()), C.c_void_p(out.data_ptr()),
                   C.c_void_p(torch.cuda.current_stream().cuda_stream))
 
@@ -706,11 +720,12 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind):
         torch.cuda.synchronize()
         ids = out.cpu().numpy()[..., 0].view(np.uint32)
         rec = _recall(ids[:nsub], truth)
-        # scanned entries (algorithmic bytes: 32-byte code row + 4-byte id per entry, plus the mask word reads)
+        # scanned entries (algorithmic bytes: code row (PQ 32 B; RaBitQ 16 B bits + 16 B meta) + 4-byte id
+        # per entry, plus the mask word reads)
         cd = torch.cdist(q, centers)
         probes = torch.topk(cd, nprobe, dim=1, largest=False).indices
         scanned = int(torch.from_numpy(lens).to(dev)[probes].sum())
-        bytes_step = scanned * (m_pq + 4) + scanned // 8
+        bytes_step = scanned * (row_bytes + 4) + scanned // 8
         # graph-captured steady state
         with torch.cuda.stream(cstream):
             search(nprobe)
@@ -741,14 +756,16 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind):
     prof = scan.profile_summary()
     # end to end through the engine (host queries, host mask words, host results)
     hq = q.cpu().numpy()
-    idx.batch_search_ivf_mode(hq, a.batch, a.k, head, rerank, "pq", words)
+    idx.batch_search_ivf_mode(hq, a.batch, a.k, head, rerank, mode, words)
     t0 = time.perf_counter()
     for i in range(a.steps):
-        idx.batch_search_ivf_mode(hq, a.batch, a.k, head, rerank, "pq", words)
+        idx.batch_search_ivf_mode(hq, a.batch, a.k, head, rerank, mode, words)
     e2e_s = time.perf_counter() - t0
-    # CPU baseline: the oracle's restatement of the reference's IVF-PQ search
-    # (coarse probe, residual LUT, ADC, shortlist, warp-order rerank) on the
-    # host cores, over the engine's own tables, for a bounded query sample
+    # CPU baseline: the oracle's restatement of the reference's IVF-PQ
+    # (coarse probe, residual LUT, ADC, shortlist, warp-order rerank) or
+    # IVF-RaBitQ search (rotation, 4-bit query code, popcount estimate,
+    # shortlist, rerank) on the host cores, over the engine's own tables, for
+    # a bounded query sample
     cpu = None
     if not a.no_cpu_baseline and rank == 0:
         sys.path.insert(0, str(ROOT / "oracle"))
@@ -756,44 +773,58 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind):
 
         oracle.build()
         threads = os.cpu_count() or 1
-        t = {"nlist": nlist}
-        for key, (table, shape, dt) in {"centroids": (0, (nlist, a.dim), np.float32),
-                                        "codebooks": (1, (m_pq, 256, a.dim // m_pq), np.float32),
-                                        "pq_codes": (2, (a.n, m_pq), np.uint8), "offsets": (6, (nlist + 1,), np.uint32),
-                                        "vec_ids": (7, (a.n,), np.uint32)}.items():
+        t = {"nlist": nlist, "padded_dim": P}
+        spec = {"centroids": (0, (nlist, a.dim), np.float32), "offsets": (6, (nlist + 1,), np.uint32),
+                "vec_ids": (7, (a.n,), np.uint32)}
+        if rq:
+            spec.update({"rot_signs": (8, (3 * P,), np.float32), "rot_centroids": (9, (nlist, P), np.float32),
+                         "rabitq_bits": (10, (a.n, P // 32), np.uint32), "rabitq_meta": (11, (a.n, 4), np.float32)})
+        else:
+            spec.update({"codebooks": (1, (m_pq, 256, a.dim // m_pq), np.float32),
+                         "pq_codes": (2, (a.n, m_pq), np.uint8)})
+        cpu_search = oracle.ivf_rabitq_search if rq else oracle.ivf_pq_search
+        for key, (table, shape, dt) in spec.items():
             arr = np.zeros(shape, dtype=dt)
             _lib.call("fv_index_export_ivf", idx._h, table, arr.ctypes.data_as(C.c_void_p), arr.nbytes)
             t[key] = arr
         rows_np = rows.cpu().numpy()
         qs_np = q[:threads].cpu().numpy()
         t0 = time.perf_counter()
-        oracle.ivf_pq_search(t, rows_np, qs_np, a.k, head, rerank, mask=words, threads=threads)
+        cpu_search(t, rows_np, qs_np, a.k, head, rerank, mask=words, threads=threads)
         per = (time.perf_counter() - t0) / qs_np.shape[0]
         nsamp = int(max(threads, min(a.batch, a.cpu_seconds / max(per, 1e-9)))) // threads * threads
         qs_np = q[:nsamp].cpu().numpy()
         t0 = time.perf_counter()
-        ref_out = oracle.ivf_pq_search(t, rows_np, qs_np, a.k, head, rerank, mask=words, threads=threads)
+        ref_out = cpu_search(t, rows_np, qs_np, a.k, head, rerank, mask=words, threads=threads)
         cdt = time.perf_counter() - t0
         same = bool(np.array_equal(ref_out["id"], out.cpu().numpy()[:nsamp, :, 0].view(np.uint32)))
         cpu = {"value": nsamp / cdt, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{nsamp} queries, the reference's IVF-PQ search restated (nprobe {head}, rerank {rerank}) "
+               "sample": f"{nsamp} queries, the reference's IVF-{'RaBitQ' if rq else 'PQ'} search restated "
+                         f"(nprobe {head}, rerank {rerank}) "
                          f"over the engine's tables, {cdt:.1f} s; ids equal to the GPU's: {same}"}
     h = sweep[head]
-    kname = "ivf_pq_scan"
+    kname = "ivf_rabitq_scan" if rq else "ivf_pq_scan"
     kms = prof[kname]["ms"] / prof[kname]["launches"]
-    achieved = h["scanned_entries_per_batch"] * (m_pq + 4) / (kms / 1e3) / 1e9
+    achieved = h["scanned_entries_per_batch"] * (row_bytes + 4) / (kms / 1e3) / 1e9
     peak = peaks.get("hbm_gbs", 6800.0)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None, "kernel": kname, "kernel_ms": kms,
-            "algorithmic_bytes": "sum over queries of probed list lengths x (32-byte code + 4-byte id)",
+            "algorithmic_bytes": "sum over queries of probed list lengths x (" +
+                                 ("16-byte sign bits + 16-byte meta" if rq else "32-byte code") + " + 4-byte id)",
             "peak_source": f"{peak_kind} STREAM copy"}
-    cfg = {"workload": "IVF-PQ, Zipf(1.1) list lengths (min 64), persistent query-queue scan, CUDA graph",
-           "N": a.n, "dim": a.dim, "nlist": nlist, "m_pq": m_pq, "batch": a.batch, "k": a.k, "rerank": rerank,
+    cfg = {"workload": ("IVF-RaBitQ" if rq else "IVF-PQ") +
+                       ", Zipf(1.1) list lengths (min 64), persistent query-queue scan, CUDA graph",
+           "N": a.n, "dim": a.dim, "nlist": nlist, "batch": a.batch, "k": a.k, "rerank": rerank,
            "nprobe": head, "mask_valid_fraction": 0.10, "list_lengths": hist, "build_seconds": build_s,
-           "l2": "inputs larger than L2 (320 MB of codes + 40 MB ids)"}
+           "l2": f"inputs larger than L2 ({a.n * row_bytes / 1e6:.0f} MB of codes + {a.n * 4 / 1e6:.0f} MB ids)"}
+    if rq:
+        cfg["padded_dim"] = P
+    else:
+        cfg["m_pq"] = m_pq
     _line(a, world, h["qps"], UNIT, h["ms_per_batch"] * a.steps / 1e3,
           {"value": a.batch * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": a.batch * a.dim * 4 + words.nbytes,
-           "d2h_bytes_per_step": a.batch * a.k * 8}, h["launches"], roof, _kernels(prof), None, cpu, "f32+u8", cfg,
+           "d2h_bytes_per_step": a.batch * a.k * 8}, h["launches"], roof, _kernels(prof), None, cpu,
+          "f32+u32" if rq else "f32+u8", cfg,
           recall_at_10=h["recall_at_10"], recall_sample=nsub, nprobe_sweep=sweep)
 
 

@@ -370,6 +370,55 @@ int fv_ivf_sq_search_ex(const IvfSqGpuTables* tables, const FvIvfOptions* option
   return ivf_sq(tables, options, d_queries, num_queries, top_k, nprobe, rerank_k, metric, d_valid_mask,
                 d_out_results, stream);
 }
+namespace {
+int ivf_rabitq(const IvfRabitqGpuTables* t, const FvIvfOptions* o, const float* q, uint32_t nq, uint32_t top_k,
+               uint32_t nprobe, uint32_t rerank_k, MetricType metric, const uint32_t* mask, GpuSearchResult* out,
+               void* stream) {
+  if (!t || !q || !out) return FV_ERR_NULL;
+  if (nq == 0 || top_k == 0 || t->nlist == 0 || t->padded_dim == 0) return 0;
+  if (!t->d_centroids || !t->d_rot_centroids || !t->d_rabitq_bits || !t->d_rabitq_meta || !t->d_rot_signs ||
+      !t->d_ivf_offsets || !t->d_ivf_vec_ids)
+    return FV_ERR_NULL;
+  if (t->words_per_vec * 32 != t->padded_dim) return FV_ERR_ARG;
+  fv::IvfLaunch L{};
+  L.centroids = t->d_centroids;
+  L.offsets = t->d_ivf_offsets;
+  L.vec_ids = t->d_ivf_vec_ids;
+  L.vectors = t->d_vectors;
+  L.num_vectors = t->num_vectors;
+  L.dim = t->dim;
+  L.nlist = t->nlist;
+  L.list_major = o && o->codes_list_major;
+  L.queries = q;
+  L.nq = nq;
+  L.top_k = top_k;
+  L.nprobe = nprobe;
+  L.rerank_k = rerank_k;
+  L.metric = metric;
+  L.mask = mask;
+  L.out = out;
+  L.rot_centroids = t->d_rot_centroids;
+  L.rq_bits = t->d_rabitq_bits;
+  L.rq_meta = t->d_rabitq_meta;
+  L.rot_signs = t->d_rot_signs;
+  L.padded_dim = t->padded_dim;
+  return fv::launch_ivf_search(fv::IVF_MODE_RABITQ, L, (cudaStream_t)stream);
+}
+}  // namespace
+
+int cuda_ivf_rabitq_search_batch(const IvfRabitqGpuTables* tables, const float* d_queries, uint32_t num_queries,
+                                 uint32_t top_k, uint32_t nprobe, uint32_t rerank_k, MetricType metric,
+                                 const uint32_t* d_valid_mask, GpuSearchResult* d_out_results, void* stream) {
+  return ivf_rabitq(tables, nullptr, d_queries, num_queries, top_k, nprobe, rerank_k, metric, d_valid_mask,
+                    d_out_results, stream);
+}
+int fv_ivf_rabitq_search_ex(const IvfRabitqGpuTables* tables, const FvIvfOptions* options, const float* d_queries,
+                            uint32_t num_queries, uint32_t top_k, uint32_t nprobe, uint32_t rerank_k,
+                            MetricType metric, const uint32_t* d_valid_mask, GpuSearchResult* d_out_results,
+                            void* stream) {
+  return ivf_rabitq(tables, options, d_queries, num_queries, top_k, nprobe, rerank_k, metric, d_valid_mask,
+                    d_out_results, stream);
+}
 int fv_ivf_relayout_codes(const uint8_t* d_codes_by_id, const uint32_t* d_ivf_vec_ids, uint32_t num_vectors,
                           uint32_t row_bytes, uint8_t* d_out_by_list, void* stream) {
   if (num_vectors && (!d_codes_by_id || !d_ivf_vec_ids || !d_out_by_list)) return FV_ERR_NULL;
@@ -402,6 +451,23 @@ int fv_build_ivf_lists(const GpuSearchResult* d_assign, uint32_t num_vectors, ui
   uint32_t* work = static_cast<uint32_t*>(fv::scratch_get(s, (size_t)nlist * 4));
   if (!work) return (int)cudaErrorMemoryAllocation;
   return fv::launch_build_lists(d_assign, num_vectors, nlist, d_out_offsets, d_out_vec_ids, work, s);
+}
+
+uint32_t fv_rabitq_padded_dim(uint32_t dim) { return fv::rabitq_padded_dim(dim); }
+
+void fv_rabitq_rot_signs(uint32_t padded_dim, uint64_t seed, float* host_out) {
+  if (host_out) fv::rabitq_rot_signs(padded_dim, seed, host_out);
+}
+
+int fv_build_rabitq(const float* d_vectors, uint32_t num_vectors, uint32_t dim, const float* d_centroids,
+                    uint32_t nlist, const GpuSearchResult* d_assign, const float* d_rot_signs, uint32_t padded_dim,
+                    float* d_out_rot_centroids, uint32_t* d_out_bits, float* d_out_meta, void* stream) {
+  if (!d_rot_signs || (nlist && (!d_centroids || !d_out_rot_centroids)) ||
+      (num_vectors && (!d_vectors || !d_assign || !d_out_bits || !d_out_meta)))
+    return FV_ERR_NULL;
+  if (dim == 0) return FV_ERR_ARG;
+  return fv::launch_rabitq_encode(d_vectors, num_vectors, dim, d_centroids, nlist, d_assign, d_rot_signs, padded_dim,
+                                  d_out_rot_centroids, d_out_bits, d_out_meta, (cudaStream_t)stream);
 }
 
 // ------------------------------------------------------------ CUDA graphs

@@ -97,6 +97,12 @@ uint64_t splitmix(uint64_t& s) {
   return z ^ (z >> 31);
 }
 
+// the reference's build: fp16 rows and the IVF-PQ, IVF-SQ8 and RaBitQ
+// tables (index.rs:404-445)
+constexpr uint32_t kDefaultBuild = FV_BUILD_FP16 | FV_BUILD_IVF_PQ | FV_BUILD_IVF_SQ8 | FV_BUILD_IVF_RABITQ;
+// RabitqEncoder::encode seed of the engine build (index.rs:435-441)
+constexpr uint64_t kRabitqSeed = 0x5F3759DFCAFEBABEull;
+
 // `count` distinct indices of [0, n) (Floyd's algorithm), ascending.
 std::vector<uint32_t> sample_rows(uint32_t n, uint32_t count, uint64_t seed) {
   count = std::min(count, n);
@@ -154,7 +160,7 @@ struct Delta {
 class Index {
  public:
   explicit Index(const FvIndexConfig& c) : cfg_(c), start_(std::chrono::steady_clock::now()) {
-    if (cfg_.build_flags == 0) cfg_.build_flags = FV_BUILD_FP16 | FV_BUILD_IVF_PQ | FV_BUILD_IVF_SQ8;
+    if (cfg_.build_flags == 0) cfg_.build_flags = kDefaultBuild;
     if (cfg_.kmeans_iters == 0) cfg_.kmeans_iters = 10;
     if (cfg_.pq_iters == 0) cfg_.pq_iters = 10;
     const uint32_t ns = cfg_.streams ? cfg_.streams : 4;
@@ -192,6 +198,7 @@ class Index {
   void info(FvIndexInfo* i);
   int export_ivf(uint32_t what, void* host_out, size_t bytes);
   int tables(IvfPqGpuTables* pq, IvfSqGpuTables* sq, FvIvfOptions* opt);
+  int rabitq_tables(IvfRabitqGpuTables* t, FvIvfOptions* opt);
 
   // served batches (serve.cpp)
   void pin() {
@@ -222,6 +229,19 @@ class Index {
   int upload_delta_live(cudaStream_t s);
   int build_from(const float* src, uint32_t n, bool device, const float* d_init_centroids);
   int build_ivf(cudaStream_t s, const float* d_init_centroids);
+  int build_rabitq(const GpuSearchResult* assign, cudaStream_t s);
+  // list-major copies of the id-indexed bits / meta (`entries` list positions)
+  int rabitq_list_major(uint32_t P, uint32_t entries, cudaStream_t s) {
+    int rc = rq_bits_lm_.alloc((size_t)entries * (P / 32));
+    if (!rc) rc = rq_meta_lm_.alloc((size_t)entries * 4);
+    if (!rc)
+      rc = launch_relayout_codes(reinterpret_cast<const uint8_t*>(rq_bits_.p), vec_ids_.p, entries, P / 8,
+                                 reinterpret_cast<uint8_t*>(rq_bits_lm_.p), s);
+    if (!rc)
+      rc = launch_relayout_codes(reinterpret_cast<const uint8_t*>(rq_meta_.p), vec_ids_.p, entries, 16,
+                                 reinterpret_cast<uint8_t*>(rq_meta_lm_.p), s);
+    return rc;
+  }
   int kmeans(const float* d_x, uint32_t n, uint32_t dim, uint32_t k, uint32_t iters, uint64_t seed, float* d_cent,
              cudaStream_t s, const float* d_init = nullptr);
   int assign_rows(const float* d_x, uint32_t n, uint32_t dim, const float* d_cent, uint32_t k, GpuSearchResult* out,
@@ -246,6 +266,12 @@ class Index {
   DevBuf<float> centroids_, codebooks_, sq_mins_, sq_scales_;
   DevBuf<uint8_t> pq_codes_, pq_codes_lm_, sq_codes_, sq_codes_lm_;
   DevBuf<uint32_t> offsets_, vec_ids_;
+  // RaBitQ: padded dimension, rotation signs [3P], rotated centroids
+  // [nlist][P], sign bits [n][P/32] and meta [n][4] by id and list-major
+  uint32_t rq_pd_ = 0;
+  uint32_t list_entries_ = 0;  // posting-list entries (offsets[nlist])
+  DevBuf<float> rq_signs_, rq_cent_, rq_meta_, rq_meta_lm_;
+  DevBuf<uint32_t> rq_bits_, rq_bits_lm_;
   DevBuf<uint32_t> valid_words_;
   std::vector<uint32_t> main_valid_;
   std::unordered_set<uint32_t> tombstones_;
@@ -307,6 +333,7 @@ int Index::kmeans(const float* d_x, uint32_t n, uint32_t dim, uint32_t k, uint32
 int Index::build_ivf(cudaStream_t s, const float* d_init_centroids) {
   const uint32_t dim = cfg_.dim;
   nlist_ = std::max(1u, std::min(cfg_.nlist, n_));
+  list_entries_ = n_;
   if (d_init_centroids && nlist_ != cfg_.nlist) return FV_ERR_ARG;
   uint32_t train = cfg_.train_rows ? cfg_.train_rows : (uint32_t)std::min<uint64_t>(n_, 256ull * nlist_);
   train = std::max(std::min(train, n_), nlist_);
@@ -380,7 +407,33 @@ int Index::build_ivf(cudaStream_t s, const float* d_init_centroids) {
     if (!rc) rc = launch_relayout_codes(sq_codes_.p, vec_ids_.p, n_, dim, sq_codes_lm_.p, s);
     if (rc) return rc;
   }
+  if (cfg_.build_flags & FV_BUILD_IVF_RABITQ) {
+    rc = build_rabitq(assign.p, s);
+    if (rc) return rc;
+  }
   return (int)cudaStreamSynchronize(s);
+}
+
+// RaBitQ tables of the built rows (index.rs:435-441: the engine's seed, the
+// rows' own coarse assignment), plus list-major copies of bits and meta.
+int Index::build_rabitq(const GpuSearchResult* assign, cudaStream_t s) {
+  const uint32_t dim = cfg_.dim, P = rabitq_padded_dim(dim), W = P / 32;
+  if (P > 4096) return 0;
+  std::vector<float> signs(3 * (size_t)P);
+  rabitq_rot_signs(P, kRabitqSeed, signs.data());
+  int rc = rq_signs_.alloc(signs.size());
+  if (!rc) rc = rq_cent_.alloc((size_t)nlist_ * P);
+  if (!rc) rc = rq_bits_.alloc((size_t)n_ * W);
+  if (!rc) rc = rq_meta_.alloc((size_t)n_ * 4);
+  if (!rc) rc = (int)cudaMemcpyAsync(rq_signs_.p, signs.data(), signs.size() * 4, cudaMemcpyHostToDevice, s);
+  if (!rc)
+    rc = launch_rabitq_encode(vectors_.p, n_, dim, centroids_.p, nlist_, assign, rq_signs_.p, P, rq_cent_.p,
+                              rq_bits_.p, rq_meta_.p, s);
+  if (!rc) rc = rabitq_list_major(P, list_entries_, s);
+  if (!rc) rc = (int)cudaStreamSynchronize(s);  // `signs` is freed on return
+  if (rc) return rc;
+  rq_pd_ = P;
+  return 0;
 }
 
 int Index::build_from(const float* host, uint32_t n, bool device, const float* d_init_centroids) {
@@ -412,6 +465,7 @@ int Index::build_from(const float* host, uint32_t n, bool device, const float* d
     src = host;
   }
   n_ = n;
+  rq_pd_ = 0;
   int rc = vectors_.alloc((size_t)n * dim);
   if (rc) return rc;
   rc = (int)cudaMemcpyAsync(vectors_.p, src, (size_t)n * dim * 4,
@@ -432,7 +486,7 @@ int Index::build_from(const float* host, uint32_t n, bool device, const float* d
     if (!rc) rc = launch_encode_fp8(vectors_.p, n, dim, pd8_, fp8_.p, fp8_scales_.p, fp8_norms_.p, s);
     if (rc) return rc;
   }
-  if (cfg_.nlist && (cfg_.build_flags & (FV_BUILD_IVF_PQ | FV_BUILD_IVF_SQ8))) {
+  if (cfg_.nlist && (cfg_.build_flags & (FV_BUILD_IVF_PQ | FV_BUILD_IVF_SQ8 | FV_BUILD_IVF_RABITQ))) {
     rc = build_ivf(s, d_init_centroids);
     if (rc) return rc;
   }
@@ -657,6 +711,16 @@ int Index::search(const FvSearchParams& p, const float* q, uint32_t nq, bool dev
                                st.s);
       break;
     }
+    case FV_ENGINE_IVF_RABITQ: {
+      if (!rq_pd_) return FV_ERR_ARG;
+      IvfRabitqGpuTables t{centroids_.p, rq_cent_.p, rq_bits_lm_.p, rq_meta_lm_.p, rq_signs_.p, offsets_.p,
+                           vec_ids_.p,   vectors_.p, n_,          dim,           rq_pd_,      rq_pd_ / 32,
+                           nlist_};
+      FvIvfOptions o{1, {0, 0, 0}};
+      rc = fv_ivf_rabitq_search_ex(&t, &o, d_q, nq, k, p.nprobe, p.rerank_k, (MetricType)cfg_.metric, d_mask,
+                                   st.res.p, st.s);
+      break;
+    }
     default:
       return FV_ERR_ARG;
   }
@@ -873,6 +937,7 @@ int Index::load_snapshot(const snap::File& f, std::string* error) {
 
   // IVF tables (ids in the lists are slots: mapped to logical ids)
   nlist_ = 0;
+  rq_pd_ = 0;
   uint64_t cb = 0, ob = 0, ib = 0;
   const uint8_t* cent = f.section("ivf_centroids", &cb);
   const uint8_t* offs = f.section("ivf_offsets", &ob);
@@ -920,6 +985,37 @@ int Index::load_snapshot(const snap::File& f, std::string* error) {
       if (!rc) rc = launch_relayout_codes(by_slot.p, slot_ids.p, (uint32_t)n, dim, sq_codes_lm_.p, s);
       if (!rc) rc = place_rows(scodes, dim, sq_codes_);
       if (!rc) rc = (int)cudaStreamSynchronize(s);
+      if (rc) return rc;
+    }
+    // RaBitQ: the file's tables when present and consistent, else encoded
+    // here from the rows and their lists
+    list_entries_ = (uint32_t)n;
+    uint64_t rsb = 0, rcb = 0, rbb = 0, rmb = 0;
+    const uint8_t* rsig = f.section("rabitq_signs", &rsb);
+    const uint8_t* rcen = f.section("rabitq_centroids", &rcb);
+    const uint8_t* rbits = f.section("rabitq_bits", &rbb);
+    const uint8_t* rmeta = f.section("rabitq_meta", &rmb);
+    const uint64_t P = m.rabitq_padded_dim;
+    if (P >= 32 && P <= 4096 && (P & (P - 1)) == 0 && P >= dim && rsig && rcen && rbits && rmeta &&
+        rsb == 3 * P * 4 && rcb == (uint64_t)m.nlist * P * 4 && rbb == n * (P / 8) && rmb == n * 16) {
+      rc = upload(rq_signs_, rsig, rsb, s);
+      if (!rc) rc = upload(rq_cent_, rcen, rcb, s);
+      if (!rc) rc = place_rows(rbits, P / 8, rq_bits_);
+      if (!rc) rc = place_rows(rmeta, 16, rq_meta_);
+      if (!rc) rc = rabitq_list_major((uint32_t)P, (uint32_t)n, s);
+      if (!rc) rc = (int)cudaStreamSynchronize(s);
+      if (rc) return rc;
+      rq_pd_ = (uint32_t)P;
+    } else if ((cfg_.build_flags & FV_BUILD_IVF_RABITQ) && rabitq_padded_dim(dim) <= 4096) {
+      std::vector<GpuSearchResult> assign(nslots, GpuSearchResult{0xFFFFFFFFu, 0.f});
+      const uint32_t* o = reinterpret_cast<const uint32_t*>(offs);
+      for (uint32_t l = 0; l < m.nlist; ++l)
+        for (uint32_t i = o[l]; i < o[l + 1] && i < n; ++i) assign[mapped[i]].id = l;
+      DevBuf<GpuSearchResult> d_assign;
+      rc = d_assign.alloc(nslots);
+      if (!rc)
+        rc = (int)cudaMemcpyAsync(d_assign.p, assign.data(), nslots * sizeof(GpuSearchResult), cudaMemcpyHostToDevice, s);
+      if (!rc) rc = build_rabitq(d_assign.p, s);
       if (rc) return rc;
     }
   }
@@ -974,10 +1070,10 @@ int Index::save_snapshot(const char* path, std::string* error) {
     host.resize(buf.n);
     return buf.n ? (int)cudaMemcpy(host.data(), buf.p, buf.bytes(), cudaMemcpyDeviceToHost) : 0;
   };
-  std::vector<float> vecs, cent, books, mins, scales, norms;
+  std::vector<float> vecs, cent, books, mins, scales, norms, rsig, rcen, rmeta;
   std::vector<uint16_t> f16;
   std::vector<uint8_t> pq, sq;
-  std::vector<uint32_t> offs, vids;
+  std::vector<uint32_t> offs, vids, rbits;
   int rc = d2h(vectors_, vecs);
   if (!rc) rc = d2h(centroids_, cent);
   if (!rc) rc = d2h(codebooks_, books);
@@ -989,6 +1085,12 @@ int Index::save_snapshot(const char* path, std::string* error) {
   if (!rc) rc = d2h(sq_codes_, sq);
   if (!rc) rc = d2h(fp16_, f16);
   if (!rc) rc = d2h(norms16_, norms);
+  if (!rc && rq_pd_) {
+    rc = d2h(rq_signs_, rsig);
+    if (!rc) rc = d2h(rq_cent_, rcen);
+    if (!rc) rc = d2h(rq_bits_, rbits);
+    if (!rc) rc = d2h(rq_meta_, rmeta);
+  }
   if (rc) return rc;
   std::vector<uint32_t> ids(n_);
   for (uint32_t i = 0; i < n_; ++i) ids[i] = i;
@@ -1004,13 +1106,13 @@ int Index::save_snapshot(const char* path, std::string* error) {
   m.metric = cfg_.metric;
   m.num_vectors = n_;
   m.fp16_padded_dim = fp16_.n ? pd16_ : 0;
+  m.rabitq_padded_dim = rq_pd_;
   m.next_logical_id = next_id_;
   auto sec = [](const char* name, const char* dtype, const auto& v) {
     using T = typename std::decay<decltype(v[0])>::type;
     return snap::OutSection{name, dtype, (uint64_t)v.size(), v.data(), (uint64_t)v.size() * sizeof(T)};
   };
   const std::vector<uint32_t> none_u32;
-  const std::vector<float> none_f32;
   std::vector<snap::OutSection> out = {
       sec("vectors", "f32", vecs),          sec("logical_ids", "u32", ids),
       sec("main_valid_words", "u32", main_valid_), sec("hnsw_adjacency", "u32", none_u32),
@@ -1019,8 +1121,8 @@ int Index::save_snapshot(const char* path, std::string* error) {
       sec("pq_codes", "u8", pq),            sec("ivf_offsets", "u32", offs),
       sec("ivf_vec_ids", "u32", vids),      sec("sq_mins", "f32", mins),
       sec("sq_scales", "f32", scales),      sec("sq_codes", "u8", sq),
-      sec("rabitq_signs", "f32", none_f32), sec("rabitq_centroids", "f32", none_f32),
-      sec("rabitq_bits", "u32", none_u32),  sec("rabitq_meta", "f32", none_f32),
+      sec("rabitq_signs", "f32", rsig),     sec("rabitq_centroids", "f32", rcen),
+      sec("rabitq_bits", "u32", rbits),     sec("rabitq_meta", "f32", rmeta),
       sec("vectors_fp16", "u16", f16),      sec("vec_norms_sq", "f32", norms)};
   if (!tomb.empty()) out.push_back(sec("tombstones", "u32", tomb));
   if (delta_.len()) {
@@ -1041,7 +1143,7 @@ int Index::launch_batch(const BatchLaunch& b, cudaStream_t s) {
   if (b.nq == 0 || b.top_k == 0) return 0;
   if (b.top_k > 256) return FV_ERR_ARG;
   if (!b.d_queries || !b.d_out) return FV_ERR_NULL;
-  const bool ivf = b.engine == FV_ENGINE_IVF_PQ || b.engine == FV_ENGINE_IVF_SQ8;
+  const bool ivf = b.engine == FV_ENGINE_IVF_PQ || b.engine == FV_ENGINE_IVF_SQ8 || b.engine == FV_ENGINE_IVF_RABITQ;
   if (!ivf && (b.d_topk || b.d_nprobe || b.d_rerank)) return FV_ERR_ARG;
   const bool has_delta = delta_.len() > 0;
   if (has_delta && (!b.d_main || !b.d_delta)) return FV_ERR_NULL;
@@ -1065,9 +1167,10 @@ int Index::launch_batch(const BatchLaunch& b, cudaStream_t s) {
       break;
     }
     case FV_ENGINE_IVF_PQ:
-    case FV_ENGINE_IVF_SQ8: {
-      const bool pq = b.engine == FV_ENGINE_IVF_PQ;
-      if (pq ? !pq_codes_lm_.p : !sq_codes_lm_.p) return FV_ERR_ARG;
+    case FV_ENGINE_IVF_SQ8:
+    case FV_ENGINE_IVF_RABITQ: {
+      const bool pq = b.engine == FV_ENGINE_IVF_PQ, rq = b.engine == FV_ENGINE_IVF_RABITQ;
+      if (rq ? !rq_pd_ : pq ? !pq_codes_lm_.p : !sq_codes_lm_.p) return FV_ERR_ARG;
       IvfLaunch L{};
       L.centroids = centroids_.p;
       L.codebooks = pq ? codebooks_.p : nullptr;
@@ -1095,11 +1198,19 @@ int Index::launch_batch(const BatchLaunch& b, cudaStream_t s) {
       L.q_nprobe = b.d_nprobe;
       L.q_rerank = b.d_rerank;
       L.filters = b.d_filters;
+      if (rq) {
+        L.codes = nullptr;
+        L.rot_centroids = rq_cent_.p;
+        L.rq_bits = rq_bits_lm_.p;
+        L.rq_meta = rq_meta_lm_.p;
+        L.rot_signs = rq_signs_.p;
+        L.padded_dim = rq_pd_;
+      }
       if (nlist_ == 0 || (pq && cfg_.m_pq == 0)) {
         rc = launch_fill_sentinel(main_out, (size_t)nq * k, s);
         break;
       }
-      rc = launch_ivf_search(pq ? 0 : 1, L, s);
+      rc = launch_ivf_search(rq ? IVF_MODE_RABITQ : pq ? IVF_MODE_PQ : IVF_MODE_SQ8, L, s);
       break;
     }
     default:
@@ -1158,7 +1269,8 @@ void Index::info(FvIndexInfo* i) {
   i->device_bytes = vectors_.bytes() + fp16_.bytes() + norms16_.bytes() + fp8_.bytes() + fp8_scales_.bytes() +
                     fp8_norms_.bytes() + centroids_.bytes() + codebooks_.bytes() + pq_codes_.bytes() +
                     pq_codes_lm_.bytes() + sq_codes_.bytes() + sq_codes_lm_.bytes() + offsets_.bytes() +
-                    vec_ids_.bytes();
+                    vec_ids_.bytes() + rq_signs_.bytes() + rq_cent_.bytes() + rq_bits_.bytes() + rq_bits_lm_.bytes() +
+                    rq_meta_.bytes() + rq_meta_lm_.bytes();
 }
 
 // Device views of the IVF tables (list-major codes) for direct kernel calls.
@@ -1173,9 +1285,20 @@ int Index::tables(IvfPqGpuTables* pq, IvfSqGpuTables* sq, FvIvfOptions* opt) {
   return 0;
 }
 
+int Index::rabitq_tables(IvfRabitqGpuTables* t, FvIvfOptions* opt) {
+  std::shared_lock<std::shared_mutex> lk(state_mu_);
+  if (!built_ || !offsets_.p || !rq_pd_) return FV_ERR_ARG;
+  if (t) *t = IvfRabitqGpuTables{centroids_.p, rq_cent_.p, rq_bits_lm_.p, rq_meta_lm_.p, rq_signs_.p, offsets_.p,
+                                 vec_ids_.p,   vectors_.p, n_,          cfg_.dim,      rq_pd_,      rq_pd_ / 32,
+                                 nlist_};
+  if (opt) *opt = FvIvfOptions{1, {0, 0, 0}};
+  return 0;
+}
+
 // Copies one IVF table to the host (for checking the build against a CPU
 // restatement): 0 centroids, 1 codebooks, 2 pq codes (by id), 3 sq mins,
-// 4 sq scales, 5 sq codes (by id), 6 offsets, 7 vec ids.
+// 4 sq scales, 5 sq codes (by id), 6 offsets, 7 vec ids, 8 RaBitQ signs,
+// 9 rotated centroids, 10 RaBitQ bits (by id), 11 RaBitQ meta (by id).
 int Index::export_ivf(uint32_t what, void* host_out, size_t bytes) {
   std::shared_lock<std::shared_mutex> lk(state_mu_);
   const void* src = nullptr;
@@ -1189,6 +1312,10 @@ int Index::export_ivf(uint32_t what, void* host_out, size_t bytes) {
     case 5: src = sq_codes_.p; have = sq_codes_.bytes(); break;
     case 6: src = offsets_.p; have = offsets_.bytes(); break;
     case 7: src = vec_ids_.p; have = vec_ids_.bytes(); break;
+    case 8: src = rq_signs_.p; have = rq_signs_.bytes(); break;
+    case 9: src = rq_cent_.p; have = rq_cent_.bytes(); break;
+    case 10: src = rq_bits_.p; have = rq_bits_.bytes(); break;
+    case 11: src = rq_meta_.p; have = rq_meta_.bytes(); break;
     default: return FV_ERR_ARG;
   }
   if (!host_out || bytes < have) return FV_ERR_ARG;
@@ -1275,6 +1402,10 @@ int fv_index_ivf_tables(FvIndex* index, IvfPqGpuTables* pq, IvfSqGpuTables* sq, 
   if (!index) return FV_ERR_NULL;
   return index->impl.tables(pq, sq, options);
 }
+int fv_index_rabitq_tables(FvIndex* index, IvfRabitqGpuTables* rabitq, FvIvfOptions* options) {
+  if (!index) return FV_ERR_NULL;
+  return index->impl.rabitq_tables(rabitq, options);
+}
 int fv_index_export_ivf(FvIndex* index, uint32_t table, void* host_out, size_t bytes) {
   if (!index) return FV_ERR_NULL;
   return index->impl.export_ivf(table, host_out, bytes);
@@ -1307,7 +1438,7 @@ int fv_index_load_snapshot(const char* path, const FvIndexConfig* config, FvInde
   c.metric = m.metric;
   c.nlist = m.nlist;
   c.m_pq = m.m_pq;
-  if (c.build_flags == 0) c.build_flags = FV_BUILD_FP16 | FV_BUILD_IVF_PQ | FV_BUILD_IVF_SQ8;
+  if (c.build_flags == 0) c.build_flags = fv::kDefaultBuild;
   FvIndex* idx = nullptr;
   try {
     idx = new FvIndex(c);

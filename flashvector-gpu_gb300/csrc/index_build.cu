@@ -17,7 +17,15 @@
 //     distance with strict `<` (cluster.rs:257-282);
 //   * SQ8: per-dimension min / max (fp32 bit-pattern atomics), scale =
 //     range / 255 or 0 when range <= 1e-12, code = round-half-away(
-//     (r - min) / scale) clamped to [0, 255] (quant.rs:14-75).
+//     (r - min) / scale) clamped to [0, 255] (quant.rs:14-75);
+//   * RaBitQ: one warp per row, the row's residual rotated in shared memory
+//     (three rounds of sign flip, Walsh-Hadamard butterflies, 1/sqrt(P)
+//     scale), sign bits by warp ballot, |r|^2, |x|^2 and sum |rot r| summed
+//     sequentially by single lanes in the reference's order
+//     (quant.rs:156-234), so the tables equal the host encoder's bit for bit.
+#include <algorithm>
+#include <cmath>
+
 #include "../../include/fv_bridge.h"
 #include "common.cuh"
 #include "kernels.h"
@@ -230,6 +238,85 @@ __global__ void gather_byte_rows_kernel(const uint8_t* __restrict__ in, const ui
   }
 }
 
+constexpr int RQ_WARPS = 4;
+
+// RaBitQ encoder. bits == nullptr: rot_out row = rotation of x row (the
+// rotated centroids). Otherwise the residual of x row to centroid
+// assign[row] is rotated and its sign bits and meta written.
+__global__ void __launch_bounds__(RQ_WARPS * 32)
+    rabitq_encode_kernel(const float* __restrict__ x, uint32_t n, uint32_t dim, const float* __restrict__ centroids,
+                         uint32_t nlist, const GpuSearchResult* __restrict__ assign, const float* __restrict__ signs,
+                         uint32_t P, float scale, float* __restrict__ rot_out, uint32_t* __restrict__ bits,
+                         float* __restrict__ meta) {
+  extern __shared__ float rq_smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t W = P / 32;
+  float* buf = rq_smem + (size_t)warp * P;
+  for (uint32_t row = blockIdx.x * RQ_WARPS + warp; row < n; row += gridDim.x * RQ_WARPS) {
+    const float* v = x + (size_t)row * dim;
+    const float* ce = nullptr;
+    if (bits) {
+      const uint32_t c = assign[row].id;
+      if (c < nlist) ce = centroids + (size_t)c * dim;
+    }
+    for (uint32_t d = lane; d < P; d += 32) buf[d] = d < dim ? (ce ? __fsub_rn(__ldg(v + d), __ldg(ce + d)) : __ldg(v + d)) : 0.f;
+    __syncwarp();
+    float res_sq = 0.f, vec_sq = 0.f, abs_sum = 0.f;
+    if (bits) {
+      // res_norm_sq += r * r, vec_norm_sq += x * x in dimension order
+      if (lane == 0)
+        for (uint32_t d = 0; d < dim; ++d) res_sq = __fadd_rn(res_sq, __fmul_rn(buf[d], buf[d]));
+      if (lane == 1)
+        for (uint32_t d = 0; d < dim; ++d) {
+          const float xv = __ldg(v + d);
+          vec_sq = __fadd_rn(vec_sq, __fmul_rn(xv, xv));
+        }
+      __syncwarp();
+    }
+    for (int st = 0; st < 3; ++st) {
+      const float* sg = signs + (size_t)st * P;
+      for (uint32_t d = lane; d < P; d += 32) buf[d] = __fmul_rn(buf[d], __ldg(sg + d));
+      __syncwarp();
+      for (uint32_t h = 1; h < P; h <<= 1) {
+        for (uint32_t i = lane; i < P / 2; i += 32) {
+          const uint32_t x0 = ((i & ~(h - 1)) << 1) | (i & (h - 1));
+          const float a = buf[x0], b = buf[x0 + h];
+          buf[x0] = __fadd_rn(a, b);
+          buf[x0 + h] = __fsub_rn(a, b);
+        }
+        __syncwarp();
+      }
+      for (uint32_t d = lane; d < P; d += 32) buf[d] = __fmul_rn(buf[d], scale);
+      __syncwarp();
+    }
+    if (!bits) {
+      for (uint32_t d = lane; d < P; d += 32) rot_out[(size_t)row * P + d] = buf[d];
+      __syncwarp();
+      continue;
+    }
+    uint32_t pop = 0;
+    for (uint32_t w = 0; w < W; ++w) {
+      const uint32_t b = __ballot_sync(0xffffffffu, buf[w * 32 + lane] >= 0.f);
+      if (lane == 0) bits[(size_t)row * W + w] = b;
+      pop += __popc(b);
+    }
+    if (lane == 2)
+      for (uint32_t d = 0; d < P; ++d) abs_sum = __fadd_rn(abs_sum, fabsf(buf[d]));
+    res_sq = __shfl_sync(0xffffffffu, res_sq, 0);
+    vec_sq = __shfl_sync(0xffffffffu, vec_sq, 1);
+    abs_sum = __shfl_sync(0xffffffffu, abs_sum, 2);
+    if (lane == 0) {
+      const float rn = __fsqrt_rn(res_sq);
+      float* m = meta + (size_t)row * 4;
+      m[0] = res_sq;
+      m[1] = (rn > 1e-12f && abs_sum > 1e-12f) ? __fdiv_rn(__fmul_rn(rn, rn), abs_sum) : 0.f;
+      m[2] = (float)pop;
+      m[3] = vec_sq;
+    }
+    __syncwarp();
+  }
+}
+
 __global__ void fill_f32_kernel(float* p, size_t n, float v) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
 }
@@ -329,6 +416,55 @@ int launch_gather_row_bytes(const void* in, const uint32_t* rows, uint32_t count
         static_cast<const uint8_t*>(in), rows, count, row_bytes, zero_row, static_cast<uint8_t*>(out));
   }
   note_launch();
+  return (int)cudaGetLastError();
+}
+
+uint32_t rabitq_padded_dim(uint32_t dim) {
+  uint32_t p = 32;
+  while (p < dim) p <<= 1;
+  return p;
+}
+
+float rabitq_inv_sqrt(uint32_t padded_dim) { return 1.0f / std::sqrt((float)padded_dim); }
+
+// The reference's seeded sign generator (quant.rs:100-116): a splitmix64
+// stream whose state starts at seed ^ 0x9e3779b97f4a7c15; sign = -1 when
+// the output's low bit is set.
+void rabitq_rot_signs(uint32_t padded_dim, uint64_t seed, float* out) {
+  const uint64_t inc = 0x9e3779b97f4a7c15ull;
+  uint64_t st = seed ^ inc;
+  for (uint32_t i = 0; i < 3u * padded_dim; ++i) {
+    st += inc;
+    uint64_t z = st;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    z ^= z >> 31;
+    out[i] = (z & 1u) ? -1.0f : 1.0f;
+  }
+}
+
+int launch_rabitq_encode(const float* x, uint32_t n, uint32_t dim, const float* centroids, uint32_t nlist,
+                         const GpuSearchResult* assign, const float* signs, uint32_t padded_dim, float* rot_centroids,
+                         uint32_t* bits, float* meta, cudaStream_t stream) {
+  const uint32_t P = padded_dim;
+  if (P < 32 || P > 4096 || (P & (P - 1)) || P < dim) return FV_ERR_ARG;
+  const size_t smem = (size_t)RQ_WARPS * P * 4;
+  cudaError_t e = cudaFuncSetAttribute(rabitq_encode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  const float scale = rabitq_inv_sqrt(P);
+  const uint32_t cap = (uint32_t)device_sm_count() * 16;
+  if (nlist) {
+    const uint32_t blocks = std::max(1u, std::min(cap, (nlist + RQ_WARPS - 1) / RQ_WARPS));
+    rabitq_encode_kernel<<<blocks, RQ_WARPS * 32, smem, stream>>>(centroids, nlist, dim, nullptr, 0, nullptr, signs, P,
+                                                                   scale, rot_centroids, nullptr, nullptr);
+    note_launch();
+  }
+  if (n) {
+    const uint32_t blocks = std::max(1u, std::min(cap, (n + RQ_WARPS - 1) / RQ_WARPS));
+    rabitq_encode_kernel<<<blocks, RQ_WARPS * 32, smem, stream>>>(x, n, dim, centroids, nlist, assign, signs, P, scale,
+                                                                   nullptr, bits, meta);
+    note_launch();
+  }
   return (int)cudaGetLastError();
 }
 

@@ -1,8 +1,9 @@
-// ivf.cu -- IVF-PQ and IVF-SQ8 inverted-list scans.
+// ivf.cu -- IVF-PQ, IVF-SQ8 and IVF-RaBitQ inverted-list scans.
 //
-// Replaces launch_ivf_pq_search / launch_ivf_sq_search and their kernels
-// (ivf_pq_lookup.cu:14-444, ivf_quant_lookup.cu:18-327, ivf_rerank.cuh:49-160)
-// with the same inputs, clamps and result semantics:
+// Replaces launch_ivf_pq_search / launch_ivf_sq_search /
+// launch_ivf_rabitq_search and their kernels (ivf_pq_lookup.cu:14-444,
+// ivf_quant_lookup.cu:18-870, ivf_rerank.cuh:49-160) with the same inputs,
+// clamps and result semantics:
 //   * top_k <= 256; nprobe clamped to [1, nlist];
 //     shortlist = rerank_k ? rerank_k : top_k, >= top_k, <= 10240;
 //     exact rerank when rerank_k != 1 and fp32 rows are present;
@@ -14,6 +15,12 @@
 //     the LUT entries of a row's codes added in sub-space order (:176-178);
 //     SQ8: sum_d fmaf over (q - centroid) - fmaf(code, scale, min)
 //     (ivf_quant_lookup.cu:83-87), L2 whatever the metric;
+//     RaBitQ: the query rotated once per query (three rounds of sign flip,
+//     Walsh-Hadamard butterflies, 1/sqrt(P) scale: ivf_quant_lookup.cu:
+//     337-376), per (query, list) its rotated residual quantised to 4 bits
+//     over [min, max] as four bit-planes (:381-460), per posting the
+//     popcount estimate (:462-489) with its roundings fixed
+//     (rabitq_estimate below);
 //   * shortlist = the best `shortlist` (approx distance, id) keys; rerank
 //     with the reference's warp-order fp32 distance; the first top_k by
 //     (distance, id) are returned.
@@ -43,7 +50,7 @@ constexpr int IVF_THREADS = 256;
 constexpr uint32_t IVF_BUF = 1536;         // candidate buffer entries (>= 1.5 rounds of 1,024 postings)
 constexpr uint32_t MAX_SHORTLIST = 10240;  // reference clamp (ivf_rerank.cuh:12)
 
-enum IvfMode { IVF_PQ = 0, IVF_SQ8 = 1 };
+enum IvfMode { IVF_PQ = IVF_MODE_PQ, IVF_SQ8 = IVF_MODE_SQ8, IVF_RABITQ = IVF_MODE_RABITQ };
 
 struct IvfArgs {
   const float* centroids;   // [nlist][dim]
@@ -51,6 +58,7 @@ struct IvfArgs {
   const float* sq_mins;     // SQ8: [dim]
   const float* sq_scales;   // SQ8: [dim]
   const uint8_t* codes;     // [N][code_bytes] by id, or by list position when list_major
+                            // (RaBitQ: the sign bits, code_bytes = 4 W)
   const uint32_t* offsets;  // [nlist + 1]
   const uint32_t* vec_ids;  // [N] ids in list order
   const float* vectors;     // fp32 rows (rerank) or null
@@ -71,6 +79,12 @@ struct IvfArgs {
   uint32_t items_per_q;           // G: a query's probed postings are cut into G ranges
   uint64_t* partial;              // G > 1: [nq * G][part_stride] sorted shortlists of the ranges
   uint32_t part_stride;           // >= every query's shortlist
+  // RaBitQ
+  const float* rot_centroids;     // [nlist][P]
+  const float* rq_meta;           // [N][4] by id, or by list position when list_major
+  const float* rot_signs;         // [3][P]
+  uint32_t P, W;                  // rotated dimension (power of two), words of bits per row
+  float inv_sqrt_p;               // 1.0f / sqrtf(P), correctly rounded
 };
 
 // Rerank of a query's shortlist keys[0, S) (sorted, sentinels last) with the
@@ -110,16 +124,159 @@ __host__ __device__ __forceinline__ uint32_t ivf_clamps(uint32_t& top_k, uint32_
 }
 
 struct IvfSmem {
-  // [keys_pow2] u64 keys | LUT (PQ: m*256 f32) or residual+mins+scales (SQ8: 3*dim f32) | query (dim f32)
-  // | PQ: query residual to the probed centroid (dim f32)
-  static size_t bytes(int mode, uint32_t keys_pow2, uint32_t dim, uint32_t m_pq) {
+  // [keys_pow2] u64 keys | table | query (dim f32) | PQ: query residual to the probed centroid (dim f32)
+  // table: PQ LUT (m*256 f32); SQ8 residual+mins+scales (3*dim f32);
+  //        RaBitQ rotated query (P f32) + rotated residual (P f32) + bit-planes (4*W u32)
+  __host__ __device__ static size_t table_floats(int mode, uint32_t dim, uint32_t m_pq, uint32_t P) {
+    return mode == IVF_PQ ? (size_t)m_pq * 256 : mode == IVF_SQ8 ? (size_t)3 * dim : (size_t)2 * P + P / 8;
+  }
+  static size_t bytes(int mode, uint32_t keys_pow2, uint32_t dim, uint32_t m_pq, uint32_t P) {
     size_t b = (size_t)keys_pow2 * 8;
-    b += mode == IVF_PQ ? (size_t)m_pq * 256 * 4 : (size_t)3 * dim * 4;
+    b += table_floats(mode, dim, m_pq, P) * 4;
     b += (size_t)dim * 4;
     if (mode == IVF_PQ) b += (size_t)dim * 4;
     return b + 64;
   }
 };
+
+// RaBitQ: the query rotated into rq[0, P) (block-collective). The rounds of
+// the reference's rotation (sign flip; butterflies x + y, x - y at half
+// length 1, 2, ..., P/2; scale by 1/sqrt(P)) with each round's scale and
+// the next round's sign flip applied in one pass -- the same two roundings.
+__device__ void rabitq_rotate_query(float* rq, const float* qs, const IvfArgs& a) {
+  const int tid = threadIdx.x;
+  const uint32_t P = a.P;
+  for (uint32_t d = tid; d < P; d += IVF_THREADS) rq[d] = __fmul_rn(d < a.dim ? qs[d] : 0.f, __ldg(a.rot_signs + d));
+  __syncthreads();
+  for (int st = 0; st < 3; ++st) {
+    for (uint32_t h = 1; h < P; h <<= 1) {
+      for (uint32_t i = tid; i < P / 2; i += IVF_THREADS) {
+        const uint32_t x0 = ((i & ~(h - 1)) << 1) | (i & (h - 1));  // (i / h) * 2h + i % h
+        const float x = rq[x0], y = rq[x0 + h];
+        rq[x0] = __fadd_rn(x, y);
+        rq[x0 + h] = __fsub_rn(x, y);
+      }
+      __syncthreads();
+    }
+    const float* next = st < 2 ? a.rot_signs + (size_t)(st + 1) * P : nullptr;
+    for (uint32_t d = tid; d < P; d += IVF_THREADS) {
+      const float v = __fmul_rn(rq[d], a.inv_sqrt_p);
+      rq[d] = next ? __fmul_rn(v, __ldg(next + d)) : v;
+    }
+    __syncthreads();
+  }
+}
+
+// RaBitQ: the 4-bit code of the rotated query residual to list l
+// (ivf_quant_lookup.cu:381-460): diff = rq - rot_centroid over all P
+// coordinates, u = clamp(rint((diff - min) * (15 / range)), 0, 15) (all 0
+// when range <= 1e-12), bit-plane j word w bit l = bit j of u[32 w + l].
+// Writes planes[4][W]; returns (min, delta = range / 15, sum u) in s_par.
+// Block-collective.
+__device__ void rabitq_query_code(const float* rq, float* rdiff, uint32_t* planes, const IvfArgs& a, uint32_t l,
+                                  float* s_par) {
+  __shared__ float s_lo[IVF_THREADS / 32], s_hi[IVF_THREADS / 32];
+  __shared__ uint32_t s_sum;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const float* rc = a.rot_centroids + (size_t)l * a.P;
+  float lo = 1e30f, hi = -1e30f;
+  for (uint32_t d = tid; d < a.P; d += IVF_THREADS) {
+    const float v = __fsub_rn(rq[d], __ldg(rc + d));
+    rdiff[d] = v;
+    lo = fminf(lo, v);
+    hi = fmaxf(hi, v);
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if (lane == 0) {
+    s_lo[warp] = lo;
+    s_hi[warp] = hi;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int w = 1; w < IVF_THREADS / 32; ++w) {
+      lo = fminf(lo, s_lo[w]);
+      hi = fmaxf(hi, s_hi[w]);
+    }
+    const float range = __fsub_rn(hi, lo);
+    const bool live = range > 1e-12f;
+    s_par[0] = lo;
+    s_par[1] = live ? __fdiv_rn(range, 15.0f) : 0.f;
+    s_par[2] = live ? __fdiv_rn(15.0f, range) : 0.f;
+    s_sum = 0;
+  }
+  __syncthreads();
+  const float qmin = s_par[0], delta = s_par[1], inv = s_par[2];
+  uint32_t su = 0;
+  for (uint32_t w = warp; w < a.W; w += IVF_THREADS / 32) {
+    uint32_t u = 0;
+    if (delta > 0.f) {
+      const int qi = __float2int_rn(__fmul_rn(__fsub_rn(rdiff[w * 32 + lane], qmin), inv));
+      u = (uint32_t)min(max(qi, 0), 15);
+    }
+    su += u;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t pj = __ballot_sync(0xffffffffu, (u >> j) & 1u);
+      if (lane == 0) planes[j * a.W + w] = pj;
+    }
+  }
+  su = __reduce_add_sync(0xffffffffu, su);
+  if (lane == 0 && su) atomicAdd(&s_sum, su);
+  __syncthreads();
+  if (tid == 0) s_par[3] = (float)s_sum;  // exact: sum u <= 15 * 4096
+  __syncthreads();
+}
+
+// RaBitQ estimate of one posting from s_bu = sum_j 2^j popc(bits & plane_j)
+// and its meta m = {|r|^2, rescale, popcount, |x|^2}
+// (ivf_quant_lookup.cu:462-489). The reference leaves the roundings to the
+// compiler; here they are fixed:
+//   t = fmaf(delta, 2 s_bu - sum_u, q_min * (2 popcount - P))
+//   est_l2 = (q_c + |r|^2) - 2 (rescale * t)
+//   IP: -0.5 ((|q|^2 + |x|^2) - est_l2); cosine: 0.5 est_l2.
+__device__ __forceinline__ float rabitq_estimate(uint32_t s_bu, float4 m, float P, float qmin, float delta,
+                                                 float sum_u, float qc, float qn, int metric) {
+  const float A = __fsub_rn(__fmul_rn(2.f, m.z), P);
+  const float B = __fsub_rn(__fmul_rn(2.f, (float)s_bu), sum_u);
+  const float t = __fmaf_rn(delta, B, __fmul_rn(qmin, A));
+  const float est = __fsub_rn(__fadd_rn(qc, m.x), __fmul_rn(2.f, __fmul_rn(m.y, t)));
+  if (metric == METRIC_INNER_PRODUCT) return __fmul_rn(-0.5f, __fsub_rn(__fadd_rn(qn, m.w), est));
+  if (metric == METRIC_COSINE) return __fmul_rn(0.5f, est);
+  return est;
+}
+
+// s_bu of a row of MW 16-byte words of bits held in registers
+template <int MW>
+__device__ __forceinline__ uint32_t rabitq_sbu(const uint32_t* planes, const uint4 (&b)[MW]) {
+  uint32_t acc = 0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    uint32_t c = 0;
+#pragma unroll
+    for (int w = 0; w < MW; ++w) {
+      const uint4 p = *reinterpret_cast<const uint4*>(planes + j * 4 * MW + 4 * w);
+      c += __popc(b[w].x & p.x) + __popc(b[w].y & p.y) + __popc(b[w].z & p.z) + __popc(b[w].w & p.w);
+    }
+    acc += c << j;
+  }
+  return acc;
+}
+
+// s_bu of a row read word by word (any W, any alignment)
+__device__ __forceinline__ uint32_t rabitq_sbu_any(const uint32_t* planes, const uint32_t* __restrict__ row,
+                                                   uint32_t W) {
+  uint32_t c[4] = {0, 0, 0, 0};
+  for (uint32_t w = 0; w < W; ++w) {
+    const uint32_t b = __ldg(row + w);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) c[j] += __popc(b & planes[j * W + w]);
+  }
+  return c[0] + (c[1] << 1) + (c[2] << 2) + (c[3] << 3);
+}
 
 // PQ: ADC of one row from its code bytes; LUT rows of 256 floats.
 __device__ __forceinline__ float adc_row(const float* __restrict__ lut, const uint8_t* __restrict__ row, uint32_t m_pq,
@@ -185,15 +342,16 @@ __device__ __forceinline__ float sq8_row(const float* __restrict__ qres, const f
   return s;
 }
 
-// MODE: PQ or SQ8. MW > 0: PQ codes of 16 * MW bytes at 16-byte-aligned
-// rows (m_pq = 16, 32, 64), scanned by the register-prefetching loop with R
-// postings per thread per round, software-pipelined across rounds (PIPE).
+// MODE: PQ, SQ8 or RaBitQ. MW > 0: code rows of 16 * MW bytes at 16-byte-
+// aligned rows (PQ m_pq = 16, 32, 64; RaBitQ P = 128 MW with 16-byte-aligned
+// meta rows), scanned by the register-prefetching loop with R postings per
+// thread per round, software-pipelined across rounds (PIPE).
 template <int MODE, int MW, int R = 4, bool PIPE = false>
 __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   uint64_t* keys = reinterpret_cast<uint64_t*>(smem);
   float* tab = reinterpret_cast<float*>(smem + (size_t)a.keys_pow2 * 8);
-  float* qs = tab + (MODE == IVF_PQ ? (size_t)a.m_pq * 256 : (size_t)3 * a.dim);
+  float* qs = tab + IvfSmem::table_floats(MODE, a.dim, a.m_pq, a.P);
   __shared__ uint32_t s_q, s_cnt;
   __shared__ uint64_t s_tau;
 
@@ -202,6 +360,11 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
   float* mins = tab + a.dim;      // SQ8 only
   float* scales = tab + 2 * a.dim;
   float* qres = qs + a.dim;       // PQ only: q - centroid of the probed list
+  float* rq = tab;                // RaBitQ only: rotated query, rotated residual, bit-planes
+  float* rdiff = tab + a.P;
+  uint32_t* planes = reinterpret_cast<uint32_t*>(tab + 2 * a.P);
+  __shared__ float s_par[4];      // RaBitQ: min, delta, 15 / range, sum u of the list's query code
+  __shared__ float s_red[IVF_THREADS];
   const bool cb4 = a.sub_dim == 4 && ((uintptr_t)a.codebooks % 16u) == 0;
 
   if (MODE == IVF_SQ8) {
@@ -244,6 +407,23 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
       s_total = total;
     }
     __syncthreads();
+    float qn = 0.f;  // RaBitQ, inner product: ||q||^2
+    if (MODE == IVF_RABITQ) {
+      if (a.metric == METRIC_INNER_PRODUCT) {
+        // in the order of the reference's 256-thread block
+        // (ivf_quant_lookup.cu:686-697): strided fmaf partials, pairwise fold
+        float part = 0.f;
+        for (uint32_t d = tid; d < a.dim; d += IVF_THREADS) part = __fmaf_rn(qs[d], qs[d], part);
+        s_red[tid] = part;
+        __syncthreads();
+        for (int st = IVF_THREADS / 2; st > 0; st >>= 1) {
+          if (tid < st) s_red[tid] = __fadd_rn(s_red[tid], s_red[tid + st]);
+          __syncthreads();
+        }
+        qn = s_red[0];
+      }
+      rabitq_rotate_query(rq, qs, a);
+    }
     // this item's range of the query's probed postings (lists in probe order)
     const uint64_t lo = G > 1 ? s_total * g / G : 0ull;
     const uint64_t hi = G > 1 ? s_total * (g + 1) / G : ~0ull;
@@ -301,10 +481,15 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
             tab[e] = s;
           }
         }
-      } else {
+      } else if (MODE == IVF_SQ8) {
         for (uint32_t d = tid; d < a.dim; d += IVF_THREADS) tab[d] = qs[d] - __ldg(cent + d);
+      } else {
+        rabitq_query_code(rq, rdiff, planes, a, l, s_par);
       }
       __syncthreads();
+      // RaBitQ: the list's query code and the query-to-centroid distance
+      const float qc = MODE == IVF_RABITQ ? a.probes[(size_t)q * a.nprobe + p].distance : 0.f;
+      const float qmin = s_par[0], qdelta = s_par[1], sum_u = s_par[3], Pf = (float)a.P;
 
       const uint32_t beg = lbeg + (uint32_t)(s0 - at), end = lbeg + (uint32_t)(s1 - at);
       auto offer = [&](float d, uint32_t vid) {
@@ -316,14 +501,14 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
           }
         }
       };
-      if (MODE == IVF_PQ && MW > 0) {
+      if (MODE != IVF_SQ8 && MW > 0) {
         // R postings per thread per round: ids and code rows of all of them
         // are loaded before any is scored. PIPE: the next round's loads are
         // issued before this round is scored, and its mask / filter words
         // after, so global-load latency overlaps the LUT arithmetic.
         constexpr int MWW = MW > 0 ? MW : 1;
         constexpr uint32_t step = IVF_THREADS * R;
-        auto issue = [&](uint32_t b0, uint32_t (&v)[R], uint4 (&c)[R][MWW]) {
+        auto issue = [&](uint32_t b0, uint32_t (&v)[R], uint4 (&c)[R][MWW], float4 (&mt)[R]) {
 #pragma unroll
           for (int r = 0; r < R; ++r) {
             const uint32_t i = b0 + r * IVF_THREADS + tid;
@@ -332,10 +517,18 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
 #pragma unroll
           for (int r = 0; r < R; ++r) {
             const uint32_t i = b0 + r * IVF_THREADS + tid;
-            const uint4* row = reinterpret_cast<const uint4*>(a.codes + (size_t)(a.list_major ? i : v[r]) * (16u * MW));
+            const size_t row_i = a.list_major ? i : v[r];
+            const uint4* row = reinterpret_cast<const uint4*>(a.codes + row_i * (16u * MW));
 #pragma unroll
             for (int j = 0; j < MWW; ++j) c[r][j] = i < end ? __ldg(row + j) : make_uint4(0u, 0u, 0u, 0u);
+            if (MODE == IVF_RABITQ)
+              mt[r] = i < end ? __ldg(reinterpret_cast<const float4*>(a.rq_meta) + row_i) : make_float4(0.f, 0.f, 0.f, 0.f);
           }
+        };
+        auto score = [&](const uint4 (&c)[MWW], const float4& mt) -> float {
+          if (MODE == IVF_RABITQ)
+            return rabitq_estimate(rabitq_sbu<MWW>(planes, c), mt, Pf, qmin, qdelta, sum_u, qc, qn, a.metric);
+          return adc_words<MWW>(tab, c);
         };
         auto admit = [&](const uint32_t (&v)[R], bool (&o)[R]) {
 #pragma unroll
@@ -344,37 +537,40 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
         };
         uint32_t vid[R];
         uint4 w[R][MWW];
+        float4 mt[R];
         bool ok[R];
         if (PIPE && beg < end) {
-          issue(beg, vid, w);
+          issue(beg, vid, w, mt);
           admit(vid, ok);
         }
         for (uint32_t base = beg; base < end; base += step) {
           if (PIPE) {
             uint32_t vn[R];
             uint4 wn[R][MWW];
+            float4 mn[R];
             bool okn[R];
             const bool more = base + step < end;  // uniform over the block
-            if (more) issue(base + step, vn, wn);
+            if (more) issue(base + step, vn, wn, mn);
 #pragma unroll
             for (int r = 0; r < R; ++r)
-              if (ok[r]) offer(adc_words<MWW>(tab, w[r]), vid[r]);
+              if (ok[r]) offer(score(w[r], mt[r]), vid[r]);
             if (more) {
               admit(vn, okn);
 #pragma unroll
               for (int r = 0; r < R; ++r) {
                 vid[r] = vn[r];
                 ok[r] = okn[r];
+                mt[r] = mn[r];
 #pragma unroll
                 for (int j = 0; j < MWW; ++j) w[r][j] = wn[r][j];
               }
             }
           } else {
-            issue(base, vid, w);
+            issue(base, vid, w, mt);
             admit(vid, ok);
 #pragma unroll
             for (int r = 0; r < R; ++r)
-              if (ok[r]) offer(adc_words<MWW>(tab, w[r]), vid[r]);
+              if (ok[r]) offer(score(w[r], mt[r]), vid[r]);
           }
           __syncthreads();
           if (s_cnt > IVF_BUF - step) flush();
@@ -385,9 +581,18 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
           if (i < end) {
             const uint32_t vid = __ldg(a.vec_ids + i);
             if (mask_allows(a.mask, vid) && filter_allows(qf, vid)) {
-              const uint8_t* row = a.codes + (size_t)(a.list_major ? i : vid) * a.code_bytes;
-              offer(MODE == IVF_PQ ? adc_row(tab, row, a.m_pq, vec16) : sq8_row(tab, mins, scales, row, a.dim, vec16),
-                    vid);
+              const size_t row_i = a.list_major ? i : vid;
+              const uint8_t* row = a.codes + row_i * a.code_bytes;
+              if (MODE == IVF_RABITQ) {
+                const float* mp = a.rq_meta + row_i * 4;
+                const float4 mt = make_float4(__ldg(mp), __ldg(mp + 1), __ldg(mp + 2), __ldg(mp + 3));
+                const uint32_t sbu = rabitq_sbu_any(planes, reinterpret_cast<const uint32_t*>(row), a.W);
+                offer(rabitq_estimate(sbu, mt, Pf, qmin, qdelta, sum_u, qc, qn, a.metric), vid);
+              } else {
+                offer(MODE == IVF_PQ ? adc_row(tab, row, a.m_pq, vec16)
+                                     : sq8_row(tab, mins, scales, row, a.dim, vec16),
+                      vid);
+              }
             }
           }
           __syncthreads();
@@ -448,6 +653,8 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   if (L.nq == 0 || L.top_k == 0 || L.nlist == 0) return 0;
   if (mode == IVF_PQ && L.m_pq == 0) return 0;
   if (L.dim == 0) return 0;
+  const uint32_t P = mode == IVF_RABITQ ? L.padded_dim : 0;
+  if (mode == IVF_RABITQ && (P < 32 || P > 4096 || (P & (P - 1)) || P < L.dim)) return FV_ERR_ARG;
   // uniform batch: the clamps of the call; heterogeneous batch: top_k,
   // nprobe and rerank_k are the batch maxima and bound every query's values
   uint32_t top_k = L.top_k, nprobe = L.nprobe;
@@ -500,7 +707,16 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   a.nlist = L.nlist;
   a.m_pq = L.m_pq;
   a.sub_dim = L.sub_dim;
-  a.code_bytes = mode == IVF_PQ ? L.m_pq : L.dim;
+  a.code_bytes = mode == IVF_PQ ? L.m_pq : mode == IVF_SQ8 ? L.dim : P / 8;
+  if (mode == IVF_RABITQ) {
+    a.codes = reinterpret_cast<const uint8_t*>(L.rq_bits);
+    a.rot_centroids = L.rot_centroids;
+    a.rq_meta = L.rq_meta;
+    a.rot_signs = L.rot_signs;
+    a.P = P;
+    a.W = P / 32;
+    a.inv_sqrt_p = rabitq_inv_sqrt(P);
+  }
   a.queries = L.queries;
   a.nq = L.nq;
   a.top_k = top_k;
@@ -522,7 +738,7 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   a.partial = partial;
   a.part_stride = shortlist;
 
-  const size_t smem = IvfSmem::bytes(mode, a.keys_pow2, L.dim, L.m_pq);
+  const size_t smem = IvfSmem::bytes(mode, a.keys_pow2, L.dim, L.m_pq, P);
   if (smem > 227 * 1024) return FV_ERR_ARG;
   const bool rows16 = mode == IVF_PQ && ((uintptr_t)L.codes % 16u) == 0;
   // "ivf.pipeline": 1 software-pipelines the PQ list scan (2 postings per
@@ -531,6 +747,16 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   // (60 registers, 4 postings per round) runs 4, which measured 7% faster.
   const bool pipe = tune_value("ivf.pipeline", 0) != 0;
   auto kern = ivf_scan_kernel<IVF_SQ8, 0>;
+  if (mode == IVF_RABITQ) {
+    // bits rows of P/8 bytes as 16-byte words when they and the meta rows
+    // are 16-byte aligned; R postings per thread per round as registers allow
+    const bool al = ((uintptr_t)L.rq_bits % 16u) == 0 && ((uintptr_t)L.rq_meta % 16u) == 0;
+    kern = ivf_scan_kernel<IVF_RABITQ, 0>;
+    if (al && P == 128) kern = ivf_scan_kernel<IVF_RABITQ, 1, 4>;
+    if (al && P == 256) kern = ivf_scan_kernel<IVF_RABITQ, 2, 2>;
+    if (al && P == 512) kern = ivf_scan_kernel<IVF_RABITQ, 4, 2>;
+    if (al && P == 1024) kern = ivf_scan_kernel<IVF_RABITQ, 8, 1>;
+  }
   if (mode == IVF_PQ) {
     kern = ivf_scan_kernel<IVF_PQ, 0>;
     if (rows16 && L.m_pq == 16) kern = pipe ? ivf_scan_kernel<IVF_PQ, 1, 2, true> : ivf_scan_kernel<IVF_PQ, 1>;
@@ -543,7 +769,7 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, IVF_THREADS, smem);
   const uint32_t grid = std::max(1u, std::min<uint32_t>(L.nq * G, (uint32_t)(std::max(1, per_sm) * sms)));
   {
-    ProfScope ps(mode == IVF_PQ ? "ivf_pq_scan" : "ivf_sq8_scan", stream);
+    ProfScope ps(mode == IVF_PQ ? "ivf_pq_scan" : mode == IVF_SQ8 ? "ivf_sq8_scan" : "ivf_rabitq_scan", stream);
     kern<<<grid, IVF_THREADS, smem, stream>>>(a);
     note_launch();
   }

@@ -141,8 +141,16 @@ struct IvfLaunch {
   const uint32_t* q_nprobe;
   const uint32_t* q_rerank;
   const QueryFilter* filters;
+  // RaBitQ: rotated centroids [nlist][P], sign bits [N][P/32] and meta
+  // [N][4] (by id, or by list position when list_major), rotation signs [3P]
+  const float* rot_centroids;
+  const uint32_t* rq_bits;
+  const float* rq_meta;
+  const float* rot_signs;
+  uint32_t padded_dim;
 };
-int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream);  // mode 0 = PQ, 1 = SQ8
+enum { IVF_MODE_PQ = 0, IVF_MODE_SQ8 = 1, IVF_MODE_RABITQ = 2 };
+int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream);
 int launch_relayout_codes(const uint8_t* by_id, const uint32_t* vec_ids, uint32_t n, uint32_t row_bytes,
                           uint8_t* by_list, cudaStream_t stream);
 
@@ -170,6 +178,14 @@ int launch_sq8_encode(const float* r, uint32_t n, uint32_t dim, const float* min
                       cudaStream_t stream);
 int launch_gather_rows(const float* x, const uint32_t* rows, uint32_t count, uint32_t dim, float* out,
                        cudaStream_t stream);
+// RaBitQ encoder: rotated centroids, sign bits and meta of every row's
+// rotated residual to its assigned centroid (inv_sqrt_p = 1 / sqrt(P))
+uint32_t rabitq_padded_dim(uint32_t dim);
+float rabitq_inv_sqrt(uint32_t padded_dim);
+void rabitq_rot_signs(uint32_t padded_dim, uint64_t seed, float* out);
+int launch_rabitq_encode(const float* x, uint32_t n, uint32_t dim, const float* centroids, uint32_t nlist,
+                         const GpuSearchResult* assign, const float* signs, uint32_t padded_dim, float* rot_centroids,
+                         uint32_t* bits, float* meta, cudaStream_t stream);
 int launch_fill_f32(float* p, size_t n, float v, cudaStream_t stream);
 // out row i = in row rows[i] (rows of row_bytes bytes), zeros where rows[i] == zero_row
 int launch_gather_row_bytes(const void* in, const uint32_t* rows, uint32_t count, uint32_t row_bytes,

@@ -89,7 +89,9 @@ struct ClassKey {
   }
 };
 
-bool is_ivf(uint32_t engine) { return engine == FV_ENGINE_IVF_PQ || engine == FV_ENGINE_IVF_SQ8; }
+bool is_ivf(uint32_t engine) {
+  return engine == FV_ENGINE_IVF_PQ || engine == FV_ENGINE_IVF_SQ8 || engine == FV_ENGINE_IVF_RABITQ;
+}
 
 // Staging layout of one batch of nq requests (one contiguous block, so one
 // copy each way): queries | top_k | nprobe | rerank_k | filters.
@@ -232,7 +234,7 @@ class Server {
   // ------------------------------------------------------------- submit
   int submit(const FvRequest* rq, const float* q, uint64_t arrival, uint64_t* ticket) {
     if (!rq || !q || !ticket) return FV_ERR_NULL;
-    if (rq->engine > FV_ENGINE_IVF_SQ8 || rq->top_k == 0 || rq->top_k > (uint32_t)kMaxTopK) return FV_ERR_ARG;
+    if (rq->engine > FV_ENGINE_IVF_RABITQ || rq->top_k == 0 || rq->top_k > (uint32_t)kMaxTopK) return FV_ERR_ARG;
     if (index_) {
       if (!index_built(index_)) return FV_ERR_ARG;
       if (is_ivf(rq->engine)) {

@@ -34,6 +34,12 @@ class IvfSqGpuTables(C.Structure):
                 ("d_ivf_vec_ids", P), ("d_vectors", P), ("num_vectors", U32), ("dim", U32), ("nlist", U32)]
 
 
+class IvfRabitqGpuTables(C.Structure):
+    _fields_ = [("d_centroids", P), ("d_rot_centroids", P), ("d_rabitq_bits", P), ("d_rabitq_meta", P),
+                ("d_rot_signs", P), ("d_ivf_offsets", P), ("d_ivf_vec_ids", P), ("d_vectors", P),
+                ("num_vectors", U32), ("dim", U32), ("padded_dim", U32), ("words_per_vec", U32), ("nlist", U32)]
+
+
 class Fp16GpuTables(C.Structure):
     _fields_ = [("d_vectors_fp16", P), ("d_vec_norms_sq", P), ("d_vectors", P), ("num_vectors", U32), ("dim", U32),
                 ("padded_dim", U32)]
@@ -124,10 +130,15 @@ SIGNATURES = {
     "cuda_ivf_sq_search_batch": (I32, [P, P, U32, U32, U32, U32, I32, P, P, P]),
     "fv_ivf_pq_search_ex": (I32, [P, P, P, U32, U32, U32, U32, I32, P, P, P]),
     "fv_ivf_sq_search_ex": (I32, [P, P, P, U32, U32, U32, U32, I32, P, P, P]),
+    "cuda_ivf_rabitq_search_batch": (I32, [P, P, U32, U32, U32, U32, I32, P, P, P]),
+    "fv_ivf_rabitq_search_ex": (I32, [P, P, P, U32, U32, U32, U32, I32, P, P, P]),
     "fv_ivf_relayout_codes": (I32, [P, P, U32, U32, P, P]),
     "fv_build_pq_encode": (I32, [P, U32, U32, U32, P, P, P]),
     "fv_build_sq8": (I32, [P, U32, U32, P, P, P, P]),
     "fv_build_ivf_lists": (I32, [P, U32, U32, P, P, P]),
+    "fv_rabitq_padded_dim": (U32, [U32]),
+    "fv_rabitq_rot_signs": (None, [U32, C.c_uint64, P]),
+    "fv_build_rabitq": (I32, [P, U32, U32, P, U32, P, P, U32, P, P, P, P]),
     "cuda_fp16_tc_search_batch": (I32, [P, P, U32, U32, I32, P, P, P]),
     "fv_fp16_search_batch_ex": (I32, [P, P, U32, U32, I32, P, P, P, P]),
     "fv_fp8_search_batch": (I32, [P, P, U32, U32, I32, P, P, P, P]),
@@ -144,6 +155,7 @@ SIGNATURES = {
     "fv_index_stats": (I32, [P, P]),
     "fv_index_info": (I32, [P, P]),
     "fv_index_ivf_tables": (I32, [P, P, P, P]),
+    "fv_index_rabitq_tables": (I32, [P, P, P]),
     "fv_index_export_ivf": (I32, [P, U32, P, SZ]),
     "fv_index_save_snapshot": (I32, [P, C.c_char_p]),
     "fv_index_load_snapshot": (I32, [C.c_char_p, P, P]),

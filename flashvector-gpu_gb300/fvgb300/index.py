@@ -22,8 +22,8 @@ from ._lib import call
 from .datasets import pack_bools
 
 METRIC = {"l2": 0, "cosine": 1, "ip": 2, "inner_product": 2}
-ENGINE = {"flat": 0, "fp16": 1, "fp8": 2, "pq": 3, "sq8": 4}
-BUILD_FP16, BUILD_FP8, BUILD_IVF_PQ, BUILD_IVF_SQ8 = 1, 2, 4, 8
+ENGINE = {"flat": 0, "fp16": 1, "fp8": 2, "pq": 3, "sq8": 4, "rabitq": 5}
+BUILD_FP16, BUILD_FP8, BUILD_IVF_PQ, BUILD_IVF_SQ8, BUILD_IVF_RABITQ = 1, 2, 4, 8, 16
 
 
 @dataclass
@@ -33,7 +33,7 @@ class IndexConfig:
     nlist: int = 256
     m_pq: int = 16
     metric: int | str = 0
-    build_flags: int = BUILD_FP16 | BUILD_IVF_PQ | BUILD_IVF_SQ8
+    build_flags: int = BUILD_FP16 | BUILD_IVF_PQ | BUILD_IVF_SQ8 | BUILD_IVF_RABITQ
     kmeans_iters: int = 10
     pq_iters: int = 10
     train_rows: int = 0
@@ -122,6 +122,7 @@ class GpuVectorIndex:
         return self._search("fp8", queries, num_queries, top_k, filter_mask=filter_mask, scan=scan)
 
     def batch_search_ivf_mode(self, queries, num_queries, top_k, nprobe, rerank_k, mode="pq", filter_mask=None):
+        """mode: "pq", "sq8" or "rabitq" (IvfQuantMode, index.rs:41-45)."""
         return self._search(mode, queries, num_queries, top_k, nprobe, rerank_k, filter_mask)
 
     def batch_search_ivf(self, queries, num_queries, top_k, nprobe, rerank_k):
@@ -156,7 +157,8 @@ class GpuVectorIndex:
         obj._h = h
         inf = obj.info()
         obj.config = IndexConfig(dim=inf["dim"], nlist=inf["nlist"], m_pq=inf["m_pq"], metric=inf["metric"],
-                                 build_flags=config.build_flags if config else BUILD_FP16 | BUILD_IVF_PQ | BUILD_IVF_SQ8)
+                                 build_flags=config.build_flags if config else
+                                 BUILD_FP16 | BUILD_IVF_PQ | BUILD_IVF_SQ8 | BUILD_IVF_RABITQ)
         return obj
 
     # ------------------------------------------------------------ status
@@ -185,6 +187,12 @@ class GpuVectorIndex:
         call("fv_index_ivf_tables", self._h, C.byref(pq), C.byref(sq), C.byref(opt))
         return pq, sq, opt
 
+    def rabitq_tables(self):
+        """(IvfRabitqGpuTables, FvIvfOptions) device views (list-major)."""
+        t, opt = _lib.IvfRabitqGpuTables(), _lib.FvIvfOptions()
+        call("fv_index_rabitq_tables", self._h, C.byref(t), C.byref(opt))
+        return t, opt
+
     def export_ivf(self) -> dict:
         """The built IVF tables as host arrays (for checking the build)."""
         inf = self.info()
@@ -195,7 +203,15 @@ class GpuVectorIndex:
         if m and self.config.build_flags & BUILD_IVF_PQ:
             spec["codebooks"] = (1, (m, 256, dim // m), np.float32)
             spec["pq_codes"] = (2, (n, m), np.uint8)
+        if self.config.build_flags & BUILD_IVF_RABITQ:
+            P = _lib.lib().fv_rabitq_padded_dim(dim)
+            spec["rot_signs"] = (8, (3 * P,), np.float32)
+            spec["rot_centroids"] = (9, (nlist, P), np.float32)
+            spec["rabitq_bits"] = (10, (n, P // 32), np.uint32)
+            spec["rabitq_meta"] = (11, (n, 4), np.float32)
         out = {"nlist": nlist}
+        if "rot_signs" in spec:
+            out["padded_dim"] = spec["rot_centroids"][1][1]
         for key, (table, shape, dt) in spec.items():
             a = np.zeros(shape, dtype=dt)
             call("fv_index_export_ivf", self._h, table, a.ctypes.data_as(C.c_void_p), a.nbytes)

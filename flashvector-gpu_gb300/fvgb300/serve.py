@@ -23,14 +23,14 @@ from ._lib import FvError, call
 from .datasets import pack_bools
 
 ALGORITHM = {"flat": 0, "fp16": 1, "fp16_tc": 1, "fp8": 2, "ivf_pq": 3, "ivf-pq": 3, "ivf": 3, "pq": 3,
-             "ivf_sq8": 4, "ivf-sq8": 4, "sq8": 4}
-ALGORITHM_NAME = {0: "flat", 1: "fp16", 2: "fp8", 3: "ivf_pq", 4: "ivf_sq8"}
+             "ivf_sq8": 4, "ivf-sq8": 4, "sq8": 4, "ivf_rabitq": 5, "ivf-rabitq": 5, "rabitq": 5}
+ALGORITHM_NAME = {0: "flat", 1: "fp16", 2: "fp8", 3: "ivf_pq", 4: "ivf_sq8", 5: "ivf_rabitq"}
 
 
 @dataclass(frozen=True)
 class BatchKey:
     """batcher.rs:55-61. algorithm: an engine name (flat, fp16, fp8, ivf_pq,
-    ivf_sq8); ef_or_nprobe is the IVF nprobe."""
+    ivf_sq8, ivf_rabitq); ef_or_nprobe is the IVF nprobe."""
     algorithm: str
     top_k: int
     ef_or_nprobe: int = 0

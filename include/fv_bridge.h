@@ -121,6 +121,27 @@ int fv_ivf_sq_search_ex(const IvfSqGpuTables* tables, const FvIvfOptions* option
                         uint32_t nprobe, uint32_t rerank_k, MetricType metric,
                         const uint32_t* d_valid_mask, GpuSearchResult* d_out_results,
                         void* stream);
+/* IVF-RaBitQ (replaces cuda_bridge.h:123-134, ivf_quant_lookup.cu:333-870,
+ * 1085-1104). Clamps and coarse probe as the IVF-PQ scan. The query is
+ * rotated (three rounds of d_rot_signs flips, Walsh-Hadamard butterflies
+ * and a 1 / sqrt(padded_dim) scale, the scale being the correctly rounded
+ * 1.0f / sqrtf(padded_dim) of the reference's host encoder); per probed list
+ * its rotated residual is quantised to 4 bits over [min, max] and every
+ * posting gets the popcount estimate of its squared L2 distance (for inner
+ * product -0.5 (|q|^2 + |x|^2 - est), for cosine 0.5 est); the shortlist of
+ * the best rerank_k estimates is re-ranked exactly. tables->words_per_vec
+ * must be padded_dim / 32 and padded_dim a power of two >= max(dim, 32),
+ * <= 4096, else FV_ERR_ARG. */
+int cuda_ivf_rabitq_search_batch(const IvfRabitqGpuTables* tables, const float* d_queries,
+                                 uint32_t num_queries, uint32_t top_k, uint32_t nprobe,
+                                 uint32_t rerank_k, MetricType metric,
+                                 const uint32_t* d_valid_mask, GpuSearchResult* d_out_results,
+                                 void* stream);
+int fv_ivf_rabitq_search_ex(const IvfRabitqGpuTables* tables, const FvIvfOptions* options,
+                            const float* d_queries, uint32_t num_queries, uint32_t top_k,
+                            uint32_t nprobe, uint32_t rerank_k, MetricType metric,
+                            const uint32_t* d_valid_mask, GpuSearchResult* d_out_results,
+                            void* stream);
 /* Gathers id-indexed code rows into list order:
  * d_out[i] = d_codes_by_id[d_ivf_vec_ids[i]] (row_bytes each). */
 int fv_ivf_relayout_codes(const uint8_t* d_codes_by_id, const uint32_t* d_ivf_vec_ids,
@@ -140,6 +161,18 @@ int fv_build_sq8(const float* d_residuals, uint32_t num_vectors, uint32_t dim, f
                  float* d_out_scales, uint8_t* d_out_codes, void* stream);
 int fv_build_ivf_lists(const GpuSearchResult* d_assign, uint32_t num_vectors, uint32_t nlist,
                        uint32_t* d_out_offsets, uint32_t* d_out_vec_ids, void* stream);
+/* RaBitQ encoder (RabitqEncoder::encode, quant.rs:156-234) on the device:
+ * rot_signs from the reference's seeded generator (host, 3 * padded_dim
+ * floats: fv_rabitq_rot_signs), rotated centroids, and per row the sign
+ * bits and meta of its rotated residual to centroid d_assign[v].id, with
+ * the reference's summation orders (bit-identical to the host encoder).
+ * fv_rabitq_padded_dim gives max(dim, 32) rounded up to a power of two. */
+uint32_t fv_rabitq_padded_dim(uint32_t dim);
+void fv_rabitq_rot_signs(uint32_t padded_dim, uint64_t seed, float* host_out);
+int fv_build_rabitq(const float* d_vectors, uint32_t num_vectors, uint32_t dim, const float* d_centroids,
+                    uint32_t nlist, const GpuSearchResult* d_assign, const float* d_rot_signs,
+                    uint32_t padded_dim, float* d_out_rot_centroids, uint32_t* d_out_bits,
+                    float* d_out_meta, void* stream);
 
 /* ---- tensor-core flat scans --------------------------------------------
  * Replaces cuda_bridge.h:138-147 (ivf_quant_lookup.cu:1106-1123). Per
@@ -218,19 +251,24 @@ int fv_index_info(FvIndex* index, FvIndexInfo* out);
  * matching options, for calling fv_ivf_{pq,sq}_search_ex directly (for
  * example inside a captured CUDA graph). Valid until the next build. */
 int fv_index_ivf_tables(FvIndex* index, IvfPqGpuTables* pq, IvfSqGpuTables* sq, FvIvfOptions* options);
+/* The same for the RaBitQ tables (list-major bits and meta, for
+ * fv_ivf_rabitq_search_ex); FV_ERR_ARG when the index has none. */
+int fv_index_rabitq_tables(FvIndex* index, IvfRabitqGpuTables* rabitq, FvIvfOptions* options);
 /* Copies IVF table `table` to host memory: 0 centroids, 1 codebooks, 2 PQ
  * codes by id, 3 SQ8 mins, 4 SQ8 scales, 5 SQ8 codes by id, 6 list offsets,
- * 7 list ids. */
+ * 7 list ids, 8 RaBitQ rotation signs, 9 rotated centroids, 10 RaBitQ bits
+ * by id, 11 RaBitQ meta by id. */
 int fv_index_export_ivf(FvIndex* index, uint32_t table, void* host_out, size_t bytes);
 
 /* Snapshots in the reference's FLSHVEC1 format (persistence.rs:1-200,
  * GpuVectorIndex::save_snapshot / load_snapshot, index.rs:845-1260).
- * save: every section the reference's loader requires (the graph and
- * RaBitQ sections it does not serve from this engine are written empty).
+ * save: every section the reference's loader requires (the graph
+ * sections, whose engines lie outside the scan path, are written empty).
  * load: the file's dim / metric / nlist / m_pq; `config` (optional)
  * supplies build_flags (FV_BUILD_FP8 adds an fp8 table built on the GPU;
  * fp16 rows are taken from the file when padded as this engine pads, else
- * encoded), streams and seed. Sections are copied to the GPU from a
+ * encoded; RaBitQ tables are taken from the file when present, else
+ * encoded on the GPU), streams and seed. Sections are copied to the GPU from a
  * read-only mapping of the file; rows whose logical id differs from their
  * slot are placed at their logical id. fv_snapshot_inspect (no GPU
  * needed) writes the manifest as JSON; fv_snapshot_error describes the last

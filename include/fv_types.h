@@ -69,6 +69,27 @@ typedef struct {
     uint32_t nlist;
 } IvfSqGpuTables;
 
+/* IVF-RaBitQ tables, field order as types.h:113-128. padded_dim is the
+ * power of two >= max(dim, 32) that the rotation works in, words_per_vec =
+ * padded_dim / 32. Row v of d_rabitq_bits holds the sign bits of vector v's
+ * rotated residual (bit d of word d / 32 set when coordinate d >= 0); row v
+ * of d_rabitq_meta holds {|r|^2, |r|^2 / sum_d |rot r|_d, popcount, |x|^2}. */
+typedef struct {
+    const float* d_centroids;      /* [nlist * dim] coarse centroids            */
+    const float* d_rot_centroids;  /* [nlist * padded_dim] rotated centroids    */
+    const uint32_t* d_rabitq_bits; /* [num_vectors * words_per_vec]             */
+    const float* d_rabitq_meta;    /* [num_vectors * 4]                         */
+    const float* d_rot_signs;      /* [3 * padded_dim] +-1 per rotation round   */
+    const uint32_t* d_ivf_offsets; /* [nlist + 1]                               */
+    const uint32_t* d_ivf_vec_ids; /* [num_vectors]                             */
+    const float* d_vectors;        /* [num_vectors * dim] fp32 rows for rerank  */
+    uint32_t num_vectors;
+    uint32_t dim;
+    uint32_t padded_dim;
+    uint32_t words_per_vec;
+    uint32_t nlist;
+} IvfRabitqGpuTables;
+
 /* FP16 flat tables, field order as types.h:131-138. padded_dim is a
  * multiple of 16; columns dim..padded_dim-1 of each fp16 row are zero.
  * When d_vectors (fp32 copy, row stride dim) is non-null the scan is
@@ -107,8 +128,9 @@ typedef struct {
 
 /* Options of the IVF extensions; no reference counterpart. */
 typedef struct {
-    uint32_t codes_list_major; /* 1: d_pq_codes / d_sq_codes row i belongs to list
-                                  position i (fv_ivf_relayout_codes), 0: row v = id v */
+    uint32_t codes_list_major; /* 1: d_pq_codes / d_sq_codes / d_rabitq_bits and
+                                  d_rabitq_meta row i belongs to list position i
+                                  (fv_ivf_relayout_codes), 0: row v = id v */
     uint32_t reserved[3];
 } FvIvfOptions;
 
@@ -122,7 +144,8 @@ typedef struct {
     uint32_t metric;        /* MetricType                                     */
     uint32_t nlist;         /* IVF lists (0 = no IVF tables)                  */
     uint32_t m_pq;          /* PQ sub-quantisers (0 = no IVF-PQ)              */
-    uint32_t build_flags;   /* FV_BUILD_* bits (0 = FP16 | IVF_PQ | IVF_SQ8)   */
+    uint32_t build_flags;   /* FV_BUILD_* bits (0 = FP16 | IVF_PQ | IVF_SQ8 |
+                               IVF_RABITQ, the reference's build)            */
     uint32_t kmeans_iters;  /* Lloyd iterations (0 = 10)                      */
     uint32_t pq_iters;      /* per-sub-space k-means iterations (0 = 10)      */
     uint32_t train_rows;    /* rows sampled to train centroids / codebooks
@@ -137,6 +160,7 @@ typedef struct {
 #define FV_BUILD_FP8 2u
 #define FV_BUILD_IVF_PQ 4u
 #define FV_BUILD_IVF_SQ8 8u
+#define FV_BUILD_IVF_RABITQ 16u
 
 /* Search engines of the scan path. */
 enum {
@@ -144,7 +168,8 @@ enum {
     FV_ENGINE_FP16 = 1,    /* fp16 tensor-core scan + fp32 rescore            */
     FV_ENGINE_FP8 = 2,     /* e4m3 tensor-core scan + fp32 rescore            */
     FV_ENGINE_IVF_PQ = 3,  /* IvfQuantMode::Pq                                */
-    FV_ENGINE_IVF_SQ8 = 4  /* IvfQuantMode::Sq8                               */
+    FV_ENGINE_IVF_SQ8 = 4, /* IvfQuantMode::Sq8                               */
+    FV_ENGINE_IVF_RABITQ = 5 /* IvfQuantMode::Rabitq                          */
 };
 
 typedef struct {

@@ -724,3 +724,203 @@ double fvo_recall(const uint32_t* approx, uint32_t astride, const uint32_t* trut
     }
     return total / nq;
 }
+
+/* ---------------------------------------------------------------- RaBitQ */
+uint32_t fvo_rabitq_padded_dim(uint32_t dim) {
+    uint32_t p = 32;
+    while (p < dim) p <<= 1;
+    return p;
+}
+
+void fvo_rabitq_rot_signs(uint32_t padded_dim, uint64_t seed, float* out) {
+    /* splitmix64 stream started at seed ^ golden-ratio increment; the low bit
+     * of each output picks the sign (quant.rs:100-116) */
+    const uint64_t inc = 0x9e3779b97f4a7c15ull;
+    uint64_t s = seed ^ inc;
+    for (uint32_t i = 0; i < 3u * padded_dim; ++i) {
+        s += inc;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        z ^= z >> 31;
+        out[i] = (z & 1u) ? -1.0f : 1.0f;
+    }
+}
+
+float fvo_rabitq_inv_sqrt(uint32_t padded_dim) { return 1.0f / sqrtf((float)padded_dim); }
+
+void fvo_rabitq_rotate(const float* v, uint32_t len, const float* signs, uint32_t padded_dim, float* out) {
+    /* three rounds of sign flip, unnormalised Walsh-Hadamard butterflies
+     * (half-length 1, 2, 4, ...) and a 1/sqrt(P) scale (quant.rs:119-154) */
+    const uint32_t P = padded_dim;
+    const float scale = fvo_rabitq_inv_sqrt(P);
+    for (uint32_t d = 0; d < P; ++d) out[d] = d < len ? v[d] : 0.0f;
+    for (uint32_t st = 0; st < 3; ++st) {
+        const float* sg = signs + (size_t)st * P;
+        for (uint32_t d = 0; d < P; ++d) out[d] = out[d] * sg[d];
+        for (uint32_t h = 1; h < P; h <<= 1)
+            for (uint32_t blk = 0; blk < P; blk += 2 * h)
+                for (uint32_t o = 0; o < h; ++o) {
+                    float x = out[blk + o], y = out[blk + o + h];
+                    out[blk + o] = x + y;
+                    out[blk + o + h] = x - y;
+                }
+        for (uint32_t d = 0; d < P; ++d) out[d] = out[d] * scale;
+    }
+}
+
+void fvo_rabitq_encode(const float* x, uint32_t n, uint32_t dim, const float* centroids, uint32_t nlist,
+                       const uint32_t* assign, const float* signs, uint32_t padded_dim, float* rot_centroids,
+                       uint32_t* bits, float* meta, int threads) {
+    const uint32_t P = padded_dim, W = P / 32;
+    for (uint32_t c = 0; c < nlist; ++c)
+        fvo_rabitq_rotate(centroids + (size_t)c * dim, dim, signs, P, rot_centroids + (size_t)c * P);
+    set_threads(threads);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        const float* v = x + (size_t)i * dim;
+        const float* ce = centroids + (size_t)assign[i] * dim;
+        float* r = (float*)malloc(sizeof(float) * dim);
+        float* rot = (float*)malloc(sizeof(float) * P);
+        float res_sq = 0.0f, vec_sq = 0.0f;
+        for (uint32_t d = 0; d < dim; ++d) {
+            r[d] = v[d] - ce[d];
+            res_sq = res_sq + r[d] * r[d];
+            vec_sq = vec_sq + v[d] * v[d];
+        }
+        fvo_rabitq_rotate(r, dim, signs, P, rot);
+        uint32_t* b = bits + (size_t)i * W;
+        memset(b, 0, sizeof(uint32_t) * W);
+        float abs_sum = 0.0f;
+        uint32_t pop = 0;
+        for (uint32_t d = 0; d < P; ++d) {
+            if (rot[d] >= 0.0f) {
+                b[d >> 5] |= 1u << (d & 31u);
+                ++pop;
+            }
+            abs_sum = abs_sum + fabsf(rot[d]);
+        }
+        const float res_norm = sqrtf(res_sq);
+        float* m = meta + (size_t)i * 4;
+        m[0] = res_sq;
+        m[1] = (res_norm > 1e-12f && abs_sum > 1e-12f) ? (res_norm * res_norm) / abs_sum : 0.0f;
+        m[2] = (float)pop;
+        m[3] = vec_sq;
+        free(r);
+        free(rot);
+    }
+}
+
+/* ||q||^2 in the order of a 256-thread block: thread t accumulates
+ * fmaf(q[d], q[d], .) over d = t, t + 256, ...; the 256 partials are then
+ * folded pairwise, partial[t] += partial[t + s] for s = 128, 64, ..., 1
+ * (ivf_quant_lookup.cu:686-697). */
+static float block256_norm_sq(const float* q, uint32_t dim) {
+    float part[256];
+    for (uint32_t t = 0; t < 256; ++t) {
+        float s = 0.0f;
+        for (uint32_t d = t; d < dim; d += 256) s = fmaf(q[d], q[d], s);
+        part[t] = s;
+    }
+    for (uint32_t s = 128; s > 0; s >>= 1)
+        for (uint32_t t = 0; t < s; ++t) part[t] = part[t] + part[t + s];
+    return part[0];
+}
+
+float fvo_rabitq_estimate(const uint32_t* b, const float* m, const uint32_t* planes, uint32_t W, uint32_t P,
+                          float q_min, float delta, float sum_u, float q_c, float q_norm_sq, int metric) {
+    uint32_t acc[4] = {0, 0, 0, 0};
+    for (uint32_t w = 0; w < W; ++w)
+        for (uint32_t j = 0; j < 4; ++j) acc[j] += (uint32_t)__builtin_popcount(b[w] & planes[j * W + w]);
+    const float s_bu = (float)(acc[0] + 2u * acc[1] + 4u * acc[2] + 8u * acc[3]);
+    const float A = 2.0f * m[2] - (float)P;
+    const float B = 2.0f * s_bu - sum_u;
+    /* the estimator of ivf_quant_lookup.cu:467-481 with its roundings fixed:
+     * q_min * A rounded, delta * B fused into it, times rescale rounded */
+    const float t = fmaf(delta, B, q_min * A);
+    const float inner = m[1] * t;
+    const float est_l2 = (q_c + m[0]) - 2.0f * inner;
+    if (metric == FVO_IP) return -0.5f * ((q_norm_sq + m[3]) - est_l2);
+    if (metric == FVO_COSINE) return 0.5f * est_l2;
+    return est_l2;
+}
+
+/* The 4-bit query code of one probed list (ivf_quant_lookup.cu:389-460):
+ * diff = rot_q - rot_centroid over all P coordinates, u = clamp(rint((diff -
+ * min) * 15 / range), 0, 15) (0 everywhere when range <= 1e-12), bit-planes
+ * planes[j][w] bit l = bit j of u[32 w + l]. Returns sum u. */
+static uint32_t rabitq_query_code(const float* rot_q, const float* rot_c, uint32_t P, uint32_t* planes,
+                                  float* q_min_out, float* delta_out) {
+    const uint32_t W = P / 32;
+    float lo = 1e30f, hi = -1e30f;
+    for (uint32_t d = 0; d < P; ++d) {
+        float v = rot_q[d] - rot_c[d];
+        if (v < lo) lo = v;
+        if (v > hi) hi = v;
+    }
+    const float range = hi - lo;
+    const float delta = range > 1e-12f ? range / 15.0f : 0.0f;
+    const float inv_delta = range > 1e-12f ? 15.0f / range : 0.0f;
+    memset(planes, 0, sizeof(uint32_t) * 4 * W);
+    uint32_t sum_u = 0;
+    for (uint32_t d = 0; d < P; ++d) {
+        uint32_t u = 0;
+        if (delta > 0.0f) {
+            float v = rot_q[d] - rot_c[d];
+            long qi = lrintf((v - lo) * inv_delta);
+            u = qi < 0 ? 0u : qi > 15 ? 15u : (uint32_t)qi;
+        }
+        sum_u += u;
+        for (uint32_t j = 0; j < 4; ++j)
+            if (u & (1u << j)) planes[j * W + (d >> 5)] |= 1u << (d & 31u);
+    }
+    *q_min_out = lo;
+    *delta_out = delta;
+    return sum_u;
+}
+
+uint32_t fvo_ivf_rabitq_search(const float* centroids, const float* rot_centroids, const uint32_t* bits,
+                               const float* meta, const float* signs, const uint32_t* offsets,
+                               const uint32_t* vec_ids, const float* vectors, uint32_t num_vectors, uint32_t dim,
+                               uint32_t padded_dim, uint32_t nlist, const float* queries, uint32_t nq,
+                               uint32_t top_k, uint32_t nprobe, uint32_t rerank_k, int metric, const uint32_t* mask,
+                               FvoResult* out, int threads) {
+    IvfClamp c;
+    const uint32_t P = padded_dim, W = P / 32;
+    if (dim == 0 || P < 32 || (P & (P - 1)) || P < dim) return 0;
+    if (!ivf_clamp(nq, top_k, nprobe, rerank_k, nlist, vectors, &c)) return 0;
+    set_threads(threads);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t qi = 0; qi < (int64_t)nq; ++qi) {
+        const float* q = queries + (size_t)qi * dim;
+        uint32_t* lists = (uint32_t*)malloc(sizeof(uint32_t) * c.nprobe);
+        float* cdist = (float*)malloc(sizeof(float) * c.nprobe);
+        coarse_topn(q, centroids, nlist, dim, c.nprobe, lists, cdist);
+        const float qn = block256_norm_sq(q, dim);
+        float* rot_q = (float*)malloc(sizeof(float) * P);
+        uint32_t* planes = (uint32_t*)malloc(sizeof(uint32_t) * 4 * W);
+        fvo_rabitq_rotate(q, dim, signs, P, rot_q);
+        uint64_t* buf = (uint64_t*)malloc(sizeof(uint64_t) * c.shortlist);
+        Heap hp = {buf, c.shortlist, 0};
+        for (uint32_t p = 0; p < c.nprobe; ++p) {
+            uint32_t cl = lists[p];
+            if (cl >= nlist) continue;
+            float q_min, delta;
+            const uint32_t sum_u = rabitq_query_code(rot_q, rot_centroids + (size_t)cl * P, P, planes, &q_min, &delta);
+            for (uint32_t i = offsets[cl]; i < offsets[cl + 1]; ++i) {
+                uint32_t vid = vec_ids[i];
+                if (!mask_ok(mask, vid)) continue;
+                float est = fvo_rabitq_estimate(bits + (size_t)vid * W, meta + (size_t)vid * 4, planes, W, P, q_min,
+                                                delta, (float)sum_u, cdist[p], qn, metric);
+                if (est < SENT_DIST) heap_push(&hp, key_of(est, vid));
+            }
+        }
+        ivf_finish(&hp, q, vectors, num_vectors, dim, metric, &c, out + (size_t)qi * c.top_k);
+        free(lists);
+        free(cdist);
+        free(rot_q);
+        free(planes);
+        free(buf);
+    }
+    return c.top_k;
+}

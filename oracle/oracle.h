@@ -117,6 +117,38 @@ uint32_t fvo_ivf_sq_search(const float* centroids, const float* mins, const floa
                            uint32_t top_k, uint32_t nprobe, uint32_t rerank_k, int metric, const uint32_t* mask,
                            FvoResult* out, int threads);
 
+/* RaBitQ (quant.rs:91-235, ivf_quant_lookup.cu:333-870).
+ * padded_dim P = next power of two >= max(dim, 32); rot_signs: 3 P signs
+ * from a splitmix64 stream (quant.rs:100-116); the rotation is three rounds
+ * of sign flip, Walsh-Hadamard butterflies and a 1/sqrt(P) scale, the
+ * scale being the correctly rounded 1.0f / sqrtf(P) of the host encoder
+ * (quant.rs:124; the reference's query kernel takes rsqrtf instead).
+ * encode: rot_centroids [nlist][P], bits [n][P/32] (bit d = rotated residual
+ * coordinate d >= 0), meta [n][4] = {|r|^2, |r|^2 / sum|rot r| (0 when
+ * either is <= 1e-12), popcount, |x|^2}, norms summed sequentially. */
+uint32_t fvo_rabitq_padded_dim(uint32_t dim);
+void fvo_rabitq_rot_signs(uint32_t padded_dim, uint64_t seed, float* out);
+float fvo_rabitq_inv_sqrt(uint32_t padded_dim);
+void fvo_rabitq_rotate(const float* v, uint32_t len, const float* signs, uint32_t padded_dim, float* out);
+void fvo_rabitq_encode(const float* x, uint32_t n, uint32_t dim, const float* centroids, uint32_t nlist,
+                       const uint32_t* assign, const float* signs, uint32_t padded_dim, float* rot_centroids,
+                       uint32_t* bits, float* meta, int threads);
+/* One row's estimated distance from the 4 query bit-planes (planes[j][w]). */
+float fvo_rabitq_estimate(const uint32_t* b, const float* m, const uint32_t* planes, uint32_t W, uint32_t P,
+                          float q_min, float delta, float sum_u, float q_c, float q_norm_sq, int metric);
+/* IVF-RaBitQ search: clamps and coarse probe as IVF-PQ; per probed list the
+ * rotated query residual is quantised to 4 bits over [min, max] and every
+ * posting gets the popcount estimate (L2, or IP / cosine forms of it);
+ * shortlist by (estimate, id); exact rerank; top_k by (distance, id).
+ * ||q||^2 (inner product only) is summed in the order of a 256-thread block
+ * (ivf_quant_lookup.cu:686-697). Returns the clamped top_k. */
+uint32_t fvo_ivf_rabitq_search(const float* centroids, const float* rot_centroids, const uint32_t* bits,
+                               const float* meta, const float* signs, const uint32_t* offsets,
+                               const uint32_t* vec_ids, const float* vectors, uint32_t num_vectors, uint32_t dim,
+                               uint32_t padded_dim, uint32_t nlist, const float* queries, uint32_t nq,
+                               uint32_t top_k, uint32_t nprobe, uint32_t rerank_k, int metric, const uint32_t* mask,
+                               FvoResult* out, int threads);
+
 /* Coarse probe order only (top-nprobe list ids per query, by (dist, id)). */
 void fvo_coarse_probe(const float* centroids, uint32_t nlist, uint32_t dim, const float* queries, uint32_t nq,
                       uint32_t nprobe, uint32_t* out_lists, float* out_dist, int threads);

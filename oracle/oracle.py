@@ -58,6 +58,13 @@ def lib():
             "fvo_ivf_sq_search": (u32, [P, P, P, P, P, P, P, u32, u32, u32, P, u32, u32, u32, u32, i32, P, P, i32]),
             "fvo_coarse_probe": (None, [P, u32, u32, P, u32, u32, P, P, i32]),
             "fvo_recall": (C.c_double, [P, u32, P, u32, u32, u32]),
+            "fvo_rabitq_padded_dim": (u32, [u32]),
+            "fvo_rabitq_rot_signs": (None, [u32, C.c_uint64, P]),
+            "fvo_rabitq_inv_sqrt": (C.c_float, [u32]),
+            "fvo_rabitq_rotate": (None, [P, u32, P, u32, P]),
+            "fvo_rabitq_encode": (None, [P, u32, u32, P, u32, P, P, u32, P, P, P, i32]),
+            "fvo_ivf_rabitq_search": (u32, [P, P, P, P, P, P, P, P, u32, u32, u32, u32, P, u32, u32, u32, u32, i32, P,
+                                            P, i32]),
         }
         for name, (res, args) in sig.items():
             f = getattr(_lib, name)
@@ -214,7 +221,45 @@ def build_ivf(x, nlist, m_pq=None, iters=25, seed=0, threads=None):
     mins, scales = sq8_fit(res)
     t["sq_mins"], t["sq_scales"] = mins, scales
     t["sq_codes"] = sq8_encode(res, mins, scales)
+    t.update(rabitq_encode(x, cent, assign, RABITQ_SEED, threads))
     return t
+
+
+# the engine's RaBitQ rotation seed (index.rs:435-441)
+RABITQ_SEED = 0x5F37_59DF_CAFE_BABE
+
+
+def rabitq_padded_dim(dim) -> int:
+    return int(lib().fvo_rabitq_padded_dim(dim))
+
+
+def rabitq_rot_signs(padded_dim, seed=RABITQ_SEED):
+    out = np.zeros(3 * padded_dim, dtype=np.float32)
+    lib().fvo_rabitq_rot_signs(padded_dim, seed, _p(out))
+    return out
+
+
+def rabitq_rotate(v, signs, padded_dim):
+    v = _f32(v)
+    out = np.zeros(padded_dim, dtype=np.float32)
+    lib().fvo_rabitq_rotate(_p(v), v.shape[0], _p(_f32(signs)), padded_dim, _p(out))
+    return out
+
+
+def rabitq_encode(x, centroids, assign, seed=RABITQ_SEED, threads=None):
+    """RabitqEncoder::encode (quant.rs:156-234): rot_signs, rot_centroids,
+    rabitq_bits [n][P/32] u32, rabitq_meta [n][4] f32."""
+    x, centroids = _f32(x), _f32(centroids)
+    n, dim = x.shape
+    nlist = centroids.shape[0]
+    P = rabitq_padded_dim(dim)
+    signs = rabitq_rot_signs(P, seed)
+    rot_c = np.zeros((nlist, P), dtype=np.float32)
+    bits = np.zeros((n, P // 32), dtype=np.uint32)
+    meta = np.zeros((n, 4), dtype=np.float32)
+    lib().fvo_rabitq_encode(_p(x), n, dim, _p(centroids), nlist, _p(np.ascontiguousarray(assign, dtype=np.uint32)),
+                            _p(signs), P, _p(rot_c), _p(bits), _p(meta), threads or threads_default())
+    return {"padded_dim": P, "rot_signs": signs, "rot_centroids": rot_c, "rabitq_bits": bits, "rabitq_meta": meta}
 
 
 def ivf_pq_search(t, vectors, queries, top_k, nprobe, rerank_k, metric="l2", mask=None, use_vectors=True,
@@ -248,6 +293,23 @@ def ivf_sq_search(t, vectors, queries, top_k, nprobe, rerank_k, metric="l2", mas
                             _p(t["sq_codes"]), _p(t["offsets"]), _p(t["vec_ids"]),
                             _p(vectors) if use_vectors else None, n, dim, t["nlist"], _p(queries), nq, top_k, nprobe,
                             rerank_k, _metric(metric), _p(mask), _p(out), threads or threads_default())
+    return out
+
+
+def ivf_rabitq_search(t, vectors, queries, top_k, nprobe, rerank_k, metric="l2", mask=None, use_vectors=True,
+                      threads=None):
+    queries = _f32(queries)
+    vectors = _f32(vectors)
+    n, dim = vectors.shape
+    nq = queries.shape[0]
+    k = min(top_k, 256)
+    out = np.zeros((nq, k), dtype=RESULT_DTYPE)
+    mask = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint32)
+    lib().fvo_ivf_rabitq_search(_p(_f32(t["centroids"])), _p(_f32(t["rot_centroids"])), _p(t["rabitq_bits"]),
+                                _p(_f32(t["rabitq_meta"])), _p(_f32(t["rot_signs"])), _p(t["offsets"]),
+                                _p(t["vec_ids"]), _p(vectors) if use_vectors else None, n, dim, t["padded_dim"],
+                                t["nlist"], _p(queries), nq, top_k, nprobe, rerank_k, _metric(metric), _p(mask),
+                                _p(out), threads or threads_default())
     return out
 
 

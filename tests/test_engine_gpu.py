@@ -20,10 +20,12 @@ def gen_clustered(n, dim, clusters, seed, sigma=0.18):
 
 
 def make_index(x, nlist, m_pq, metric="l2", flags=None, **kw):
-    from fvgb300.index import BUILD_FP8, BUILD_FP16, BUILD_IVF_PQ, BUILD_IVF_SQ8, GpuVectorIndex, IndexConfig
+    from fvgb300.index import (BUILD_FP8, BUILD_FP16, BUILD_IVF_PQ, BUILD_IVF_RABITQ, BUILD_IVF_SQ8, GpuVectorIndex,
+                               IndexConfig)
 
     cfg = IndexConfig(dim=x.shape[1], nlist=nlist, m_pq=m_pq, metric=metric,
-                      build_flags=flags or (BUILD_FP16 | BUILD_FP8 | BUILD_IVF_PQ | BUILD_IVF_SQ8), **kw)
+                      build_flags=flags or (BUILD_FP16 | BUILD_FP8 | BUILD_IVF_PQ | BUILD_IVF_SQ8 | BUILD_IVF_RABITQ),
+                      **kw)
     idx = GpuVectorIndex(cfg)
     idx.build(x)
     return idx
@@ -54,9 +56,15 @@ def test_built_tables_match_oracle_encoders(cuda, oracle_mod, e2e):
     mins, scales = oracle_mod.sq8_fit(res)
     assert np.array_equal(mins, t["sq_mins"]) and np.array_equal(scales, t["sq_scales"])
     assert np.array_equal(oracle_mod.sq8_encode(res, mins, scales), t["sq_codes"])
+    # RaBitQ (index.rs:435-441: the engine's seed, the rows' own assignment)
+    rq = oracle_mod.rabitq_encode(x, t["centroids"], assign)
+    assert t["padded_dim"] == rq["padded_dim"] == 128
+    assert np.array_equal(rq["rot_signs"], t["rot_signs"])
+    for key in ("rot_centroids", "rabitq_bits", "rabitq_meta"):
+        assert np.array_equal(rq[key].view(np.uint32), t[key].view(np.uint32)), key
 
 
-@pytest.mark.parametrize("mode", ["pq", "sq8"])
+@pytest.mark.parametrize("mode", ["pq", "sq8", "rabitq"])
 def test_ivf_recall_and_parity_at_reference_params(cuda, oracle_mod, e2e, mode):
     """e2e_search_test.rs:231-277: nprobe 12, rerank 256, recall@10 >= 0.80
     for the first 8 rows as queries; answers equal the oracle on the
@@ -66,7 +74,8 @@ def test_ivf_recall_and_parity_at_reference_params(cuda, oracle_mod, e2e, mode):
     q = x[:8]
     for rerank in (256, 512):
         ids, dist = idx.batch_search_ivf_mode(q, 8, 10, 12, rerank, mode)
-        fn = oracle_mod.ivf_pq_search if mode == "pq" else oracle_mod.ivf_sq_search
+        fn = {"pq": oracle_mod.ivf_pq_search, "sq8": oracle_mod.ivf_sq_search,
+              "rabitq": oracle_mod.ivf_rabitq_search}[mode]
         ref = fn(t, x, q, 10, 12, rerank)
         assert np.array_equal(ids, ref["id"]) and np.array_equal(dist, ref["distance"])
         truth = oracle_mod.exact_knn(x, q, 10)
@@ -99,6 +108,7 @@ def test_bitmask_filtering_all_engines(cuda):
         "fp8": idx.batch_search_fp8(q, 1, 10, words),
         "ivf_pq": idx.batch_search_ivf_mode(q, 1, 10, 12, 64, "pq", words),
         "ivf_sq8": idx.batch_search_ivf_mode(q, 1, 10, 12, 64, "sq8", words),
+        "ivf_rabitq": idx.batch_search_ivf_mode(q, 1, 10, 12, 64, "rabitq", words),
     }
     for name, (ids, _) in runs.items():
         valid = ids[ids != 0xFFFFFFFF]
@@ -117,7 +127,8 @@ def test_delta_insert_and_tombstones(cuda):
     assert idx.delta_len() == 1
     for search in (lambda q: idx.batch_search_flat(q, 1, 5), lambda q: idx.batch_search_fp16_tc(q, 1, 5),
                    lambda q: idx.batch_search_ivf_mode(q, 1, 5, 8, 32, "pq"),
-                   lambda q: idx.batch_search_ivf_mode(q, 1, 5, 8, 32, "sq8")):
+                   lambda q: idx.batch_search_ivf_mode(q, 1, 5, 8, 32, "sq8"),
+                   lambda q: idx.batch_search_ivf_mode(q, 1, 5, 8, 32, "rabitq")):
         ids, dist = search(marker)
         assert ids[0, 0] == 400
         assert np.all(dist[0, :-1] <= dist[0, 1:])
@@ -127,7 +138,8 @@ def test_delta_insert_and_tombstones(cuda):
     q0 = x[:1]
     for ids, _ in (idx.batch_search_flat(q0, 1, 10), idx.batch_search_fp16_tc(q0, 1, 10),
                    idx.batch_search_ivf_mode(q0, 1, 10, 8, 32, "pq"),
-                   idx.batch_search_ivf_mode(q0, 1, 10, 8, 32, "sq8")):
+                   idx.batch_search_ivf_mode(q0, 1, 10, 8, 32, "sq8"),
+                   idx.batch_search_ivf_mode(q0, 1, 10, 8, 32, "rabitq")):
         assert np.all(ids != 0)
     # deleting a live-insert id removes it too
     assert idx.delete_ids([400]) == 1

@@ -1,9 +1,10 @@
-"""IVF-PQ / IVF-SQ8 scans through the C ABI against the oracle.
+"""IVF-PQ / IVF-SQ8 / IVF-RaBitQ scans through the C ABI against the oracle.
 
 Every distance of the path (coarse L2, LUT entries, ADC sums, SQ8 decode,
-warp-order rerank) is evaluated in the reference's operation order, so ids
-and distances must be bit-identical to the oracle's restatement; results
-are ordered by (distance, id)."""
+RaBitQ rotation, 4-bit query code and popcount estimate, warp-order rerank)
+is evaluated in the reference's operation order (the RaBitQ estimate in the
+fixed order both sides restate), so ids and distances must be bit-identical
+to the oracle's restatement; results are ordered by (distance, id)."""
 from __future__ import annotations
 
 import numpy as np
@@ -16,6 +17,14 @@ def gen_clustered(n, dim, clusters, seed, sigma=0.18):
     rng = np.random.default_rng(seed)
     centers = rng.uniform(-1, 1, size=(clusters, dim)).astype(np.float32)
     return (centers[np.arange(n) % clusters] + np.float32(sigma) * rng.standard_normal((n, dim))).astype(np.float32)
+
+
+MODES = ["pq", "sq8", "rabitq"]
+
+
+def oracle_fn(oracle_mod, mode):
+    return {"pq": oracle_mod.ivf_pq_search, "sq8": oracle_mod.ivf_sq_search,
+            "rabitq": oracle_mod.ivf_rabitq_search}[mode]
 
 
 def res_np(res):
@@ -50,30 +59,30 @@ def run(cuda, t, x, q, mode, k, nprobe, rerank, metric="l2", mask=None, list_maj
     return res_np(res)
 
 
-@pytest.mark.parametrize("mode", ["pq", "sq8"])
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("rerank", [256, 512, 0, 1, 20])
 def test_ivf_matches_oracle_e2e_params(cuda, oracle_mod, e2e_case, mode, rerank):
     x, t = e2e_case
     q = x[:8]
     ids, dist = run(cuda, t, x, q, mode, 10, 12, rerank)
-    fn = oracle_mod.ivf_pq_search if mode == "pq" else oracle_mod.ivf_sq_search
+    fn = oracle_fn(oracle_mod, mode)
     assert_same(ids, dist, fn(t, x, q, 10, 12, rerank))
     if rerank not in (0, 1):
         truth = oracle_mod.exact_knn(x, q, 10)
         assert oracle_mod.recall(ids, truth["id"]) >= 0.80
 
 
-@pytest.mark.parametrize("mode", ["pq", "sq8"])
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("metric", ["ip", "cosine"])
 def test_ivf_rerank_metrics(cuda, oracle_mod, e2e_case, mode, metric):
     x, t = e2e_case
     q = x[100:140] + np.float32(0.01)
     ids, dist = run(cuda, t, x, q, mode, 16, 6, 64, metric)
-    fn = oracle_mod.ivf_pq_search if mode == "pq" else oracle_mod.ivf_sq_search
+    fn = oracle_fn(oracle_mod, mode)
     assert_same(ids, dist, fn(t, x, q, 16, 6, 64, metric))
 
 
-@pytest.mark.parametrize("mode", ["pq", "sq8"])
+@pytest.mark.parametrize("mode", MODES)
 def test_ivf_mask_and_list_major(cuda, oracle_mod, e2e_case, mode):
     """No masked-out id is returned (e2e_search_test.rs:322-433 window), and
     the list-major code layout gives the identical answer."""
@@ -85,7 +94,7 @@ def test_ivf_mask_and_list_major(cuda, oracle_mod, e2e_case, mode):
     words = pack_bools(allowed)
     q = x[:2]
     ids, dist = run(cuda, t, x, q, mode, 5, 8, 64, mask=words)
-    fn = oracle_mod.ivf_pq_search if mode == "pq" else oracle_mod.ivf_sq_search
+    fn = oracle_fn(oracle_mod, mode)
     assert_same(ids, dist, fn(t, x, q, 5, 8, 64, mask=words))
     valid = ids[ids != 0xFFFFFFFF]
     assert valid.size > 0 and np.all(allowed[valid])
@@ -100,15 +109,15 @@ def test_ivf_large_k_sorted(cuda, oracle_mod):
     x = rng.standard_normal((1000, 64), dtype=np.float32)
     t = oracle_mod.build_ivf(x, nlist=16, m_pq=8, iters=10, seed=1)
     q = rng.standard_normal((3, 64), dtype=np.float32)
-    for mode in ("pq", "sq8"):
+    for mode in MODES:
         ids, dist = run(cuda, t, x, q, mode, 100, 16, 0)
-        fn = oracle_mod.ivf_pq_search if mode == "pq" else oracle_mod.ivf_sq_search
+        fn = oracle_fn(oracle_mod, mode)
         assert_same(ids, dist, fn(t, x, q, 100, 16, 0))
         assert (ids[0] != 0xFFFFFFFF).sum() >= 90
         assert np.all(dist[:, :-1] <= dist[:, 1:])
 
 
-@pytest.mark.parametrize("mode", ["pq", "sq8"])
+@pytest.mark.parametrize("mode", MODES)
 def test_ivf_wide_batch_vector_loads(cuda, oracle_mod, mode):
     """d=128, M=32 (16-byte code loads), 300 queries, 400-candidate rerank,
     list-major and id-major layouts."""
@@ -118,7 +127,7 @@ def test_ivf_wide_batch_vector_loads(cuda, oracle_mod, mode):
     x = datasets.sample_np(mix, 30000, seed=3, stream=0)
     q = datasets.sample_np(mix, 300, seed=3, stream=1)
     t = oracle_mod.build_ivf(x, nlist=128, m_pq=32, iters=8, seed=2)
-    fn = oracle_mod.ivf_pq_search if mode == "pq" else oracle_mod.ivf_sq_search
+    fn = oracle_fn(oracle_mod, mode)
     ref = fn(t, x, q, 10, 16, 400)
     for lm in (False, True):
         ids, dist = run(cuda, t, x, q, mode, 10, 16, 400, list_major=lm)
@@ -145,7 +154,7 @@ def test_ivf_clamps_and_noops(cuda, oracle_mod, e2e_case):
     assert _lib.lib().cuda_ivf_pq_search_batch(None, None, 1, 10, 4, 0, 0, None, None, None) == -1
 
 
-@pytest.mark.parametrize("mode", ["pq", "sq8"])
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("split", [0, 2, 7, 33])
 def test_ivf_posting_ranges_give_the_same_answer(cuda, oracle_mod, mode, split):
     """A query's probed postings cut into G ranges (separate CTAs, merged
@@ -171,6 +180,58 @@ def test_ivf_posting_ranges_give_the_same_answer(cuda, oracle_mod, mode, split):
     mask = pack_bools(words)
     with scan.tuned(ivf_split=split):
         ids, dist = run(cuda, t, x, q, mode, 20, 6, 64, mask=mask, list_major=True)
-    fn = oracle_mod.ivf_pq_search if mode == "pq" else oracle_mod.ivf_sq_search
+    fn = oracle_fn(oracle_mod, mode)
     assert_same(ids, dist, fn(t, x, q, 20, 6, 64, mask=mask))
     assert np.all(words[ids[ids != 0xFFFFFFFF]])
+
+
+@pytest.mark.parametrize("dim", [20, 64, 200, 300, 1000])
+@pytest.mark.parametrize("metric", ["l2", "ip"])
+def test_rabitq_padded_dims(cuda, oracle_mod, dim, metric):
+    """Every row width of the RaBitQ scan: P = 32 (one word, scalar path),
+    256 / 512 / 1024 (2, 4, 8 sixteen-byte words in registers), both
+    layouts, masks, against the oracle."""
+    from fvgb300.datasets import pack_bools
+
+    x = gen_clustered(3000, dim, 20, 9 + dim, sigma=0.3)
+    t = oracle_mod.build_ivf(x, nlist=20, m_pq=None, iters=8, seed=4)
+    assert t["padded_dim"] == oracle_mod.rabitq_padded_dim(dim)
+    rng = np.random.default_rng(dim)
+    q = (x[rng.integers(0, 3000, 24)] + np.float32(0.05) * rng.standard_normal((24, dim))).astype(np.float32)
+    mask = pack_bools(rng.random(3000) < 0.8)
+    ref = oracle_mod.ivf_rabitq_search(t, x, q, 10, 5, 100, metric, mask=mask)
+    for lm in (False, True):
+        ids, dist = run(cuda, t, x, q, "rabitq", 10, 5, 100, metric, mask=mask, list_major=lm)
+        assert_same(ids, dist, ref)
+    ids, dist = run(cuda, t, x, q, "rabitq", 10, 5, 1, metric)  # estimates themselves (no rerank)
+    assert_same(ids, dist, oracle_mod.ivf_rabitq_search(t, x, q, 10, 5, 1, metric))
+
+
+def test_rabitq_query_on_a_centroid(cuda, oracle_mod, e2e_case):
+    """A query equal to a coarse centroid has a zero rotated residual to its
+    own list: range 0, every 4-bit code 0 (ivf_quant_lookup.cu:409-424)."""
+    x, t = e2e_case
+    q = np.ascontiguousarray(t["centroids"][:6])
+    for rerank in (1, 64):
+        ids, dist = run(cuda, t, x, q, "rabitq", 10, 3, rerank)
+        assert_same(ids, dist, oracle_mod.ivf_rabitq_search(t, x, q, 10, 3, rerank))
+
+
+@pytest.mark.parametrize("dim", [96, 300])
+def test_rabitq_gpu_encoder_matches_host_encoder(cuda, oracle_mod, dim):
+    """fv_build_rabitq gives the host encoder's (quant.rs:156-234) rotated
+    centroids, sign bits and meta bit for bit."""
+    import torch
+
+    from fvgb300.ivf import build_rabitq
+
+    x = gen_clustered(2000, dim, 10, 31, sigma=0.4)
+    t = oracle_mod.build_ivf(x, nlist=10, m_pq=None, iters=5, seed=6)
+    enc = build_rabitq(torch.from_numpy(x).cuda(), torch.from_numpy(t["centroids"]).cuda(),
+                       torch.from_numpy(t["assign"].astype(np.int32)).cuda())
+    torch.cuda.synchronize()
+    assert enc["padded_dim"] == t["padded_dim"]
+    assert np.array_equal(enc["rot_signs"].cpu().numpy(), t["rot_signs"])
+    assert np.array_equal(enc["rot_centroids"].cpu().numpy().view(np.uint32), t["rot_centroids"].view(np.uint32))
+    assert np.array_equal(enc["rabitq_bits"].cpu().numpy().view(np.uint32), t["rabitq_bits"])
+    assert np.array_equal(enc["rabitq_meta"].cpu().numpy().view(np.uint32), t["rabitq_meta"].view(np.uint32))

@@ -125,7 +125,7 @@ def ivf_case(oracle_mod):
     return x, t
 
 
-@pytest.mark.parametrize("mode", ["pq", "sq8"])
+@pytest.mark.parametrize("mode", ["pq", "sq8", "rabitq"])
 @pytest.mark.parametrize("rerank", [256, 512, 0, 1])
 def test_ivf_oracle_recall_at_reference_params(oracle_mod, ivf_case, mode, rerank):
     """e2e_search_test.rs:231-277: d=96, N=1500, nlist=24, M=12, nprobe=12,
@@ -133,7 +133,7 @@ def test_ivf_oracle_recall_at_reference_params(oracle_mod, ivf_case, mode, reran
     >= 0.80 against exact search."""
     x, t = ivf_case
     q = x[:8]
-    fn = oracle_mod.ivf_pq_search if mode == "pq" else oracle_mod.ivf_sq_search
+    fn = {"pq": oracle_mod.ivf_pq_search, "sq8": oracle_mod.ivf_sq_search, "rabitq": oracle_mod.ivf_rabitq_search}[mode]
     res = fn(t, x, q, 10, 12, rerank)
     truth = oracle_mod.exact_knn(x, q, 10)
     r = oracle_mod.recall(res["id"], truth["id"])
@@ -162,7 +162,102 @@ def test_ivf_oracle_respects_mask(oracle_mod, ivf_case):
     allowed = np.zeros(x.shape[0], dtype=bool)
     allowed[10:200] = True
     words = pack_bools(allowed)
-    for fn in (oracle_mod.ivf_pq_search, oracle_mod.ivf_sq_search):
+    for fn in (oracle_mod.ivf_pq_search, oracle_mod.ivf_sq_search, oracle_mod.ivf_rabitq_search):
         res = fn(t, x, x[:2], 5, 8, 64, mask=words)
         ids = res["id"][res["id"] != 0xFFFFFFFF]
         assert ids.size > 0 and np.all(allowed[ids])
+
+
+# ---------------------------------------------------------------- RaBitQ
+def _splitmix_signs(padded_dim, seed):
+    """quant.rs:100-116 restated independently of the C oracle."""
+    m = (1 << 64) - 1
+    inc = 0x9E3779B97F4A7C15
+    s = seed ^ inc
+    out = []
+    for _ in range(3 * padded_dim):
+        s = (s + inc) & m
+        z = s
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+        z ^= z >> 31
+        out.append(-1.0 if z & 1 else 1.0)
+    return np.array(out, dtype=np.float32)
+
+
+def test_rabitq_padded_dim(oracle_mod):
+    """quant.rs:95-97 (and quant.rs:336-337: 96 -> 128)."""
+    for dim, p in ((96, 128), (1, 32), (32, 32), (33, 64), (129, 256), (768, 1024), (1024, 1024)):
+        assert oracle_mod.rabitq_padded_dim(dim) == p
+
+
+def test_rabitq_sign_stream_pinned(oracle_mod, built_lib):
+    """The sign generator is splitmix64 started at seed ^ 0x9e3779b97f4a7c15:
+    with seed = that constant the state starts at 0, whose published first
+    outputs are 0xe220a8397b1dcdaf, 0x6e789e6aa1b965f4, 0x06c45d188009454f,
+    0xf88bb8a8724c81ec (low bits 1, 0, 1, 0 -> -1, +1, -1, +1). The C oracle,
+    this Python restatement and the library's host generator agree for the
+    engine's seed."""
+    from fvgb300.ivf import rabitq_rot_signs
+
+    first = oracle_mod.rabitq_rot_signs(32, 0x9E3779B97F4A7C15)[:4]
+    assert first.tolist() == [-1.0, 1.0, -1.0, 1.0]
+    for P, seed in ((128, oracle_mod.RABITQ_SEED), (1024, oracle_mod.RABITQ_SEED), (64, 42)):
+        ref = _splitmix_signs(P, seed)
+        assert np.array_equal(oracle_mod.rabitq_rot_signs(P, seed), ref)
+        assert np.array_equal(rabitq_rot_signs(P, seed), ref)
+
+
+def test_rabitq_rotation_is_orthogonal(oracle_mod):
+    """quant.rs:334-347: d=96, seed 42, dot products preserved to 1e-4."""
+    dim = 96
+    P = oracle_mod.rabitq_padded_dim(dim)
+    signs = oracle_mod.rabitq_rot_signs(P, 42)
+    i = np.arange(dim, dtype=np.float32)
+    a = np.sin(i * np.float32(0.13)).astype(np.float32)
+    b = np.cos(i * np.float32(0.29)).astype(np.float32)
+    ra, rb = oracle_mod.rabitq_rotate(a, signs, P), oracle_mod.rabitq_rotate(b, signs, P)
+    assert abs(float(np.dot(a, b)) - float(np.dot(ra, rb))) < 1e-4
+    assert abs(float(np.dot(a, a)) - float(np.dot(ra, ra))) < 1e-4
+
+
+def test_rabitq_encoder_tables(oracle_mod):
+    """Per row: bit d set iff rotated residual coordinate d >= 0; meta =
+    {sequential |r|^2, |r|^2 / sum|rot r|, popcount, sequential |x|^2}."""
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((200, 40)).astype(np.float32)
+    cent = rng.standard_normal((4, 40)).astype(np.float32)
+    assign = rng.integers(0, 4, 200).astype(np.uint32)
+    t = oracle_mod.rabitq_encode(x, cent, assign)
+    P = t["padded_dim"]
+    assert P == 64 and t["rabitq_bits"].shape == (200, 2)
+    for i in range(0, 200, 17):
+        r = (x[i] - cent[assign[i]]).astype(np.float32)
+        rot = oracle_mod.rabitq_rotate(r, t["rot_signs"], P)
+        bits = np.unpackbits(t["rabitq_bits"][i].view(np.uint8), bitorder="little").astype(bool)
+        assert np.array_equal(bits, rot >= 0)
+        m = t["rabitq_meta"][i]
+        res_sq = np.float32(0)
+        vec_sq = np.float32(0)
+        for d in range(40):
+            res_sq = np.float32(res_sq + np.float32(r[d] * r[d]))
+            vec_sq = np.float32(vec_sq + np.float32(x[i, d] * x[i, d]))
+        abs_sum = np.float32(0)
+        for v in rot:
+            abs_sum = np.float32(abs_sum + np.float32(abs(v)))
+        rn = np.sqrt(res_sq, dtype=np.float32)
+        assert m[0] == res_sq and m[3] == vec_sq and m[2] == bits.sum()
+        assert m[1] == np.float32(np.float32(rn * rn) / abs_sum)
+    for c in range(4):
+        assert np.array_equal(t["rot_centroids"][c], oracle_mod.rabitq_rotate(cent[c], t["rot_signs"], P))
+
+
+def test_rabitq_estimate_tracks_distance(oracle_mod, ivf_case):
+    """The popcount estimate is an unbiased-ish stand-in for |q - x|^2: on the
+    reference's e2e data its correlation with the exact distance is high."""
+    x, t = ivf_case
+    q = x[3:4]
+    res = oracle_mod.ivf_rabitq_search(t, x, q, 256, 24, 1)  # estimates of the 256 best
+    ids = res["id"][0]
+    exact = ((x[ids] - q[0]) ** 2).sum(1)
+    assert np.corrcoef(res["distance"][0], exact)[0, 1] > 0.8

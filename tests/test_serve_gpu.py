@@ -17,11 +17,13 @@ def gen_clustered(n, dim, clusters, seed, sigma=0.25):
 
 @pytest.fixture(scope="module")
 def served(cuda):
-    from fvgb300.index import BUILD_FP8, BUILD_FP16, BUILD_IVF_PQ, BUILD_IVF_SQ8, GpuVectorIndex, IndexConfig
+    from fvgb300.index import (BUILD_FP8, BUILD_FP16, BUILD_IVF_PQ, BUILD_IVF_RABITQ, BUILD_IVF_SQ8, GpuVectorIndex,
+                               IndexConfig)
 
     x = gen_clustered(6000, 64, 24, 11)
     idx = GpuVectorIndex(IndexConfig(dim=64, nlist=32, m_pq=8, metric="l2",
-                                     build_flags=BUILD_FP16 | BUILD_FP8 | BUILD_IVF_PQ | BUILD_IVF_SQ8))
+                                     build_flags=BUILD_FP16 | BUILD_FP8 | BUILD_IVF_PQ | BUILD_IVF_SQ8 |
+                                     BUILD_IVF_RABITQ))
     idx.build(x)
     extra = gen_clustered(300, 64, 24, 12)
     idx.add_vectors(extra)
@@ -53,7 +55,7 @@ def alone(idx, key, q, filt):
     if eng in (1, 2):
         return (idx.batch_search_fp16_tc if eng == 1 else idx.batch_search_fp8)(q[None], 1, key.top_k, filt)
     return idx.batch_search_ivf_mode(q[None], 1, key.top_k, key.ef_or_nprobe, key.rerank_k,
-                                     "pq" if eng == 3 else "sq8", filt)
+                                     {3: "pq", 4: "sq8", 5: "rabitq"}[eng], filt)
 
 
 @pytest.mark.parametrize("group", [False, True])
@@ -64,7 +66,7 @@ def test_identical_alone_and_in_the_mix(served, group):
     rng = np.random.default_rng(5 + group)
     n_ids = rows.shape[0]
     filters = [rng.random(n_ids) < 0.2, (np.arange(n_ids) % 3) == 0]
-    engines = ["flat", "fp16", "fp8", "ivf_pq", "ivf_sq8"]
+    engines = ["flat", "fp16", "fp8", "ivf_pq", "ivf_sq8", "ivf_rabitq"]
     keys, fids, q = make_mix(160, rng, 64, engines)
     with SearchBatcher.for_index(idx, max_wait_us=2000, max_batch_size=64, inflight=3,
                                  group_by_params=group) as b:
