@@ -898,7 +898,10 @@ def run_serve(a, world, rank, local, dev, peaks, peak_kind):
     cfg = {"workload": "continuous batching: fp16 flat (1M x 768, IP) + IVF-SQ8 (nlist 4096) resident; requests "
                        "k in {10,100}, nprobe in {16,64}, filter in {none, 20%}; Poisson arrivals",
            "N": a.n, "dim": a.dim, "rates": rates, "max_batch": 1024, "max_wait_us": 200, "inflight": 4,
-           "build_seconds": build_s, "l2": "inputs larger than L2 (fp16 base 1.54 GB, SQ8 codes 0.77 GB)"}
+           "build_seconds": build_s, "l2": "inputs larger than L2 (fp16 base 1.54 GB, SQ8 codes 0.77 GB)",
+           "ivf_recall_note": "the mixture is nearly isotropic (unit centres, sigma 0.3 x sqrt(768) noise): true "
+                              "neighbours spread over almost all 4096 lists, so IVF at nprobe 16-64 finds few; "
+                              "the IVF requests measure serving latency, the fp16 requests carry recall@10"}
     per_req_in = a.dim * 4 + 24
     _line(a, world, top["sustained_qps"], UNIT, top["requests"] / max(top["sustained_qps"], 1e-9),
           {"value": top["sustained_qps"], "unit": UNIT, "h2d_bytes_per_step": per_req_in,
