@@ -13,7 +13,10 @@
 //    are bit-identical to it;
 //  * per query a max-heap of (distance, slot) keys in shared memory keeps
 //    the running top-k (ties -> lower slot, as the reference's strict `<`
-//    insertion in slot order);
+//    insertion in slot order); after each tile every thread tests its own
+//    4 x 8 block against the queries' current k-th keys and appends only
+//    the keys that can enter to a per-query candidate list, so the
+//    per-query heap work touches a few keys instead of the whole tile;
 //  * when the base range is split over several CTAs the per-split heaps go
 //    to scratch and a second kernel merges them.
 #include <mutex>
@@ -98,10 +101,13 @@ __global__ void __launch_bounds__(NT) flat_f32_scan_kernel(FlatArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* qs = reinterpret_cast<float*>(smem_raw);  // [DK][QS]
   float* xs = qs + DK * QS;                          // [DK][VS]
-  float* ds = xs + DK * VS;                          // [QT][VS] distances of a tile
-  float* qn = ds + QT * VS;                          // [QT]
+  float* cd = xs + DK * VS;                          // [QT][VT] candidate distances of a tile
+  float* qn = cd + QT * VT;                          // [QT]
   float* xn = qn + QT;                               // [VT]
   uint64_t* heap = reinterpret_cast<uint64_t*>(xn + VT);  // [k][QT], 8B aligned (see smem size)
+  uint64_t* wq = heap + (size_t)a.k * QT;                 // [QT] current k-th key per query
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(wq + QT);   // [QT] candidates of the tile per query
+  uint8_t* cr = reinterpret_cast<uint8_t*>(cnt + QT);     // [QT][VT] their rows within the tile
 
   const int tid = threadIdx.x;
   const int ty = tid >> 4, tx = tid & 15;
@@ -112,6 +118,10 @@ __global__ void __launch_bounds__(NT) flat_f32_scan_kernel(FlatArgs a) {
   const uint32_t t_end = min(t_begin + a.tiles_per_split, ntiles);
 
   for (uint32_t i = tid; i < k * QT; i += NT) heap[i] = kSentinelKey;
+  if (tid < QT) {
+    wq[tid] = kSentinelKey;
+    cnt[tid] = 0;
+  }
   if (METRIC == METRIC_COSINE && tid < QT) {
     float s = 0.f;
     if (q0 + tid < a.nq) {
@@ -225,11 +235,12 @@ __global__ void __launch_bounds__(NT) flat_f32_scan_kernel(FlatArgs a) {
     }
 
     if (METRIC == METRIC_COSINE && tid < VT) xn[tid] = xnorm;
-    __syncthreads();  // xn visible; previous selection finished reading ds
+    __syncthreads();  // xn visible; the previous selection has finished (wq, cnt)
 
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int qi = ty * 4 + i;
+      const uint64_t wk = wq[qi];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const int vi = tx + 16 * j;
@@ -243,25 +254,35 @@ __global__ void __launch_bounds__(NT) flat_f32_scan_kernel(FlatArgs a) {
           dist = __fsub_rn(1.0f, __fdiv_rn(acc[i][j], denom));
         }
         const uint32_t slot = v0 + vi;
-        bool ok = slot < a.n && mask_allows(a.mask, slot);
-        if (ok && a.filters) ok = filter_allows(qf[i], a.vec_ids ? __ldg(a.vec_ids + slot) : slot);
-        ds[qi * VS + vi] = ok ? dist : __int_as_float(0x7fc00000);  // NaN never passes `<`
+        // a key that cannot beat the query's current k-th key never enters
+        // (the k-th key only decreases, so testing against an older one
+        // admits a superset); NaN fails `<`
+        if (dist < kSentinelDist && make_key(dist, slot) < wk && slot < a.n && mask_allows(a.mask, slot) &&
+            (!a.filters || filter_allows(qf[i], a.vec_ids ? __ldg(a.vec_ids + slot) : slot))) {
+          const uint32_t pos = atomicAdd(cnt + qi, 1u);
+          cd[qi * VT + pos] = dist;
+          cr[qi * VT + pos] = (uint8_t)vi;
+        }
       }
     }
     __syncthreads();
 
-    if (tid < QT && q0 + tid < a.nq) {
-      uint64_t* h = heap + tid;
-      for (int vi = 0; vi < VT; ++vi) {
-        float dist = ds[tid * VS + vi];
-        if (dist < kSentinelDist) {
-          uint64_t key = make_key(dist, v0 + vi);
+    if (tid < QT) {
+      // the tile's candidates of query tid, inserted in row order (the kept
+      // set does not depend on the order; keys are unique by slot)
+      const uint32_t m = cnt[tid];
+      if (m > 0 && q0 + tid < a.nq) {
+        uint64_t* h = heap + tid;
+        for (uint32_t c = 0; c < m; ++c) {
+          const uint64_t key = make_key(cd[tid * VT + c], v0 + cr[tid * VT + c]);
           if (key < worst) {
             heap_replace_root(h, (int)k, QT, key);
             worst = h[0];
           }
         }
+        wq[tid] = worst;
       }
+      cnt[tid] = 0;
     }
   }
   __syncthreads();
@@ -297,19 +318,41 @@ __global__ void __launch_bounds__(256) merge_partial_topk_kernel(const uint64_t*
 }
 
 size_t flat_f32_smem_bytes(uint32_t k) {
-  size_t floats = (size_t)DK * QS + (size_t)DK * VS + (size_t)QT * VS + QT + VT;
+  size_t floats = (size_t)DK * QS + (size_t)DK * VS + (size_t)QT * VT + QT + VT;
   size_t bytes = floats * 4;
   bytes = (bytes + 7) & ~(size_t)7;
-  return bytes + (size_t)k * QT * 8;
+  // heaps | k-th keys | candidate counts | candidate rows
+  return bytes + (size_t)k * QT * 8 + QT * 8 + QT * 4 + (size_t)QT * VT;
 }
 
 FlatPlan plan_flat_f32(uint32_t n, uint32_t nq, uint32_t k, uint32_t forced_splits) {
   const uint32_t nqb = (nq + QT - 1) / QT;
   const uint32_t ntiles = (n + VT - 1) / VT;
   int sms = device_sm_count();
-  uint32_t splits = forced_splits ? forced_splits : (uint32_t)((2 * sms + nqb - 1) / nqb);
   const uint32_t pow2k = next_pow2(k);
-  splits = std::max(1u, std::min(splits, std::min(ntiles, 8192u / pow2k)));
+  const uint32_t smax = std::max(1u, std::min(ntiles, 8192u / pow2k));  // merge sorts splits * k keys
+  uint32_t splits = forced_splits;
+  if (!splits) {
+    // two CTAs per SM: the fewest splits that give every slot a CTA, or a
+    // few more when that fills the last wave better (a query block count
+    // just above the slot count otherwise leaves a nearly empty wave)
+    const uint64_t slots = 2ull * (uint64_t)sms;
+    const uint32_t s0 = (uint32_t)std::max<uint64_t>(1, (slots + nqb - 1) / nqb);
+    auto fullness = [&](uint32_t sp) {
+      const uint64_t ctas = (uint64_t)nqb * sp, waves = (ctas + slots - 1) / slots;
+      return (double)ctas / (double)(waves * slots);
+    };
+    splits = std::min(s0, smax);
+    double best = fullness(splits);
+    for (uint32_t sp = splits + 1; sp <= std::min(std::max(2 * s0, 8u), smax); ++sp) {
+      const double f = fullness(sp);
+      if (f > best + 0.01) {
+        best = f;
+        splits = sp;
+      }
+    }
+  }
+  splits = std::max(1u, std::min(splits, smax));
   uint32_t tps = (ntiles + splits - 1) / splits;
   splits = (ntiles + tps - 1) / tps;
   FlatPlan p;
