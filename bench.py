@@ -502,7 +502,9 @@ def run_workload(a, world, rank, local):
         roof = {"bound": "fp32", "achieved": flops / (kms / 1e3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": flops / (kms / 1e3) / 1e12 / fp32_peak, "traffic": None, "kernel": kname, "kernel_ms": kms,
                 "peak_source": "nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 x 2.07 GHz (no measured FP32 peak)",
-                "note": "the exact form spends 3 FP32 ops (sub, mul, add) per element for bit-identical sums"}
+                "note": "the exact form spends 3 FP32 ops (sub, mul, add) per element for bit-identical sums",
+                # 3 separately rounded ops per 2 algorithmic flops: the issue bound is a third of the FMA rate
+                "issue_bound": fp32_peak / 3.0, "issue_bound_frac": flops / (kms / 1e3) / 1e12 / (fp32_peak / 3.0)}
         cpu = None
         if not a.no_cpu_baseline:
             sys.path.insert(0, str(ROOT / "oracle"))
