@@ -147,6 +147,21 @@ def dist_setup():
     return world, rank, local
 
 
+def replica_max(values, world, device=None):
+    """Per-rank timings -> their maximum over the ranks. The GPUs run
+    independent replicas of the scan (no data-path collective); this one
+    all_reduce of the clocks is the only exchange. Works on any initialised
+    process group (NCCL on the GPUs, gloo in the CPU tests)."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -314,12 +329,7 @@ def run_ours(a, world, rank, local):
     barrier()
 
     # ---- max over ranks
-    times = torch.tensor([dev_ms / 1e3, e2e_s], dtype=torch.float64, device=dev)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.all_reduce(times, op=dist.ReduceOp.MAX)
-    dev_s, e2e_s = times.tolist()
+    dev_s, e2e_s = replica_max([dev_ms / 1e3, e2e_s], world, dev)
     total_q = a.batch * a.steps * world
     qps = total_q / dev_s
     e2e_qps = total_q / e2e_s
@@ -347,6 +357,10 @@ def run_ours(a, world, rank, local):
     recall = hits / (a.batch * a.k)
 
     if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
         return
     peaks, peak_kind = measured_peaks()
     scan_name = "tc_scan_fp16"
