@@ -531,6 +531,13 @@ def run_workload(a, world, rank, local):
             cdt = time.perf_counter() - t0
             cpu = {"value": a.batch / cdt, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"all {a.batch} queries, exact fp32 search of the full base, {cdt:.2f} s"}
+            # the reference's exact_knn is single-threaded: the same port on one core, on a sample
+            n1 = min(a.batch, 100)
+            t0 = time.perf_counter()
+            oracle.exact_knn(bnp, qnp[:n1], a.k, "l2", threads=1)
+            c1 = time.perf_counter() - t0
+            cpu["single_thread"] = {"value": n1 / c1, "unit": UNIT, "cores": 1,
+                                    "sample": f"{n1} queries on one thread, {c1:.2f} s"}
         cfg = {"workload": "exact fp32 flat L2 scan (integer-valued data, 1,024 components)", "N": a.n, "dim": a.dim,
                "batch": a.batch, "k": a.k, "l2": "base 51 MB < L2: steps hit L2 (a compute-bound kernel)"}
         _line(a, world, a.batch * a.steps / dev_s, UNIT, dev_s,
