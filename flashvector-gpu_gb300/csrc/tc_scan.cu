@@ -136,11 +136,16 @@ __global__ void __launch_bounds__(SEL_THREADS) tc_select_kernel(SelectArgs s) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t total = s.lists * s.kl;
   const uint64_t* src = s.partial + (size_t)q * total;
+  __shared__ uint32_t n_live;
   if (threadIdx.x == 0) incomplete = 0;
-  for (uint32_t i = threadIdx.x; i < s.pow2; i += SEL_THREADS) keys[i] = i < total ? src[i] : kSentinelKey;
-  __syncthreads();
-  block_bitonic_sort(keys, s.pow2);
+  // only the kept keys are sorted (lists that stayed partly empty hold
+  // sentinels); sorted they are the same sequence as the whole table sorted
   const uint32_t kp = min(s.shortlist, total);
+  const uint32_t live = block_compact_keys(src, total, keys, &n_live);
+  const uint32_t sp2 = next_pow2_dev(max(max(live, kp), 2u));
+  for (uint32_t i = live + threadIdx.x; i < sp2; i += SEL_THREADS) keys[i] = kSentinelKey;
+  __syncthreads();
+  block_bitonic_sort(keys, sp2);
   if (s.kl < kp) {
     // a range whose heap stayed full and whose worst kept key still beats the
     // kp-th merged key may have dropped keys that belong in the shortlist
@@ -222,12 +227,20 @@ __global__ void __launch_bounds__(SEL_THREADS) tc_select_kernel(SelectArgs s) {
 __global__ void __launch_bounds__(128) tc_tau_kernel(const uint64_t* __restrict__ partial, uint32_t total,
                                                      uint32_t pow2, uint32_t r, float* __restrict__ tau) {
   extern __shared__ uint64_t keys[];
+  __shared__ uint32_t n_live;
   const uint32_t q = blockIdx.x;
   const uint64_t* src = partial + (size_t)q * total;
-  for (uint32_t i = threadIdx.x; i < pow2; i += blockDim.x) keys[i] = i < total ? src[i] : kSentinelKey;
+  const uint32_t live = block_compact_keys(src, total, keys, &n_live);
+  if (live < r) {
+    // fewer than r sampled keys: no bound
+    if (threadIdx.x == 0) tau[q] = kSentinelDist;
+    return;
+  }
+  const uint32_t sp2 = next_pow2_dev(max(live, 2u));
+  for (uint32_t i = live + threadIdx.x; i < sp2; i += blockDim.x) keys[i] = kSentinelKey;
   __syncthreads();
-  block_bitonic_sort(keys, pow2);
-  if (threadIdx.x == 0) tau[q] = (r <= total && keys[r - 1] != kSentinelKey) ? key_dist(keys[r - 1]) : kSentinelDist;
+  block_bitonic_sort(keys, sp2);
+  if (threadIdx.x == 0) tau[q] = key_dist(keys[r - 1]);
 }
 
 // cuTensorMapEncodeTiled resolved through the runtime, so the library does
