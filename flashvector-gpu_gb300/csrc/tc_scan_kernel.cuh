@@ -491,10 +491,12 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
       tc::tc_fence_before();
       __syncwarp();
       if (lane == 0) {
+        // relaxed: the buffer's TMEM values are in registers (wait::ld); the
+        // arrival must not wait for this lane's shared-bound red.min updates
         if (PAIR && rank != 0)
-          tc::mbar_arrive_cluster(tc::mapa(tc::smem_addr(&acc_empty[buf]), 0));
+          tc::mbar_arrive_cluster_relaxed(tc::mapa(tc::smem_addr(&acc_empty[buf]), 0));
         else
-          tc::mbar_arrive(&acc_empty[buf]);
+          tc::mbar_arrive_relaxed(&acc_empty[buf]);
       }
     }
     if (qvalid) {
