@@ -95,11 +95,11 @@ static __device__ __forceinline__ void heap_down(uint64_t* h, int kl, int i, uin
 }
 
 // Turns kl unordered keys into a max-heap (bottom-up).
-static __device__ __noinline__ void heap_build(uint64_t* h, int kl) {
+static __device__ __forceinline__ void heap_build(uint64_t* h, int kl) {
   for (int i = kl / 2 - 1; i >= 0; --i) heap_down(h, kl, i, h[i * TC_M]);
 }
 
-static __device__ __noinline__ void heap_sift(uint64_t* h, int kl, uint64_t key) {
+static __device__ __forceinline__ void heap_sift(uint64_t* h, int kl, uint64_t key) {
   // replace the root of a max-heap stored with stride TC_M
   int i = 0;
   while (true) {
