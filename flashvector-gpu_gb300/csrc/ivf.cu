@@ -462,13 +462,23 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
         const uint32_t entries = a.m_pq * 256;
         if (cb4) {
           const float4* cbv = reinterpret_cast<const float4*>(a.codebooks);
-#pragma unroll 4
-          for (uint32_t e = tid; e < entries; e += IVF_THREADS) {
-            const float4 w = __ldg(cbv + e);  // codeword (m, c) = row e of 4 floats
+          auto entry = [&](uint32_t e, float4 w) {  // codeword (m, c) = row e of 4 floats
             const float* r = qres + (e >> 8) * 4;
             const float t0 = r[0] - w.x, t1 = r[1] - w.y, t2 = r[2] - w.z, t3 = r[3] - w.w;
             tab[e] = fmaf(t3, t3, fmaf(t2, t2, fmaf(t1, t1, fmaf(t0, t0, 0.f))));
+          };
+          // B codeword loads in flight per thread before any is used (the
+          // codebooks, 16 KB per sub-space, stream from L2 for every list)
+          constexpr uint32_t B = MW >= 2 ? 8 : 4;  // fewer where the register budget is small
+          uint32_t e0 = tid;
+          for (; e0 + (B - 1) * IVF_THREADS < entries; e0 += B * IVF_THREADS) {
+            float4 w[B];
+#pragma unroll
+            for (uint32_t b = 0; b < B; ++b) w[b] = __ldg(cbv + e0 + b * IVF_THREADS);
+#pragma unroll
+            for (uint32_t b = 0; b < B; ++b) entry(e0 + b * IVF_THREADS, w[b]);
           }
+          for (uint32_t e = e0; e < entries; e += IVF_THREADS) entry(e, __ldg(cbv + e));
         } else {
           for (uint32_t e = tid; e < entries; e += IVF_THREADS) {
             const uint32_t m = e >> 8, c = e & 255u;
