@@ -621,11 +621,12 @@ def run_workload(a, world, rank, local):
             cpu = {"value": threads / cdt, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"{threads} queries, exact fp32 search of the full base, {cdt:.1f} s"}
         eff_overfetch = fp8_overfetch or (tuned_knobs or {}).get("overfetch") or 4
-        cfg = {"workload": "fp8 e4m3 flat L2 scan (per-row scales) + fp32 rescore (autotuned over-fetch) + fp64 "
-                           "boundary", "N": a.n, "dim": a.dim, "batch": a.batch, "k": a.k, "overfetch": eff_overfetch,
+        cfg = {"workload": "fp8 e4m3 flat L2 scan (power-of-two scales, row norms as e4m3 digits inside the MMA) + "
+                           "fp32 rescore (autotuned over-fetch) + fp64 boundary", "N": a.n, "dim": a.dim,
+               "padded_dim": table.pd, "batch": a.batch, "k": a.k, "overfetch": eff_overfetch,
                "autotuned": tuned_knobs,
                "mixture": "16384 comps, N(0,1) means, sigma 0.5",
-               "l2": "inputs larger than L2 (0.96 GB fp8 base streamed per step)"}
+               "l2": f"inputs larger than L2 ({a.n * table.pd / 1e9:.2f} GB fp8 base streamed per step)"}
         _line(a, world, qps, UNIT, dev_s,
               {"value": a.batch * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": a.batch * a.dim * 4,
                "d2h_bytes_per_step": a.batch * a.k * 8}, launches, roof, _kernels(prof), clk, cpu, "e4m3", cfg,

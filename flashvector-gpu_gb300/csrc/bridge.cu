@@ -267,6 +267,7 @@ int tc_common(const fv::TcTables& t, const float* q, uint32_t nq, uint32_t top_k
   if ((uintptr_t)t.base % 16 != 0) return FV_ERR_ARG;
   if (metric != METRIC_INNER_PRODUCT && !t.norms) return FV_ERR_NULL;
   if (t.fp8 && !t.scales) return FV_ERR_NULL;
+  if (t.fp8 && t.padded_dim < t.dim + 3) return FV_ERR_ARG;  // room for the three norm digits
   FvScanOptions o{};
   if (opt) o = *opt;
   else o.boundary_fp64 = 1;
@@ -311,8 +312,8 @@ int fv_encode_fp16_padded(const float* d_vectors, uint32_t num_vectors, uint32_t
 
 int fv_encode_fp8(const float* d_vectors, uint32_t num_vectors, uint32_t dim, uint32_t padded_dim,
                   uint8_t* d_out_fp8, float* d_out_scales, float* d_out_norms_sq, void* stream) {
-  if (num_vectors && (!d_vectors || !d_out_fp8 || !d_out_scales)) return FV_ERR_NULL;
-  if (padded_dim < dim || padded_dim % 16) return FV_ERR_ARG;
+  if (num_vectors && (!d_vectors || !d_out_fp8 || !d_out_scales || !d_out_norms_sq)) return FV_ERR_NULL;
+  if (padded_dim < dim + 3 || padded_dim % 16) return FV_ERR_ARG;
   return fv::launch_encode_fp8(d_vectors, num_vectors, dim, padded_dim, d_out_fp8, d_out_scales, d_out_norms_sq,
                                (cudaStream_t)stream);
 }

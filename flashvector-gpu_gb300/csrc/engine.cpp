@@ -479,7 +479,7 @@ int Index::build_from(const float* host, uint32_t n, bool device, const float* d
     if (rc) return rc;
   }
   if (cfg_.build_flags & FV_BUILD_FP8) {
-    pd8_ = (dim + 15) / 16 * 16;
+    pd8_ = (dim + 3 + 15) / 16 * 16;  // three norm-digit columns
     rc = fp8_.alloc((size_t)n * pd8_);
     if (!rc) rc = fp8_scales_.alloc(n);
     if (!rc) rc = fp8_norms_.alloc(n);
@@ -927,7 +927,7 @@ int Index::load_snapshot(const snap::File& f, std::string* error) {
     if (rc) return rc;
   }
   if (cfg_.build_flags & FV_BUILD_FP8) {
-    pd8_ = (dim + 15) / 16 * 16;
+    pd8_ = (dim + 3 + 15) / 16 * 16;  // three norm-digit columns
     rc = fp8_.alloc((size_t)n_ * pd8_);
     if (!rc) rc = fp8_scales_.alloc(n_);
     if (!rc) rc = fp8_norms_.alloc(n_);

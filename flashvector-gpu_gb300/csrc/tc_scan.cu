@@ -36,16 +36,23 @@ namespace {
 // ---------------------------------------------------------------------------
 // Query preparation: fp32 -> fp16 (round to nearest even, as the reference
 // converts queries: ivf_quant_lookup.cu:953) or fp32 -> e4m3 with a per-query
-// scale amax/448; ||q||^2 of the fp32 query (the reference's :922-928, here
-// summed across the warp: it only enters the scan's approximate distance).
-// One warp per query.
+// power-of-two scale s_q = 2^a: the smallest with max|q| <= 448 s_q, raised
+// where needed to 2^(b - 8) (s = 2^b the table's scale) so that the L2
+// norm-digit factor -s / s_q = -2^(b - a) is an e4m3 value; it goes into
+// columns dim..dim+2 against the table's norm digits (0 there for inner
+// product and cosine, and for L2 where b - a < -9: a query so much larger
+// than every row that the rows' norms no longer order the candidates);
+// ||q||^2 of the fp32 query (the reference's :922-928, here summed across
+// the warp: it only enters the scan's approximate distance). One warp per
+// query.
 // ---------------------------------------------------------------------------
 template <bool FP8>
 __global__ void __launch_bounds__(256) tc_prep_queries_kernel(const float* __restrict__ q, uint32_t nq, uint32_t dim,
                                                               uint32_t pd, void* __restrict__ out,
                                                               float* __restrict__ qnorm, float* __restrict__ qscale,
                                                               uint32_t* __restrict__ tslot, uint32_t kl,
-                                                              uint32_t stride) {
+                                                              uint32_t stride, const float* __restrict__ xscale,
+                                                              int metric) {
   const uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (qi >= nq) return;
@@ -66,11 +73,21 @@ __global__ void __launch_bounds__(256) tc_prep_queries_kernel(const float* __res
     for (uint32_t d = lane; d < dim; d += 32) amax = fmaxf(amax, fabsf(src[d]));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-    const float scale = amax > 0.f ? amax / 448.0f : 1.0f;
-    if (lane == 0) qscale[qi] = scale;
+    const int b = ilogbf(__ldg(xscale));
+    int a = b - 8;
+    if (amax > 0.f) {
+      int ap = ilogbf(amax) - 8;
+      for (int it = 0; it < 4 && ldexpf(448.0f, ap) < amax; ++it) ++ap;
+      for (int it = 0; it < 4 && ldexpf(448.0f, ap - 1) >= amax; ++it) --ap;
+      a = max(a, ap);
+    }
+    if (lane == 0) qscale[qi] = ldexpf(1.0f, a);
+    const float digit = (metric == METRIC_L2 && b - a >= -9) ? -ldexpf(1.0f, b - a) : 0.f;
     uint8_t* o8 = static_cast<uint8_t*>(out) + (size_t)qi * pd;
-    for (uint32_t d = lane; d < pd; d += 32)
-      o8[d] = d < dim ? (uint8_t)__nv_cvt_float_to_fp8(src[d] / scale, __NV_SATFINITE, __NV_E4M3) : (uint8_t)0;
+    for (uint32_t d = lane; d < pd; d += 32) {
+      const float v = d < dim ? ldexpf(src[d], -a) : (d < dim + 3 ? digit : 0.f);
+      o8[d] = (uint8_t)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
+    }
   } else {
     __half* o16 = static_cast<__half*>(out) + (size_t)qi * pd;
     for (uint32_t d = lane; d < pd; d += 32) o16[d] = d < dim ? __float2half_rn(src[d]) : __float2half_rn(0.f);
@@ -446,10 +463,11 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
     const uint32_t slot_kl = prepass ? pr : kl;
     if (fp8)
       tc_prep_queries_kernel<true><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm, qscale,
-                                                               tslot, slot_kl, slot_stride);
+                                                               tslot, slot_kl, slot_stride, t.scales, (int)metric);
     else
       tc_prep_queries_kernel<false><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm,
-                                                                qscale, tslot, slot_kl, slot_stride);
+                                                                qscale, tslot, slot_kl, slot_stride, nullptr,
+                                                                (int)metric);
     note_launch();
   }
 

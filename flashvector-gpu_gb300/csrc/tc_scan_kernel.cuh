@@ -132,9 +132,13 @@ static __device__ __forceinline__ float select32(const float* v, int j) {
   return (j & 16) ? t[1] : t[0];
 }
 
-// G epilogue groups: with G = 2 each group owns one of the two TMEM
-// accumulator buffers (tiles alternate between the groups) and keeps its
-// own heaps, which are dumped as separate lists (partial row split * G + g).
+// G epilogue groups, each with its own heaps, dumped as separate lists
+// (partial row split * G + g). With G = 2 a full scan splits columns: both
+// groups drain every tile, group g the columns [128 g, 128 g + 128) of it,
+// so the MMA of tile i + 1 (the other accumulator buffer) runs while tile i
+// is drained. A sampled scan (tile stride > 1, whose tile loads are further
+// apart) alternates tiles instead: group g drains tiles g, g + 2, .., so
+// each group's wait for its next tile overlaps the other group's work.
 //
 // PAIR: the CTA is one of a cluster of two (a cta_group::2 pair) sharing the
 // same base range: CTA r holds query block 2p + r and rows [128 r, 128 r +
@@ -187,6 +191,7 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
     if (!__syncthreads_or(any)) return;
   }
   const uint32_t tstride = a.tile_stride ? a.tile_stride : 1u;
+  const bool col_split = G == 2 && tstride == 1;
   const uint32_t ntiles = ((a.n + TC_N - 1) / TC_N + tstride - 1) / tstride;
   const uint32_t t_begin = split * a.tiles_per_split;
   const uint32_t t_end = min(t_begin + a.tiles_per_split, ntiles);
@@ -199,7 +204,8 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
     }
     for (int b = 0; b < 2; ++b) {
       tc::mbar_init(&acc_full[b], 1);
-      tc::mbar_init(&acc_empty[b], PAIR ? 8 : 4);  // the epilogue warps (of both CTAs) that drain buffer b
+      // the epilogue warps (of both CTAs) that drain buffer b
+      tc::mbar_init(&acc_empty[b], PAIR ? 8 : (col_split ? 4 * G : 4));
     }
     tc::mbar_init(mma_done, 1);
     *abort_flag = 0;
@@ -216,6 +222,9 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
   if constexpr (PAIR) tc::cluster_sync();  // both CTAs' barriers exist before either signals the other's
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  // one K block per tile: the query tile is loaded once (with the first base
+  // tile, into stage 0) and stays resident; only base tiles stream after it
+  const bool a_resident = !PAIR && a.kblocks == 1;
 
   if (warp == 0) {
     // ------------------------------------------------------ TMA producer
@@ -245,9 +254,11 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
             tc::tma_load_2d_pair(sB + stage * b_stage, &tmB, fb, (int32_t)(kb * kb_elems),
                                  row_b + (int32_t)(rank * (TC_N / 2)), pol_b);
           } else {
-            tc::mbar_arrive_expect_tx(&full[stage], A_STAGE + B_STAGE);
-            tc::tma_load_2d(sA + stage * A_STAGE, &tmA, &full[stage], (int32_t)(kb * kb_elems), (int32_t)(qb * TC_M),
-                            pol_a);
+            const bool load_a = !a_resident || i == 0;
+            tc::mbar_arrive_expect_tx(&full[stage], (load_a ? A_STAGE : 0) + B_STAGE);
+            if (load_a)
+              tc::tma_load_2d(sA + stage * A_STAGE, &tmA, &full[stage], (int32_t)(kb * kb_elems),
+                              (int32_t)(qb * TC_M), pol_a);
             tc::tma_load_2d(sB + stage * B_STAGE, &tmB, &full[stage], (int32_t)(kb * kb_elems), row_b, pol_b);
           }
           issued_parity[stage] = (int32_t)phase;
@@ -285,7 +296,7 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
             break;
           }
           tc::tc_fence_after();
-          const uint32_t a_base = tc::smem_addr(sA + stage * A_STAGE);
+          const uint32_t a_base = tc::smem_addr(sA + (a_resident ? 0u : stage * A_STAGE));
           const uint32_t b_base = tc::smem_addr(sB + stage * b_stage);
 #pragma unroll
           for (uint32_t kk = 0; kk < 4; ++kk) {
@@ -330,6 +341,13 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
     const float qn = qvalid ? __ldg(a.qnorm + q) : 0.f;
     const QueryFilter qf = (a.filters && qvalid) ? load_filter(a.filters, q) : QueryFilter{nullptr, 0u, 0u};
     const float qs = (FP8 && qvalid) ? __ldg(a.qscale + q) : 1.f;
+    // fp8 L2 and inner product: the accumulator is the ranking value in the
+    // table's units (L2: the norm digits fold -||x||^2 / (2 s s_q) into the
+    // dot product), v = sc * acc with sc = -2 s s_q (L2) or -s s_q (IP), a
+    // power of two, so the scaling is exact and no per-row data is read
+    constexpr bool FUSED = FP8 && METRIC != METRIC_COSINE;
+    const float sc = FUSED ? (METRIC == METRIC_L2 ? -2.0f : -1.0f) * qs * __ldg(a.xscale) : 1.f;
+    const float inv_sc = FUSED ? __fdiv_rn(1.0f, sc) : 1.f;
     float worst = kSentinelDist;  // this CTA's kl-th best distance (1e30 until the heap is full)
     // admission bound: the query's pre-pass bound, lowered by the shared slots
     float bound = (a.qbound && qvalid) ? __ldg(a.qbound + q) : kSentinelDist;
@@ -353,6 +371,21 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
       }
       if (slots) atomicMin(slots + __umulhi(slot * 2654435761u, (uint32_t)kl), float_order(dist));
     };
+    // admission threshold in the v domain, refreshed when worst or bound
+    // moves: every v whose distance could enter (D(v) < worst and D(v) <=
+    // bound) has v <= thr (for L2 the subtraction of the query norm is padded
+    // by a relative slack, so thr errs on the admitting side; exact tests
+    // follow). Fused fp8 tests the accumulator instead: v <= thr <=> acc >=
+    // thr / sc (sc < 0, a power of two), padded the same way against underflow.
+    float thr = 0.f;
+    auto refresh = [&]() {
+      const float w = fminf(worst, bound);
+      thr = METRIC == METRIC_L2 ? (w - qn) + 1e-6f * (fabsf(w) + fabsf(qn)) + 1e-30f : w;
+      if (FUSED) {
+        thr *= inv_sc;
+        thr -= 1e-6f * fabsf(thr) + 1e-37f;
+      }
+    };
 
     // per-warp copy of the current tile's column data (norms, fp8 factors,
     // mask words): staged by the warp itself, so the epilogue warps never
@@ -368,9 +401,9 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
       for (int r = 0; r < TC_N / 32; ++r) {
         const uint32_t slot = v0n + lane + 32 * r;
         const bool in = slot < a.n;
-        pre_n[r] = (METRIC != METRIC_INNER_PRODUCT && in) ? __ldg(a.xnorm + slot) : 0.f;
-        // per-column factor of the scaled dot: -2 xs (L2), -xs (IP), xs (cosine)
-        const float xs = (FP8 && in) ? __ldg(a.xscale + slot) : 0.f;
+        pre_n[r] = (METRIC != METRIC_INNER_PRODUCT && !FUSED && in) ? __ldg(a.xnorm + slot) : 0.f;
+        // per-column factor of the scaled dot: xs (cosine; fp8 L2 and IP need none)
+        const float xs = (FP8 && !FUSED && in) ? __ldg(a.xscale + slot) : 0.f;
         pre_s[r] = METRIC == METRIC_L2 ? -2.0f * xs : (METRIC == METRIC_INNER_PRODUCT ? -xs : xs);
       }
       pre_m = 0;
@@ -383,19 +416,22 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
         }
       }
     };
-    if ((uint32_t)grp < my_tiles) prefetch((uint32_t)grp);
-    for (uint32_t i = (uint32_t)grp; i < my_tiles; i += G) {
+    // this group's tiles (first, step) and columns [c_lo, c_hi) of each
+    const uint32_t t_first = col_split ? 0u : (uint32_t)grp, t_step = col_split ? 1u : (uint32_t)G;
+    const int c_lo = col_split ? grp * (TC_N / G) : 0, c_hi = col_split ? c_lo + TC_N / G : TC_N;
+    if (t_first < my_tiles) prefetch(t_first);
+    for (uint32_t i = t_first; i < my_tiles; i += t_step) {
       const uint32_t buf = i & 1, use = i >> 1;
       const uint32_t v0 = (t_begin + i) * tstride * TC_N;
       __syncwarp();
 #pragma unroll
       for (int r = 0; r < TC_N / 32; ++r) {
-        if (METRIC != METRIC_INNER_PRODUCT) cb[lane + 32 * r] = pre_n[r];
-        if (FP8) cb[TC_N + lane + 32 * r] = pre_s[r];
+        if (METRIC != METRIC_INNER_PRODUCT && !FUSED) cb[lane + 32 * r] = pre_n[r];
+        if (FP8 && !FUSED) cb[TC_N + lane + 32 * r] = pre_s[r];
       }
       if (lane < 8) cm[lane] = pre_m;
       __syncwarp();
-      if (i + G < my_tiles) prefetch(i + G);
+      if (i + t_step < my_tiles) prefetch(i + t_step);
       // the shared bound, loaded before the accumulator wait hides its latency
       uint32_t smax = 0;
       if (slots)
@@ -406,10 +442,11 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
       if (!tc::mbar_wait(&acc_full[buf], use & 1, abort_flag, a.status)) break;
       tc::tc_fence_after();
       if (slots && smax != 0xFFFFFFFFu) bound = fminf(bound, order_float(smax));
+      refresh();
 
       const uint32_t t_row = tmem + ((uint32_t)(quad * 32) << 16) + buf * TC_N;
 #pragma unroll 1
-      for (int c0 = 0; c0 < TC_N; c0 += 64) {
+      for (int c0 = c_lo; c0 < c_hi; c0 += 64) {
         uint32_t ra[32], rb[32];
         __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent insertions
         tc::tmem_ld32_async(t_row + c0, ra);
@@ -426,9 +463,12 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
         // c0+32..; the distance is D(v): L2  D(v) = max(0, ||q||^2 + v) with
         // v = ||x||^2 - 2 <q, x> (the query's norm is added after the
         // minimum, D being monotone), IP  D(v) = v = -<q, x>, cosine the
-        // full expression. FP8 dots carry the per-query and per-row scales.
+        // full expression. FP8 cosine dots carry the query and table scales.
         float v[64];
-        if (METRIC == METRIC_COSINE) {
+        if constexpr (FUSED) {
+#pragma unroll
+          for (int j = 0; j < 64; ++j) v[j] = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
+        } else if (METRIC == METRIC_COSINE) {
 #pragma unroll
           for (int j = 0; j < 64; ++j) {
             float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
@@ -437,55 +477,56 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
           }
         } else {
           const float4* nb = reinterpret_cast<const float4*>(cb + c0);
-          const float4* sb = reinterpret_cast<const float4*>(cb + TC_N + c0);
 #pragma unroll
           for (int j4 = 0; j4 < 16; ++j4) {
             const float4 n4 = METRIC == METRIC_L2 ? nb[j4] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 s4 = FP8 ? sb[j4] : make_float4(0.f, 0.f, 0.f, 0.f);
             const float nv[4] = {n4.x, n4.y, n4.z, n4.w};
-            const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
               const int j = 4 * j4 + e;
               const float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
-              if (FP8)
-                v[j] = METRIC == METRIC_L2 ? fmaf(dot * qs, sv[e], nv[e]) : (dot * qs) * sv[e];
-              else
-                v[j] = METRIC == METRIC_L2 ? fmaf(-2.0f, dot, nv[e]) : -dot;
+              v[j] = METRIC == METRIC_L2 ? fmaf(-2.0f, dot, nv[e]) : -dot;
             }
           }
         }
-        auto D = [&](float x) { return METRIC == METRIC_L2 ? fmaxf(0.f, qn + x) : x; };
-        // admission threshold in the v domain: every v whose distance could
-        // enter (D(v) < worst and D(v) <= bound) has v <= thr (for L2 the
-        // subtraction of the query norm is padded by a relative slack, so
-        // thr errs on the admitting side; exact tests follow)
-        const float w = fminf(worst, bound);
-        const float thr = METRIC == METRIC_L2 ? (w - qn) + 1e-6f * (fabsf(w) + fabsf(qn)) + 1e-30f : w;
-        // pairwise minima, then a min tree: a 64-column batch whose minimum
-        // cannot enter is skipped whole (the common case once warm)
-        float m1[32], m[16];
+        // D: distance from v (fused fp8: from the accumulator, v = sc * acc)
+        auto D = [&](float x) {
+          if (FUSED) x *= sc;
+          return METRIC == METRIC_L2 ? fmaxf(0.f, qn + x) : x;
+        };
+        // better(x, y): the smaller v, i.e. the larger accumulator when fused
+        auto better = [](float x, float y) { return FUSED ? fmaxf(x, y) : fminf(x, y); };
+        auto may = [&](float x) { return FUSED ? x >= thr : x <= thr; };
+        // pairwise best, then a tree: a 64-column batch whose best cannot
+        // enter is skipped whole (the common case once warm)
+        float m1[32], m2[16], m3[8], t4[4];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) m1[j] = fminf(v[j], v[j + 32]);
+        for (int j = 0; j < 32; ++j) m1[j] = better(v[j], v[j + 32]);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) m[j] = fminf(m1[j], m1[j + 16]);
+        for (int j = 0; j < 16; ++j) m2[j] = better(m1[j], m1[j + 16]);
 #pragma unroll
-        for (int t = 8; t > 0; t >>= 1)
+        for (int j = 0; j < 8; ++j) m3[j] = better(m2[j], m2[j + 8]);
 #pragma unroll
-          for (int j = 0; j < t; ++j) m[j] = fminf(m[j], m[j + t]);
-        if (!(m[0] <= thr)) continue;
+        for (int j = 0; j < 4; ++j) t4[j] = better(m3[j], m3[j + 4]);
+        if (!(mw != 0ull && may(better(better(t4[0], t4[2]), better(t4[1], t4[3]))))) continue;
         // pairs (j, j+32) that may hold a candidate, walked lane-parallel
         uint32_t pass = 0;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) pass |= (uint32_t)(m1[j] <= thr) << j;
+        for (int j = 0; j < 32; ++j) pass |= (uint32_t)may(m1[j]) << j;
         pass &= (uint32_t)mw | (uint32_t)(mw >> 32);
         while (pass) {
           const int j = __ffs(pass) - 1;
           pass &= pass - 1;
           const float dlo = D(select32(v, j));
           const float dhi = D(select32(v + 32, j));
-          if (((mw >> j) & 1ull) && dlo < worst && dlo <= bound) keep(dlo, v0 + c0 + j);
-          if (((mw >> (j + 32)) & 1ull) && dhi < worst && dhi <= bound) keep(dhi, v0 + c0 + j + 32);
+          if (((mw >> j) & 1ull) && dlo < worst && dlo <= bound) {
+            keep(dlo, v0 + c0 + j);
+            refresh();
+          }
+          if (((mw >> (j + 32)) & 1ull) && dhi < worst && dhi <= bound) {
+            keep(dhi, v0 + c0 + j + 32);
+            refresh();
+          }
         }
       }
       tc::tc_fence_before();

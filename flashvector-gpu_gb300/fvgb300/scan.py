@@ -94,10 +94,16 @@ def encode_fp16(vectors, pd=None, stream=None):
     return out, norms
 
 
+def fp8_padded_dim(dim: int) -> int:
+    """Row length of an fp8 table: dim codes + three norm digits, to 16."""
+    return padded_dim(dim + 3)
+
+
 def encode_fp8(vectors, pd=None, stream=None):
-    """fv_encode_fp8: e4m3 rows with per-row scales + compensated ||x||^2."""
+    """fv_encode_fp8: e4m3 rows at the table's power-of-two scale, three
+    norm digits, the scale (per row, all equal) and compensated ||x||^2."""
     n, dim = vectors.shape
-    pd = pd or padded_dim(dim)
+    pd = pd or fp8_padded_dim(dim)
     out = torch.empty((n, pd), dtype=torch.uint8, device=vectors.device)
     scales = torch.empty((n,), dtype=torch.float32, device=vectors.device)
     norms = torch.empty((n,), dtype=torch.float32, device=vectors.device)
@@ -121,7 +127,7 @@ class Fp16Table:
 class Fp8Table:
     def __init__(self, vectors, keep_fp32=True, stream=None):
         self.n, self.dim = vectors.shape
-        self.pd = padded_dim(self.dim)
+        self.pd = fp8_padded_dim(self.dim)
         self.fp8, self.scales, self.norms = encode_fp8(vectors, self.pd, stream)
         self.fp32 = vectors if keep_fp32 else None
         self.struct = _lib.FvFp8GpuTables(self.fp8.data_ptr(), self.scales.data_ptr(), self.norms.data_ptr(),

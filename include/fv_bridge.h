@@ -196,9 +196,11 @@ int fv_fp16_search_batch_ex(const Fp16GpuTables* tables, const float* d_queries,
                             const uint32_t* d_valid_mask, const FvScanOptions* options,
                             GpuSearchResult* d_out_results, void* stream);
 
-/* FP8 (E4M3, per-row scale) tensor-core flat scan; same contract as the
- * fp16 scan, the per-query scale is amax(|q|)/448. No reference
- * counterpart (the reference has no fp8 path). */
+/* FP8 (E4M3) tensor-core flat scan over a table written by fv_encode_fp8
+ * (padded_dim >= dim + 3); same contract as the fp16 scan. Queries get a
+ * power-of-two scale (the smallest 2^a with max|q| <= 448 * 2^a, at least
+ * 2^(b-8) for the table scale 2^b). No reference counterpart (the
+ * reference has no fp8 path). */
 int fv_fp8_search_batch(const FvFp8GpuTables* tables, const float* d_queries,
                         uint32_t num_queries, uint32_t top_k, MetricType metric,
                         const uint32_t* d_valid_mask, const FvScanOptions* options,
@@ -206,8 +208,9 @@ int fv_fp8_search_batch(const FvFp8GpuTables* tables, const float* d_queries,
 
 /* Device-side table encoders. fv_encode_fp16_padded restates the
  * reference's host encoder encode_fp16_padded (quant.rs:306-327, rounding
- * of quant.rs:239-274). fv_encode_fp8 has no counterpart. padded_dim must
- * be a multiple of 16 and >= dim. */
+ * of quant.rs:239-274); padded_dim a multiple of 16, >= dim.
+ * fv_encode_fp8 has no counterpart: the layout of FvFp8GpuTables
+ * (padded_dim a multiple of 16, >= dim + 3; all three outputs required). */
 int fv_encode_fp16_padded(const float* d_vectors, uint32_t num_vectors, uint32_t dim,
                           uint32_t padded_dim, uint16_t* d_out_fp16, float* d_out_norms_sq,
                           void* stream);

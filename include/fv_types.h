@@ -103,10 +103,15 @@ typedef struct {
     uint32_t padded_dim;
 } Fp16GpuTables;
 
-/* FP8 (E4M3) flat tables; no reference counterpart. Row v of d_vectors_fp8
- * holds round_e4m3(x_v[d] / d_scales[v]) for d < dim and zero padding up to
- * padded_dim (a multiple of 32). d_scales[v] = max|x_v| / 448 (1 for a zero
- * row). d_vec_norms_sq holds ||x_v||^2 of the fp32 row. */
+/* FP8 (E4M3) flat tables; no reference counterpart. One power-of-two
+ * scale s = 2^b for the table, the smallest with max_v ||x_v||^2 <= 896 s^2
+ * (1 for an all-zero table); every d_scales[v] holds s. Row v of
+ * d_vectors_fp8 holds round_e4m3(x_v[d] / s) for d < dim (round to nearest
+ * even), then three norm digits n1, n2, n3 at columns dim..dim+2 (n1 the
+ * e4m3 value nearest ||x_v||^2 / (2 s^2), n2 and n3 the e4m3 values nearest
+ * what the earlier digits leave), then zero padding up to padded_dim (a
+ * multiple of 16, >= dim + 3). d_vec_norms_sq holds ||x_v||^2 of the fp32
+ * row (compensated sum). */
 typedef struct {
     const uint8_t* d_vectors_fp8;   /* [num_vectors * padded_dim] E4M3 bytes     */
     const float* d_scales;          /* [num_vectors] per-vector dequant scale    */

@@ -70,20 +70,109 @@ def test_encode_fp16_matches_oracle(cuda, oracle_mod):
     assert np.array_equal(norms.cpu().numpy().view(np.uint32), ref_norms.view(np.uint32))
 
 
+def fp8_table_exponent(max_norm):
+    """Smallest b with max_norm <= 896 * 4^b (0 for an all-zero table)."""
+    if not max_norm > 0:
+        return 0
+    b = -62
+    while b < 62 and np.ldexp(np.float32(896.0), 2 * b) < max_norm:
+        b += 1
+    return b
+
+
+def fp8_query_exponent(q, b):
+    """Smallest a with max|q| <= 448 * 2^a, at least b - 8."""
+    amax = np.float32(np.abs(q).max())
+    a = b - 8
+    if amax > 0:
+        ap = -200
+        while np.ldexp(np.float32(448.0), ap) < amax:
+            ap += 1
+        a = max(a, ap)
+    return a
+
+
+def e4m3(torch, x):
+    return torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).cuda().to(torch.float8_e4m3fn)
+
+
 def test_encode_fp8(cuda):
+    """One power-of-two scale for the table, e4m3 codes at that scale, three
+    norm digits summing to ||x||^2 / (2 s^2), zero padding."""
     from fvgb300 import scan
 
     torch = cuda
     rng = np.random.default_rng(1)
     x = rng.standard_normal((500, 96)).astype(np.float32)
     x[3] = 0.0
+    x[7] *= np.float32(1e-3)
+    x[8] *= np.float32(40.0)
     codes, scales, norms = scan.encode_fp8(torch.from_numpy(x).cuda())
-    amax = np.abs(x).max(axis=1)
-    exp_scale = np.where(amax > 0, amax / np.float32(448.0), 1.0).astype(np.float32)
-    assert np.array_equal(scales.cpu().numpy(), exp_scale)
-    ref = (torch.from_numpy(x).cuda() / scales[:, None]).to(torch.float8_e4m3fn).view(torch.uint8)
+    assert codes.shape == (500, scan.fp8_padded_dim(96)) == (500, 112)
+    nrm = norms.cpu().numpy()
+    assert np.allclose(nrm, (x.astype(np.float64) ** 2).sum(1), rtol=1e-6)
+    b = fp8_table_exponent(nrm.max())
+    assert np.ldexp(np.float32(896.0), 2 * b - 2) < nrm.max() <= np.ldexp(np.float32(896.0), 2 * b)
+    assert np.all(scales.cpu().numpy() == np.ldexp(np.float32(1.0), b))
+    ref = e4m3(torch, np.ldexp(x, -b)).view(torch.uint8)
     assert torch.equal(codes[:, :96], ref)
-    assert np.allclose(norms.cpu().numpy(), (x.astype(np.float64) ** 2).sum(1), rtol=1e-6)
+    r = np.ldexp(nrm, -1 - 2 * b).astype(np.float32)
+    want = r.copy()
+    for i in range(3):
+        c = e4m3(torch, r)
+        assert torch.equal(codes[:, 96 + i], c.view(torch.uint8))
+        r = (r - c.float().cpu().numpy()).astype(np.float32)
+    assert np.all(np.abs(r) <= want * 2.0 ** -11 + 2.0 ** -10)
+    assert torch.all(codes[:, 99:] == 0)
+    assert torch.all(codes[3] == 0)
+    # the all-zero table: scale 1, zero codes
+    z_codes, z_scales, _ = scan.encode_fp8(torch.zeros((4, 20), device="cuda"))
+    assert torch.all(z_codes == 0) and torch.all(z_scales == 1.0)
+
+
+@pytest.mark.parametrize("metric", ["ip", "l2", "cosine"])
+@pytest.mark.parametrize("n,dim,nq,k", [(20000, 96, 200, 10), (5003, 70, 129, 16), (1000, 128, 1, 5),
+                                        (257, 253, 64, 10)])
+def test_fp8_scan_ranking_without_rescore(cuda, metric, n, dim, nq, k):
+    """No fp32 copy: results are the top-k of the fp8 tensor-core distance
+    (L2 through the norm digits). Checked against an fp64 evaluation of the
+    same e4m3 products."""
+    from fvgb300 import scan
+
+    torch = cuda
+    rng = np.random.default_rng(n + dim)
+    base = (rng.standard_normal((n, dim)) + rng.standard_normal((32, dim))[rng.integers(0, 32, n)]).astype(np.float32)
+    base *= rng.uniform(0.5, 2.0, (n, 1)).astype(np.float32)
+    queries = (rng.standard_normal((nq, dim)) * 1.3).astype(np.float32)
+    table = scan.Fp8Table(torch.from_numpy(base).cuda(), keep_fp32=False)
+    res = scan.fp8_search(table, torch.from_numpy(queries).cuda(), k, metric, opts=scan.options(boundary_fp64=0))
+    torch.cuda.synchronize()
+    ids, dist = res_np(res)
+    s = np.float64(table.scales[0].item())
+    b = int(np.log2(s))
+    x8 = table.fp8.view(torch.float8_e4m3fn).double().cpu().numpy()
+    xn = table.norms.cpu().numpy().astype(np.float64)
+    qn = (queries.astype(np.float64) ** 2).sum(1)
+    a = np.array([fp8_query_exponent(q, b) for q in queries])
+    q8 = np.stack([e4m3(torch, np.ldexp(q, -int(ai))).double().cpu().numpy() for q, ai in zip(queries, a)])
+    dots = q8 @ x8[:, :dim].T
+    qs = np.ldexp(1.0, a)
+    if metric == "l2":
+        c = np.where(b - a >= -9, -np.ldexp(1.0, b - a), 0.0)
+        acc = dots + c[:, None] * x8[:, dim:dim + 3].sum(1)[None, :]
+        d64 = np.maximum(0, qn[:, None] - 2 * (qs * s)[:, None] * acc)
+    elif metric == "ip":
+        d64 = -(qs * s)[:, None] * dots
+    else:
+        d64 = 1 - (qs * s)[:, None] * dots / (np.sqrt(qn[:, None] * xn[None, :]) + 1e-8)
+    order = np.argsort(d64, axis=1, kind="stable")[:, :k]
+    hit = np.mean([len(set(ids[i]) & set(order[i])) / k for i in range(nq)])
+    assert hit >= 0.995, hit
+    got = np.take_along_axis(d64, ids.astype(np.int64), axis=1)
+    scale = np.abs(d64).max(axis=1, keepdims=True)
+    assert np.all(np.abs(dist - got) <= 2e-5 * np.maximum(scale, 1.0)), np.abs(dist - got).max()
+    assert np.all(dist[:, :-1] <= dist[:, 1:])
+    assert scan.device_status() == 0
 
 
 @pytest.mark.parametrize("metric", ["ip", "l2", "cosine"])
