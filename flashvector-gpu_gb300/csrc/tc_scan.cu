@@ -340,9 +340,10 @@ uint32_t poisson_rank(double lambda, double tail) {
 
 // One CTA per SM at a time: a grid of nqb * splits CTAs runs in
 // ceil(nqb * splits / sms) waves, the last one possibly part-empty. Among
-// split counts in [s_min, 2 s_min] (within the tile count and the select
-// kernel's 16,384-key sort), take the smallest whose waves are at least
-// 1% fuller than those of every smaller candidate.
+// split counts in [s_min, max(2 s_min, 32)] (within the tile count and the
+// select kernel's 16,384-key sort), take the smallest whose waves are at
+// least 1% fuller than those of every smaller candidate (a grid of 79 query
+// blocks x 1 split fills 53% of 148 SMs; x 13 splits, 99%).
 uint32_t fill_waves(uint32_t s_min, uint32_t nqb, uint32_t ntiles, uint32_t sms, uint32_t keys_per_split) {
   auto fullness = [&](uint32_t s) {
     const uint64_t ctas = (uint64_t)nqb * s, waves = (ctas + sms - 1) / sms;
@@ -350,7 +351,7 @@ uint32_t fill_waves(uint32_t s_min, uint32_t nqb, uint32_t ntiles, uint32_t sms,
   };
   uint32_t best = s_min;
   double best_f = fullness(s_min);
-  for (uint32_t s = s_min + 1; s <= 2 * s_min && s <= ntiles; ++s) {
+  for (uint32_t s = s_min + 1; s <= std::max(2 * s_min, 32u) && s <= ntiles; ++s) {
     if (next_pow2(s * keys_per_split) > 16384u) break;
     const double f = fullness(s);
     if (f > best_f + 0.01) {

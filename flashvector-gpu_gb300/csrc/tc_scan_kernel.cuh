@@ -497,18 +497,30 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
         // better(x, y): the smaller v, i.e. the larger accumulator when fused
         auto better = [](float x, float y) { return FUSED ? fmaxf(x, y) : fminf(x, y); };
         auto may = [&](float x) { return FUSED ? x >= thr : x <= thr; };
-        // pairwise best, then a tree: a 64-column batch whose best cannot
-        // enter is skipped whole (the common case once warm)
-        float m1[32], m2[16], m3[8], t4[4];
+        // a tree of three-input bests: a 64-column batch whose best cannot
+        // enter is skipped whole (the common case once warm); the pairwise
+        // bests (j, j + 32) are formed only for a batch that passes
+        // best of three in one instruction (three-input min / max)
+        auto best3 = [](float x, float y, float z) {
+          float d;
+          if (FUSED)
+            asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(x), "f"(y), "f"(z));
+          else
+            asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(x), "f"(y), "f"(z));
+          return d;
+        };
+        float r[22], s8[8];
+#pragma unroll
+        for (int i = 0; i < 21; ++i) r[i] = best3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+        r[21] = v[63];
+#pragma unroll
+        for (int i = 0; i < 7; ++i) s8[i] = best3(r[3 * i], r[3 * i + 1], r[3 * i + 2]);
+        s8[7] = r[21];
+        const float top = best3(best3(s8[0], s8[1], s8[2]), best3(s8[3], s8[4], s8[5]), better(s8[6], s8[7]));
+        if (!(mw != 0ull && may(top))) continue;
+        float m1[32];
 #pragma unroll
         for (int j = 0; j < 32; ++j) m1[j] = better(v[j], v[j + 32]);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) m2[j] = better(m1[j], m1[j + 16]);
-#pragma unroll
-        for (int j = 0; j < 8; ++j) m3[j] = better(m2[j], m2[j + 8]);
-#pragma unroll
-        for (int j = 0; j < 4; ++j) t4[j] = better(m3[j], m3[j + 4]);
-        if (!(mw != 0ull && may(better(better(t4[0], t4[2]), better(t4[1], t4[3]))))) continue;
         // pairs (j, j+32) that may hold a candidate, walked lane-parallel
         uint32_t pass = 0;
 #pragma unroll
