@@ -52,10 +52,19 @@ __global__ void __launch_bounds__(256) tc_prep_queries_kernel(const float* __res
                                                               float* __restrict__ qnorm, float* __restrict__ qscale,
                                                               uint32_t* __restrict__ tslot, uint32_t kl,
                                                               uint32_t stride, const float* __restrict__ xscale,
-                                                              int metric) {
+                                                              int metric, uint32_t nq_rows) {
   const uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (qi >= nq) return;
+  if (qi >= nq_rows) return;
+  if (qi >= nq) {
+    // padding rows up to a whole query block: zero codes, so that every TMA
+    // load of a query tile is in bounds (an out-of-bounds fill of most of a
+    // 128-row tile, reloaded per K block, slowed a one-query scan by 40%)
+    const size_t row_bytes = (size_t)pd * (FP8 ? 1 : 2);
+    uint8_t* o = static_cast<uint8_t*>(out) + (size_t)qi * row_bytes;
+    for (size_t b = (size_t)lane * 16; b < row_bytes; b += 32 * 16) *reinterpret_cast<uint4*>(o + b) = make_uint4(0, 0, 0, 0);
+    return;
+  }
   const float* src = q + (size_t)qi * dim;
   // shared-bound slots: empty (all ones) for the kl used, 0 for the padding
   for (uint32_t s = lane; s < stride; s += 32) tslot[(size_t)qi * stride + s] = s < kl ? 0xFFFFFFFFu : 0u;
@@ -436,7 +445,10 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
 
   // scratch: prepared queries | ||q||^2 | q scales | partial heaps | slots
   //          [| pre-pass heaps | tau | redo flags]
-  const size_t q_bytes = align_up((size_t)nq * t.padded_dim * elem, 1024);
+  // prepared queries padded with zero rows to whole query blocks (of the
+  // CTA pairs' grid when pairs run)
+  const uint32_t nq_rows = nqb_grid * TC_M;
+  const size_t q_bytes = align_up((size_t)nq_rows * t.padded_dim * elem, 1024);
   const size_t qn_bytes = align_up((size_t)nq * 4, 256);
   const size_t part_bytes = align_up((size_t)nq * splits * groups * kl * 8, 256);
   const uint32_t slot_stride = ((prepass ? std::max(kl, pr) : kl) + 3) / 4 * 4;
@@ -458,22 +470,23 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
 
   {
     ProfScope ps(fp8 ? "tc_prep_queries_fp8" : "tc_prep_queries_fp16", stream);
-    const uint32_t blocks = (nq * 32 + 255) / 256;
+    const uint32_t blocks = (nq_rows * 32 + 255) / 256;
     // the shared-bound slots serve the scan that shares a bound: the main
     // scan when its heap holds the whole shortlist, else the pre-pass
     const uint32_t slot_kl = prepass ? pr : kl;
     if (fp8)
       tc_prep_queries_kernel<true><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm, qscale,
-                                                               tslot, slot_kl, slot_stride, t.scales, (int)metric);
+                                                               tslot, slot_kl, slot_stride, t.scales, (int)metric,
+                                                               nq_rows);
     else
       tc_prep_queries_kernel<false><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm,
                                                                 qscale, tslot, slot_kl, slot_stride, nullptr,
-                                                                (int)metric);
+                                                                (int)metric, nq_rows);
     note_launch();
   }
 
   CUtensorMap ta, tb, tb_half;
-  if (!encode_tmap(&ta, qprep, fp8, t.padded_dim, nq, (uint64_t)t.padded_dim * elem, TC_M) ||
+  if (!encode_tmap(&ta, qprep, fp8, t.padded_dim, nq_rows, (uint64_t)t.padded_dim * elem, TC_M) ||
       !encode_tmap(&tb, t.base, fp8, t.padded_dim, t.n, (uint64_t)t.padded_dim * elem, TC_N) ||
       (pair && !encode_tmap(&tb_half, t.base, fp8, t.padded_dim, t.n, (uint64_t)t.padded_dim * elem, TC_N / 2)))
     return FV_ERR_ARG;
