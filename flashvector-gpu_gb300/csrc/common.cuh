@@ -138,18 +138,43 @@ __device__ __forceinline__ float warp_tree_sum(float v) {
 
 __device__ __forceinline__ float warp_metric_distance(const float* __restrict__ q, const float* __restrict__ x,
                                                       uint32_t dim, int lane, MetricType metric) {
+  // The lane-strided elements are loaded eight steps ahead of the
+  // accumulation, which keeps the per-lane fmaf order (and so the result
+  // bit for bit) while a row's loads are in flight together.
+  constexpr int B = 8;
   if (metric == METRIC_INNER_PRODUCT) {
     float dot = 0.f;
-    for (uint32_t d = lane; d < dim; d += 32) dot = fmaf(q[d], __ldg(x + d), dot);
+    for (uint32_t d0 = lane; d0 < dim; d0 += 32 * B) {
+      float qa[B], xa[B];
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        const uint32_t d = d0 + 32 * b;
+        qa[b] = d < dim ? q[d] : 0.f;
+        xa[b] = d < dim ? __ldg(x + d) : 0.f;
+      }
+#pragma unroll
+      for (int b = 0; b < B; ++b)
+        if (d0 + 32 * b < dim) dot = fmaf(qa[b], xa[b], dot);
+    }
     return -warp_tree_sum(dot);
   }
   if (metric == METRIC_COSINE) {
     float dot = 0.f, nq = 0.f, nx = 0.f;
-    for (uint32_t d = lane; d < dim; d += 32) {
-      float a = q[d], b = __ldg(x + d);
-      dot = fmaf(a, b, dot);
-      nq = fmaf(a, a, nq);
-      nx = fmaf(b, b, nx);
+    for (uint32_t d0 = lane; d0 < dim; d0 += 32 * B) {
+      float qa[B], xa[B];
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        const uint32_t d = d0 + 32 * b;
+        qa[b] = d < dim ? q[d] : 0.f;
+        xa[b] = d < dim ? __ldg(x + d) : 0.f;
+      }
+#pragma unroll
+      for (int b = 0; b < B; ++b)
+        if (d0 + 32 * b < dim) {
+          dot = fmaf(qa[b], xa[b], dot);
+          nq = fmaf(qa[b], qa[b], nq);
+          nx = fmaf(xa[b], xa[b], nx);
+        }
     }
     dot = warp_tree_sum(dot);
     nq = warp_tree_sum(nq);
@@ -158,9 +183,20 @@ __device__ __forceinline__ float warp_metric_distance(const float* __restrict__ 
     return __fsub_rn(1.0f, __fdiv_rn(dot, denom));
   }
   float acc = 0.f;
-  for (uint32_t d = lane; d < dim; d += 32) {
-    float diff = q[d] - __ldg(x + d);
-    acc = fmaf(diff, diff, acc);
+  for (uint32_t d0 = lane; d0 < dim; d0 += 32 * B) {
+    float qa[B], xa[B];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      const uint32_t d = d0 + 32 * b;
+      qa[b] = d < dim ? q[d] : 0.f;
+      xa[b] = d < dim ? __ldg(x + d) : 0.f;
+    }
+#pragma unroll
+    for (int b = 0; b < B; ++b)
+      if (d0 + 32 * b < dim) {
+        const float diff = qa[b] - xa[b];
+        acc = fmaf(diff, diff, acc);
+      }
   }
   return warp_tree_sum(acc);
 }

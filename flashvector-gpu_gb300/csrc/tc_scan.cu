@@ -108,15 +108,27 @@ __global__ void __launch_bounds__(256) tc_prep_queries_kernel(const float* __res
 __device__ double warp_distance_f64(const float* __restrict__ q, const float* __restrict__ x, uint32_t dim, int lane,
                                     int metric) {
   double a = 0.0, b = 0.0, c = 0.0;
-  for (uint32_t d = lane; d < dim; d += 32) {
-    const double u = q[d], w = __ldg(x + d);
-    if (metric == METRIC_L2) {
-      const double t = u - w;
-      a += t * t;
-    } else {
-      a += u * w;
-      b += u * u;
-      c += w * w;
+  constexpr int B = 8;  // loads in flight ahead of the (ordered) accumulation
+  for (uint32_t d0 = lane; d0 < dim; d0 += 32 * B) {
+    float qa[B], xa[B];
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      const uint32_t d = d0 + 32 * i;
+      qa[i] = d < dim ? q[d] : 0.f;
+      xa[i] = d < dim ? __ldg(x + d) : 0.f;
+    }
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      if (d0 + 32 * i >= dim) break;
+      const double u = qa[i], w = xa[i];
+      if (metric == METRIC_L2) {
+        const double t = u - w;
+        a += t * t;
+      } else {
+        a += u * w;
+        b += u * u;
+        c += w * w;
+      }
     }
   }
 #pragma unroll
@@ -202,10 +214,14 @@ __global__ void __launch_bounds__(SEL_THREADS) tc_select_kernel(SelectArgs s) {
     block_bitonic_sort(keys, p2);
 
     if (s.boundary && s.k <= kp && keys[s.k - 1] != kSentinelKey) {
+      // ||q||^2 for the band's width, summed by warp 0 (lane-strided, tree)
+      float qn = 0.f;
+      if (warp == 0) {
+        for (uint32_t d = lane; d < s.dim; d += 32) qn = fmaf(qv[d], qv[d], qn);
+        qn = warp_tree_sum(qn);
+      }
       if (threadIdx.x == 0) {
         const float dk = key_dist(keys[s.k - 1]);
-        float qn = 0.f;
-        for (uint32_t d = 0; d < s.dim; ++d) qn = fmaf(qv[d], qv[d], qn);
         // scale of the accumulated terms: |d_k| for L2; |q||x| bounds |dot|
         float scale = fabsf(dk) + (s.metric == METRIC_L2 ? 0.f : sqrtf(qn) * 2.0f);
         const float band = s.eps * scale;

@@ -36,15 +36,24 @@ __device__ __forceinline__ uint32_t block_compact_keys(const uint64_t* __restric
   const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0) *counter = 0;
   __syncthreads();
-  for (uint32_t i0 = 0; i0 < total; i0 += blockDim.x) {
-    const uint32_t i = i0 + threadIdx.x;
-    const uint64_t key = i < total ? src[i] : kSentinelKey;
-    const bool keep = key != kSentinelKey;
-    const uint32_t m = __ballot_sync(0xffffffffu, keep);
-    uint32_t base = 0;
-    if (lane == 0 && m) base = atomicAdd(counter, (uint32_t)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (keep) keys[base + __popc(m & ((1u << lane) - 1u))] = key;
+  // eight loads in flight per thread before any of them is compacted
+  constexpr int B = 8;
+  for (uint32_t i0 = 0; i0 < total; i0 += blockDim.x * B) {
+    uint64_t kb[B];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      const uint32_t i = i0 + (uint32_t)b * blockDim.x + threadIdx.x;
+      kb[b] = i < total ? src[i] : kSentinelKey;
+    }
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      const bool keep = kb[b] != kSentinelKey;
+      const uint32_t m = __ballot_sync(0xffffffffu, keep);
+      uint32_t base = 0;
+      if (lane == 0 && m) base = atomicAdd(counter, (uint32_t)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (keep) keys[base + __popc(m & ((1u << lane) - 1u))] = kb[b];
+    }
   }
   __syncthreads();
   return *counter;
