@@ -345,6 +345,41 @@ def test_fp8_rescored_recall(cuda, oracle_mod, k):
     assert scan.device_status() == 0
 
 
+def test_fp8_extreme_query_scales(cuda, oracle_mod):
+    """Queries 2 x 10^5 times longer than the rows: the norm-digit factor
+    -2^(b-a) falls below e4m3's range and is dropped, the rows' norms then
+    weighing little against the dot. Each query is a scaled row, whose own
+    row must come first (the gap to any other row is 4 x 10^5 (1 - cos),
+    far above fp32's resolution at ||q||^2 = 4e10). Queries 10^4 times shorter:
+    the query scale is held at 2^(b - 8) and small codes lose precision; the
+    rescored distances stay exact. A zero query returns rows; an all-zero
+    table ties every row at ||q||^2 (lower slots first)."""
+    from fvgb300 import scan
+
+    torch = cuda
+    base = unit_mixture(20000, 96, 64, 0.4, 21)
+    table = scan.Fp8Table(torch.from_numpy(base).cuda())
+    src = np.random.default_rng(23).choice(20000, 32, replace=False)
+    big = (base[src] * np.float32(2e5)).astype(np.float32)
+    ids, dist = res_np(scan.fp8_search(table, torch.from_numpy(big).cuda(), 1, "l2"))
+    torch.cuda.synchronize()
+    assert np.array_equal(ids[:, 0], src.astype(np.uint32))
+    small = (unit_mixture(32, 96, 64, 0.4, 22) * np.float32(1e-4)).astype(np.float32)
+    small[0] = 0.0
+    ids, dist = res_np(scan.fp8_search(table, torch.from_numpy(small).cuda(), 10, "l2"))
+    torch.cuda.synchronize()
+    rec = check_rescored(oracle_mod, base, small, ids, dist, "l2", 10)
+    assert rec >= 0.9, rec
+    assert np.all(ids[0] != 0xFFFFFFFF)
+    zero = scan.Fp8Table(torch.zeros((300, 40), device="cuda"))
+    q = torch.from_numpy(np.full((2, 40), 0.5, np.float32)).cuda()
+    ids, dist = res_np(scan.fp8_search(zero, q, 5, "l2"))
+    torch.cuda.synchronize()
+    assert np.array_equal(ids, np.tile(np.arange(5, dtype=np.uint32), (2, 1)))
+    assert np.all(dist == np.float32(10.0))
+    assert scan.device_status() == 0
+
+
 @pytest.mark.parametrize("fp8", [False, True])
 def test_sampled_prepass_gives_the_unbounded_answer(cuda, oracle_mod, fp8):
     """k = 100 (a 400-entry shortlist, above the 64-entry range heap): the
