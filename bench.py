@@ -739,6 +739,8 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind, mode="pq"):
     sweep = {}
     head = None
     cstream = torch.cuda.Stream()
+    clocks = ClockSampler(local)  # sampled across the nprobe sweep (graph replays and recall checks)
+    clocks.start()
     for nprobe in [int(x) for x in a.nprobe.split(",")]:
         search(nprobe)
         torch.cuda.synchronize()
@@ -771,6 +773,7 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind, mode="pq"):
                          "graph_kernels": graph.kernels, "launches": launches}
         if head is None or nprobe == 32:
             head = nprobe
+    clk = clocks.stop()
     # per-kernel split of one (non-graph) call at the headline nprobe
     scan.profile_enable(True)
     for i in range(a.steps):
@@ -847,7 +850,7 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind, mode="pq"):
         cfg["m_pq"] = m_pq
     _line(a, world, h["qps"], UNIT, h["ms_per_batch"] * a.steps / 1e3,
           {"value": a.batch * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": a.batch * a.dim * 4 + words.nbytes,
-           "d2h_bytes_per_step": a.batch * a.k * 8}, h["launches"], roof, _kernels(prof), None, cpu,
+           "d2h_bytes_per_step": a.batch * a.k * 8}, h["launches"], roof, _kernels(prof), clk, cpu,
           "f32+u32" if rq else "f32+u8", cfg,
           recall_at_10=h["recall_at_10"], recall_sample=nsub, nprobe_sweep=sweep)
 
@@ -863,7 +866,7 @@ def run_serve(a, world, rank, local, dev, peaks, peak_kind):
     import numpy as np
     import torch
 
-    from fvgb300 import datasets
+    from fvgb300 import datasets, scan
     from fvgb300.index import BUILD_FP16, BUILD_IVF_SQ8, GpuVectorIndex, IndexConfig
     from fvgb300.serve import BatchKey, SearchBatcher
 
@@ -887,6 +890,9 @@ def run_serve(a, world, rank, local, dev, peaks, peak_kind):
         # warm-up: every launch class once
         wk = [BatchKey(e, k, p, 0) for e in ("fp16", "ivf_sq8") for k in (10, 100) for p in (16, 64)]
         b.replay(wk, qall[:len(wk)], np.zeros(len(wk), np.uint64))
+        clocks = ClockSampler(local)
+        clocks.start()
+        l0 = scan.launch_count()
         for rate, n in zip(rates, counts):
             eng = rng.integers(0, 2, n)
             ks = rng.choice([10, 100], n)
@@ -918,6 +924,8 @@ def run_serve(a, world, rank, local, dev, peaks, peak_kind):
                            "avg_batch": st["avg_batch_size"], "batches": st["total_batches"],
                            "max_inflight": st["max_inflight"], "failed": int((status != 0).sum()),
                            "recall_at_10": rec}
+        launches = scan.launch_count() - l0
+        clk = clocks.stop()
     top = sweep[rates[-1]]
     cfg = {"workload": "continuous batching: fp16 flat (1M x 768, IP) + IVF-SQ8 (nlist 4096) resident; requests "
                        "k in {10,100}, nprobe in {16,64}, filter in {none, 20%}; Poisson arrivals",
@@ -930,8 +938,8 @@ def run_serve(a, world, rank, local, dev, peaks, peak_kind):
     _line(a, world, top["sustained_qps"], UNIT, top["requests"] / max(top["sustained_qps"], 1e-9),
           {"value": top["sustained_qps"], "unit": UNIT, "h2d_bytes_per_step": per_req_in,
            "d2h_bytes_per_step": 8 * 55, "note": "the served path starts from host queries; value is end to end"},
-          None, None, None, None, None, "f16+u8", cfg, p50_ms=top["p50_ms"], p99_ms=top["p99_ms"],
-          serve_sweep=sweep)
+          launches, None, None, clk, None, "f16+u8", cfg, p50_ms=top["p50_ms"], p99_ms=top["p99_ms"],
+          serve_sweep=sweep, gpu_launches_note="kernels launched over the whole rate sweep (every rate's trace)")
 
 
 def main():
