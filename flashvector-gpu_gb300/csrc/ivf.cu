@@ -67,6 +67,11 @@ struct IvfArgs {
   uint32_t nq, top_k, nprobe, rerank_k, list_major;
   int metric;
   const uint32_t* mask;
+  // the mask in list order: bit i of this array = mask bit of vec_ids[i], for
+  // list positions i < list_n (null when there is no mask); one shared word
+  // per 32 postings replaces a dependent id + mask-word load per posting
+  const uint32_t* list_allow;
+  uint32_t list_n;
   const uint32_t* q_topk;         // per-query top_k / nprobe / rerank_k, or null (uniform)
   const uint32_t* q_nprobe;
   const uint32_t* q_rerank;
@@ -512,17 +517,24 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
         }
       };
       if (MODE != IVF_SQ8 && MW > 0) {
-        // R postings per thread per round: ids and code rows of all of them
-        // are loaded before any is scored. PIPE: the next round's loads are
-        // issued before this round is scored, and its mask / filter words
-        // after, so global-load latency overlaps the LUT arithmetic.
+        // R postings per thread per round: the ids of all of them, then their
+        // mask / filter words, then the code rows of the admitted ones only
+        // (a 10% mask leaves 9 of 10 rows unread), all before any is scored.
+        // PIPE: the next round's loads are issued before this round is
+        // scored, so global-load latency overlaps the LUT arithmetic.
         constexpr int MWW = MW > 0 ? MW : 1;
         constexpr uint32_t step = IVF_THREADS * R;
-        auto issue = [&](uint32_t b0, uint32_t (&v)[R], uint4 (&c)[R][MWW], float4 (&mt)[R]) {
+        auto issue = [&](uint32_t b0, uint32_t (&v)[R], uint4 (&c)[R][MWW], float4 (&mt)[R], bool (&o)[R]) {
+          // in: the posting exists and, where the list-order bits cover it,
+          // the mask admits it -- known from the bit word alone, so the code
+          // rows (list-major: addressed by position) load alongside the ids
+          bool bits[R], in[R];
 #pragma unroll
           for (int r = 0; r < R; ++r) {
             const uint32_t i = b0 + r * IVF_THREADS + tid;
-            v[r] = i < end ? __ldg(a.vec_ids + i) : 0xFFFFFFFFu;
+            bits[r] = a.list_allow != nullptr && i < a.list_n;
+            in[r] = i < end && (!bits[r] || ((__ldg(a.list_allow + (i >> 5)) >> (i & 31u)) & 1u));
+            v[r] = in[r] ? __ldg(a.vec_ids + i) : 0xFFFFFFFFu;
           }
 #pragma unroll
           for (int r = 0; r < R; ++r) {
@@ -530,29 +542,26 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
             const size_t row_i = a.list_major ? i : v[r];
             const uint4* row = reinterpret_cast<const uint4*>(a.codes + row_i * (16u * MW));
 #pragma unroll
-            for (int j = 0; j < MWW; ++j) c[r][j] = i < end ? __ldg(row + j) : make_uint4(0u, 0u, 0u, 0u);
+            for (int j = 0; j < MWW; ++j) c[r][j] = in[r] ? __ldg(row + j) : make_uint4(0u, 0u, 0u, 0u);
             if (MODE == IVF_RABITQ)
-              mt[r] = i < end ? __ldg(reinterpret_cast<const float4*>(a.rq_meta) + row_i) : make_float4(0.f, 0.f, 0.f, 0.f);
+              mt[r] = in[r] ? __ldg(reinterpret_cast<const float4*>(a.rq_meta) + row_i) : make_float4(0.f, 0.f, 0.f, 0.f);
           }
+          // scored: also the id-based mask (positions the bits do not cover)
+          // and the query's filter
+#pragma unroll
+          for (int r = 0; r < R; ++r)
+            o[r] = in[r] && (bits[r] || mask_allows(a.mask, v[r])) && filter_allows(qf, v[r]);
         };
         auto score = [&](const uint4 (&c)[MWW], const float4& mt) -> float {
           if (MODE == IVF_RABITQ)
             return rabitq_estimate(rabitq_sbu<MWW>(planes, c), mt, Pf, qmin, qdelta, sum_u, qc, qn, a.metric);
           return adc_words<MWW>(tab, c);
         };
-        auto admit = [&](const uint32_t (&v)[R], bool (&o)[R]) {
-#pragma unroll
-          for (int r = 0; r < R; ++r)
-            o[r] = v[r] != 0xFFFFFFFFu && mask_allows(a.mask, v[r]) && filter_allows(qf, v[r]);
-        };
         uint32_t vid[R];
         uint4 w[R][MWW];
         float4 mt[R];
         bool ok[R];
-        if (PIPE && beg < end) {
-          issue(beg, vid, w, mt);
-          admit(vid, ok);
-        }
+        if (PIPE && beg < end) issue(beg, vid, w, mt, ok);
         for (uint32_t base = beg; base < end; base += step) {
           if (PIPE) {
             uint32_t vn[R];
@@ -560,12 +569,11 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
             float4 mn[R];
             bool okn[R];
             const bool more = base + step < end;  // uniform over the block
-            if (more) issue(base + step, vn, wn, mn);
+            if (more) issue(base + step, vn, wn, mn, okn);
 #pragma unroll
             for (int r = 0; r < R; ++r)
               if (ok[r]) offer(score(w[r], mt[r]), vid[r]);
             if (more) {
-              admit(vn, okn);
 #pragma unroll
               for (int r = 0; r < R; ++r) {
                 vid[r] = vn[r];
@@ -576,8 +584,7 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
               }
             }
           } else {
-            issue(base, vid, w, mt);
-            admit(vid, ok);
+            issue(base, vid, w, mt, ok);
 #pragma unroll
             for (int r = 0; r < R; ++r)
               if (ok[r]) offer(score(w[r], mt[r]), vid[r]);
@@ -588,9 +595,10 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
       } else {
         for (uint32_t base = beg; base < end; base += IVF_THREADS) {
           const uint32_t i = base + tid;
-          if (i < end) {
+          const bool bits = a.list_allow != nullptr && i < a.list_n;
+          if (i < end && (!bits || ((__ldg(a.list_allow + (i >> 5)) >> (i & 31u)) & 1u))) {
             const uint32_t vid = __ldg(a.vec_ids + i);
-            if (mask_allows(a.mask, vid) && filter_allows(qf, vid)) {
+            if ((bits || mask_allows(a.mask, vid)) && filter_allows(qf, vid)) {
               const size_t row_i = a.list_major ? i : vid;
               const uint8_t* row = a.codes + row_i * a.code_bytes;
               if (MODE == IVF_RABITQ) {
@@ -646,6 +654,15 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_merge_kernel(IvfArgs a) {
   ivf_finish_query(a, keys, q, S, kq, do_rerank, a.queries + (size_t)q * a.dim);
 }
 
+// The mask in list order (one word per 32 list positions), for one call.
+__global__ void __launch_bounds__(256) ivf_list_mask_kernel(const uint32_t* __restrict__ vec_ids, uint32_t n,
+                                                            const uint32_t* __restrict__ mask, uint32_t* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool b = i < n && mask_allows(mask, __ldg(vec_ids + i));
+  const uint32_t w = __ballot_sync(0xffffffffu, b);
+  if ((threadIdx.x & 31u) == 0 && i < n) out[i >> 5] = w;
+}
+
 __global__ void relayout_codes_kernel(const uint8_t* __restrict__ by_id, const uint32_t* __restrict__ vec_ids,
                                       uint32_t n, uint32_t row_bytes, uint8_t* __restrict__ by_list) {
   const uint64_t total = (uint64_t)n * row_bytes;
@@ -691,8 +708,13 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   const size_t coarse_bytes = align256(cp.scratch_bytes);
   const size_t probe_bytes = align256((size_t)L.nq * nprobe * sizeof(GpuSearchResult));
   const size_t part_bytes = G > 1 ? align256((size_t)L.nq * G * shortlist * 8) : 0;
-  uint8_t* scratch = static_cast<uint8_t*>(scratch_get(stream, coarse_bytes + probe_bytes + part_bytes + 256));
+  const uint32_t list_n = L.mask ? L.num_vectors : 0u;
+  const size_t allow_bytes = align256(((size_t)list_n + 31) / 32 * 4);
+  uint8_t* scratch =
+      static_cast<uint8_t*>(scratch_get(stream, coarse_bytes + probe_bytes + part_bytes + 256 + allow_bytes));
   if (!scratch) return (int)cudaErrorMemoryAllocation;
+  uint32_t* list_allow =
+      list_n ? reinterpret_cast<uint32_t*>(scratch + coarse_bytes + probe_bytes + part_bytes + 256) : nullptr;
   GpuSearchResult* probes = reinterpret_cast<GpuSearchResult*>(scratch + coarse_bytes);
   uint64_t* partial = G > 1 ? reinterpret_cast<uint64_t*>(scratch + coarse_bytes + probe_bytes) : nullptr;
   uint32_t* work = reinterpret_cast<uint32_t*>(scratch + coarse_bytes + probe_bytes + part_bytes);
@@ -702,6 +724,11 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   if (rc != 0) return rc;
   cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t), stream);
   if (e != cudaSuccess) return (int)e;
+  if (list_n) {
+    ProfScope ps("ivf_list_mask", stream);
+    ivf_list_mask_kernel<<<(list_n + 255) / 256, 256, 0, stream>>>(L.vec_ids, list_n, L.mask, list_allow);
+    note_launch();
+  }
 
   IvfArgs a{};
   a.centroids = L.centroids;
@@ -735,6 +762,8 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   a.list_major = L.list_major ? 1u : 0u;
   a.metric = (int)L.metric;
   a.mask = L.mask;
+  a.list_allow = list_allow;
+  a.list_n = list_n;
   a.q_topk = L.q_topk;
   a.q_nprobe = L.q_nprobe;
   a.q_rerank = L.q_rerank;
