@@ -353,6 +353,9 @@ __device__ __forceinline__ float sq8_row(const float* __restrict__ qres, const f
 // thread per round, software-pipelined across rounds (PIPE).
 template <int MODE, int MW, int R = 4, bool PIPE = false>
 __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
+  // a round offers at most IVF_THREADS * R candidates, appended after the
+  // shortlist; the buffer is flushed between rounds, so one round must fit
+  static_assert((uint32_t)IVF_THREADS * R <= IVF_BUF, "a round of postings must fit the candidate buffer");
   extern __shared__ __align__(16) uint8_t smem[];
   uint64_t* keys = reinterpret_cast<uint64_t*>(smem);
   float* tab = reinterpret_cast<float*>(smem + (size_t)a.keys_pow2 * 8);
