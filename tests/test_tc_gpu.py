@@ -1,6 +1,6 @@
 """Tensor-core flat scans (fp16 / fp8) through the C ABI.
 
-Reduced-precision forms are judged the way the scan path's contract states
+Reduced-precision forms are assessed the way the scan path's contract states
 them: the candidate ranking must agree with an fp64 evaluation of the same
 quantised products, the fp32-rescored results must reach recall@k >= 0.99
 against the fp64 oracle, and every reported distance must be the fp32
