@@ -600,6 +600,27 @@ def run_workload(a, world, rank, local):
             hout.copy_(out, non_blocking=True)
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
+        # the same workload over the per-vector-scale layout (scales max|x| / 448,
+        # each row's scale and norm applied per value in the epilogue)
+        pv_table = scan.Fp8Table(base, per_vector=True)
+        pv_step = lambda i: scan.fp8_search(pv_table, qb[i % 2], a.k, "l2", opts=opts, out=out)  # noqa: E731
+        for i in range(max(3, a.warmup)):
+            pv_step(i)
+        torch.cuda.synchronize()
+        scan.profile_summary()
+        scan.profile_enable(True)
+        pv_s = _dev_time(pv_step, a.steps, stream)
+        scan.profile_enable(False)
+        pv_prof = scan.profile_summary()
+        pv_step(0)
+        torch.cuda.synchronize()
+        pres = out.cpu().numpy()
+        pids = pres[..., 0].view(np.uint32)
+        per_vector = {"value": a.batch * a.steps / pv_s, "unit": UNIT,
+                      "scan_ms": pv_prof["tc_scan_fp8"]["ms"] / pv_prof["tc_scan_fp8"]["launches"],
+                      "recall_at_10": _recall(pids[:nsub, :10], truth[:, :10]), "recall_at_k": _recall(pids[:nsub], truth),
+                      "layout": "per-vector scales max|x|/448, padded_dim " + str(pv_table.pd)}
+        del pv_table
         kname = "tc_scan_fp8"
         kms = prof[kname]["ms"] / prof[kname]["launches"]
         flops = 2.0 * a.n * a.dim * a.batch
@@ -631,7 +652,8 @@ def run_workload(a, world, rank, local):
               {"value": a.batch * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": a.batch * a.dim * 4,
                "d2h_bytes_per_step": a.batch * a.k * 8}, launches, roof, _kernels(prof), clk, cpu, "e4m3", cfg,
               recall_at_10=rec10, recall_at_k=rec_k, recall_sample=nsub,
-              fp32_exact_scan={"value": f32_qps, "unit": UNIT, "steps": f32_steps, "speedup_fp8_over_fp32": qps / f32_qps})
+              fp32_exact_scan={"value": f32_qps, "unit": UNIT, "steps": f32_steps, "speedup_fp8_over_fp32": qps / f32_qps},
+              per_vector_scales=per_vector)
         return
 
     if a.workload in ("ivf_pq", "ivf_rabitq"):

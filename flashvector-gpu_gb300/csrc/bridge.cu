@@ -267,7 +267,8 @@ int tc_common(const fv::TcTables& t, const float* q, uint32_t nq, uint32_t top_k
   if ((uintptr_t)t.base % 16 != 0) return FV_ERR_ARG;
   if (metric != METRIC_INNER_PRODUCT && !t.norms) return FV_ERR_NULL;
   if (t.fp8 && !t.scales) return FV_ERR_NULL;
-  if (t.fp8 && t.padded_dim < t.dim + 3) return FV_ERR_ARG;  // room for the three norm digits
+  if (t.fp8 && t.fp8_table_scale && t.padded_dim < t.dim + 3) return FV_ERR_ARG;  // room for the norm digits
+  if (t.fp8 && !t.fp8_table_scale && metric != METRIC_INNER_PRODUCT && !t.norms) return FV_ERR_NULL;
   FvScanOptions o{};
   if (opt) o = *opt;
   else o.boundary_fp64 = 1;
@@ -297,8 +298,9 @@ int fv_fp8_search_batch(const FvFp8GpuTables* tables, const float* d_queries, ui
                         MetricType metric, const uint32_t* d_valid_mask, const FvScanOptions* options,
                         GpuSearchResult* d_out_results, void* stream) {
   if (!tables || !d_queries || !d_out_results) return FV_ERR_NULL;
+  if (tables->scale_mode > 1u) return FV_ERR_ARG;
   fv::TcTables t{true, tables->d_vectors_fp8, tables->d_vec_norms_sq, tables->d_scales, tables->d_vectors,
-                 tables->num_vectors, tables->dim, tables->padded_dim};
+                 tables->num_vectors, tables->dim, tables->padded_dim, tables->scale_mode == 0u};
   return tc_common(t, d_queries, num_queries, top_k, metric, d_valid_mask, options, d_out_results, stream);
 }
 
@@ -316,6 +318,14 @@ int fv_encode_fp8(const float* d_vectors, uint32_t num_vectors, uint32_t dim, ui
   if (padded_dim < dim + 3 || padded_dim % 16) return FV_ERR_ARG;
   return fv::launch_encode_fp8(d_vectors, num_vectors, dim, padded_dim, d_out_fp8, d_out_scales, d_out_norms_sq,
                                (cudaStream_t)stream);
+}
+
+int fv_encode_fp8_per_vector(const float* d_vectors, uint32_t num_vectors, uint32_t dim, uint32_t padded_dim,
+                             uint8_t* d_out_fp8, float* d_out_scales, float* d_out_norms_sq, void* stream) {
+  if (num_vectors && (!d_vectors || !d_out_fp8 || !d_out_scales || !d_out_norms_sq)) return FV_ERR_NULL;
+  if (padded_dim < dim || padded_dim % 16) return FV_ERR_ARG;
+  return fv::launch_encode_fp8_per_vector(d_vectors, num_vectors, dim, padded_dim, d_out_fp8, d_out_scales,
+                                          d_out_norms_sq, (cudaStream_t)stream);
 }
 
 // ------------------------------------------------------------------ IVF

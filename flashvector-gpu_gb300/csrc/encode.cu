@@ -19,6 +19,8 @@
 //    the per-query factor -2 s s_q and the query's norm; remaining columns
 //    zero; ||x||^2 by compensated (Neumaier) fp32 summation; every entry of
 //    the scale array holds s.
+//  * fp8, per-row scales (the other layout, selected by the table's
+//    scale_mode): s_v = max|x_v| / 448, codes e4m3(x / s_v), no digits.
 #include <cuda_fp8.h>
 
 #include "common.cuh"
@@ -152,6 +154,40 @@ __global__ void __launch_bounds__(256) encode_fp8_kernel(const float* __restrict
   if (lane == 0) scales[row] = s;
 }
 
+// Per-row-scale table (the other fp8 layout): s_v = max|x_v| / 448 (1 for a
+// zero row), codes e4m3(x / s_v) round-to-nearest-even with saturation, zero
+// padding, ||x||^2 by compensated fp32 summation.
+__global__ void __launch_bounds__(256) encode_fp8_per_vector_kernel(const float* __restrict__ x, uint32_t n,
+                                                                    uint32_t dim, uint32_t pd, uint8_t* __restrict__ out,
+                                                                    float* __restrict__ scales,
+                                                                    float* __restrict__ norms) {
+  const uint64_t row = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const float* src = x + row * dim;
+  float amax = 0.f, sum = 0.f, comp = 0.f;
+  for (uint32_t d = lane; d < dim; d += 32) {
+    const float v = __ldg(src + d);
+    amax = fmaxf(amax, fabsf(v));
+    neumaier_add(sum, comp, __fmul_rn(v, v));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    const float os = __shfl_xor_sync(0xffffffffu, sum, o);
+    const float oc = __shfl_xor_sync(0xffffffffu, comp, o);
+    neumaier_add(sum, comp, os);
+    comp += oc;
+  }
+  const float scale = amax > 0.f ? amax / 448.0f : 1.0f;
+  uint8_t* dst = out + row * pd;
+  for (uint32_t d = lane; d < pd; d += 32) dst[d] = d < dim ? e4m3_code(__ldg(src + d) / scale) : (uint8_t)0;
+  if (lane == 0) {
+    scales[row] = scale;
+    norms[row] = sum + comp;
+  }
+}
+
 }  // namespace
 
 int launch_encode_fp16(const float* x, uint32_t n, uint32_t dim, uint32_t pd, uint16_t* out, float* norms,
@@ -174,6 +210,19 @@ int launch_encode_fp8(const float* x, uint32_t n, uint32_t dim, uint32_t pd, uin
   fp8_table_scale_kernel<<<1, 1, 0, stream>>>(word);
   encode_fp8_kernel<<<(unsigned)blocks, 256, 0, stream>>>(x, n, dim, pd, out, scales, norms);
   note_launch(3);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace fv
+
+namespace fv {
+
+int launch_encode_fp8_per_vector(const float* x, uint32_t n, uint32_t dim, uint32_t pd, uint8_t* out, float* scales,
+                                 float* norms, cudaStream_t stream) {
+  if (n == 0) return 0;
+  const uint64_t blocks = ((uint64_t)n * 32 + 255) / 256;
+  encode_fp8_per_vector_kernel<<<(unsigned)blocks, 256, 0, stream>>>(x, n, dim, pd, out, scales, norms);
+  note_launch();
   return (int)cudaGetLastError();
 }
 

@@ -68,8 +68,9 @@ struct IvfArgs {
   int metric;
   const uint32_t* mask;
   // the mask in list order: bit i of this array = mask bit of vec_ids[i], for
-  // list positions i < list_n (null when there is no mask); one shared word
-  // per 32 postings replaces a dependent id + mask-word load per posting
+  // list positions i < list_n (null when there is no mask; positions past the
+  // lists hold 0); one shared word per 32 postings replaces a dependent id +
+  // mask-word load per posting
   const uint32_t* list_allow;
   uint32_t list_n;
   const uint32_t* q_topk;         // per-query top_k / nprobe / rerank_k, or null (uniform)
@@ -658,10 +659,15 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_merge_kernel(IvfArgs a) {
 }
 
 // The mask in list order (one word per 32 list positions), for one call.
-__global__ void __launch_bounds__(256) ivf_list_mask_kernel(const uint32_t* __restrict__ vec_ids, uint32_t n,
-                                                            const uint32_t* __restrict__ mask, uint32_t* __restrict__ out) {
+// Only positions inside the lists (< offsets[nlist]) read an id: vec_ids may
+// be shorter than the id space n (an engine whose slots carry remapped ids).
+__global__ void __launch_bounds__(256) ivf_list_mask_kernel(const uint32_t* __restrict__ vec_ids,
+                                                            const uint32_t* __restrict__ offsets, uint32_t nlist,
+                                                            uint32_t n, const uint32_t* __restrict__ mask,
+                                                            uint32_t* __restrict__ out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool b = i < n && mask_allows(mask, __ldg(vec_ids + i));
+  const uint32_t postings = min(n, __ldg(offsets + nlist));
+  const bool b = i < postings && mask_allows(mask, __ldg(vec_ids + i));
   const uint32_t w = __ballot_sync(0xffffffffu, b);
   if ((threadIdx.x & 31u) == 0 && i < n) out[i >> 5] = w;
 }
@@ -729,7 +735,8 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   if (e != cudaSuccess) return (int)e;
   if (list_n) {
     ProfScope ps("ivf_list_mask", stream);
-    ivf_list_mask_kernel<<<(list_n + 255) / 256, 256, 0, stream>>>(L.vec_ids, list_n, L.mask, list_allow);
+    ivf_list_mask_kernel<<<(list_n + 255) / 256, 256, 0, stream>>>(L.vec_ids, L.offsets, L.nlist, list_n, L.mask,
+                                                                     list_allow);
     note_launch();
   }
 

@@ -101,18 +101,19 @@ int launch_flat_f32(const float* vectors, const uint32_t* vec_ids, uint32_t n, u
 
 // tensor-core flat scans (tc_scan.cu)
 struct TcTables {
-  bool fp8;              // false: fp16 rows, true: e4m3 rows with per-row scales
+  bool fp8;              // false: fp16 rows, true: e4m3 rows
   const void* base;      // [n][padded_dim] fp16 or e4m3
   const float* norms;    // [n] ||x||^2 (may be null for inner product)
   const float* scales;   // [n] per-row dequantisation scale (fp8 only)
   const float* vectors;  // [n][dim] fp32 rows for the rescore (optional)
   uint32_t n, dim, padded_dim;
+  bool fp8_table_scale = true;  // fp8: one power-of-two table scale + norm digits; false: per-row scales
 };
 struct TcScanArgs;
-cudaError_t dispatch_tc_scan_fp16(int kl, int groups, int metric, const CUtensorMap& ta, const CUtensorMap& tb,
-                                  const TcScanArgs& a, uint32_t grid, cudaStream_t stream);
-cudaError_t dispatch_tc_scan_fp8(int kl, int groups, int metric, const CUtensorMap& ta, const CUtensorMap& tb,
-                                 const TcScanArgs& a, uint32_t grid, cudaStream_t stream);
+cudaError_t dispatch_tc_scan_fp16(int kl, int groups, int metric, bool table_scale, const CUtensorMap& ta,
+                                  const CUtensorMap& tb, const TcScanArgs& a, uint32_t grid, cudaStream_t stream);
+cudaError_t dispatch_tc_scan_fp8(int kl, int groups, int metric, bool table_scale, const CUtensorMap& ta,
+                                 const CUtensorMap& tb, const TcScanArgs& a, uint32_t grid, cudaStream_t stream);
 int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
                    const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream,
                    const QueryFilter* filters = nullptr);
@@ -196,6 +197,8 @@ int launch_encode_fp16(const float* x, uint32_t n, uint32_t dim, uint32_t pd, ui
                        cudaStream_t stream);
 int launch_encode_fp8(const float* x, uint32_t n, uint32_t dim, uint32_t pd, uint8_t* out, float* scales,
                       float* norms, cudaStream_t stream);
+int launch_encode_fp8_per_vector(const float* x, uint32_t n, uint32_t dim, uint32_t pd, uint8_t* out, float* scales,
+                                 float* norms, cudaStream_t stream);
 
 // test fixtures (fixtures.cu)
 int launch_distance_matrix(const float* queries, const float* base, uint32_t nq, uint32_t n, uint32_t dim,

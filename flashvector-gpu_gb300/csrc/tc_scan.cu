@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(256) tc_prep_queries_kernel(const float* __res
                                                               float* __restrict__ qnorm, float* __restrict__ qscale,
                                                               uint32_t* __restrict__ tslot, uint32_t kl,
                                                               uint32_t stride, const float* __restrict__ xscale,
-                                                              int metric, uint32_t nq_rows) {
+                                                              int metric, uint32_t nq_rows, bool table_scale) {
   const uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (qi >= nq_rows) return;
@@ -82,6 +82,15 @@ __global__ void __launch_bounds__(256) tc_prep_queries_kernel(const float* __res
     for (uint32_t d = lane; d < dim; d += 32) amax = fmaxf(amax, fabsf(src[d]));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    if (!table_scale) {
+      // per-row-scale table: the query's scale amax / 448, no norm digits
+      const float scale = amax > 0.f ? amax / 448.0f : 1.0f;
+      if (lane == 0) qscale[qi] = scale;
+      uint8_t* o8 = static_cast<uint8_t*>(out) + (size_t)qi * pd;
+      for (uint32_t d = lane; d < pd; d += 32)
+        o8[d] = d < dim ? (uint8_t)__nv_cvt_float_to_fp8(src[d] / scale, __NV_SATFINITE, __NV_E4M3) : (uint8_t)0;
+      return;
+    }
     const int b = ilogbf(__ldg(xscale));
     int a = b - 8;
     if (amax > 0.f) {
@@ -493,11 +502,11 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
     if (fp8)
       tc_prep_queries_kernel<true><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm, qscale,
                                                                tslot, slot_kl, slot_stride, t.scales, (int)metric,
-                                                               nq_rows);
+                                                               nq_rows, t.fp8_table_scale);
     else
       tc_prep_queries_kernel<false><<<blocks, 256, 0, stream>>>(queries, nq, t.dim, t.padded_dim, qprep, qnorm,
                                                                 qscale, tslot, slot_kl, slot_stride, nullptr,
-                                                                (int)metric, nq_rows);
+                                                                (int)metric, nq_rows, false);
     note_launch();
   }
 
@@ -529,8 +538,8 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
     const int g = use_pair ? -1 : groups;
     const uint32_t grid = (use_pair ? nqb_grid : nqb) * splits_n;
     const CUtensorMap& b = use_pair ? tb_half : tb;
-    return fp8 ? dispatch_tc_scan_fp8(kl_t, g, (int)metric, ta, b, args, grid, stream)
-               : dispatch_tc_scan_fp16(kl_t, g, (int)metric, ta, b, args, grid, stream);
+    return fp8 ? dispatch_tc_scan_fp8(kl_t, g, (int)metric, t.fp8_table_scale, ta, b, args, grid, stream)
+               : dispatch_tc_scan_fp16(kl_t, g, (int)metric, true, ta, b, args, grid, stream);
   };
   cudaError_t e;
   if (prepass) {

@@ -5,9 +5,9 @@
 
 namespace fv {
 
-cudaError_t dispatch_tc_scan_fp16(int kl, int groups, int metric, const CUtensorMap& ta, const CUtensorMap& tb,
-                                     const TcScanArgs& a, uint32_t grid, cudaStream_t stream) {
-  return dispatch_scan<false>(kl, groups, metric, ta, tb, a, grid, stream);
+cudaError_t dispatch_tc_scan_fp16(int kl, int groups, int metric, bool table_scale, const CUtensorMap& ta,
+                                  const CUtensorMap& tb, const TcScanArgs& a, uint32_t grid, cudaStream_t stream) {
+  return dispatch_scan<false>(kl, groups, metric, table_scale, ta, tb, a, grid, stream);
 }
 
 }  // namespace fv

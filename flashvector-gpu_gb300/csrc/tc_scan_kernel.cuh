@@ -25,6 +25,8 @@
 #include <cuda_fp16.h>
 #include <cuda_fp8.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "tc_ptx.cuh"
@@ -148,7 +150,7 @@ static __device__ __forceinline__ float select32(const float* v, int j) {
 // TMA loads count on the even CTA's full barriers; the even CTA's commits
 // are multicast to both CTAs' barriers; the odd CTA's epilogue arrives on
 // the even CTA's accumulator barriers.
-template <bool FP8, int KL, int STAGES, int METRIC, int G, bool PAIR>
+template <bool FP8, int KL, int STAGES, int METRIC, int G, bool PAIR, bool TS>
 __global__ void __launch_bounds__(scan_threads(G), 1)
     tc_scan_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcScanArgs a) {
   using L = ScanSmem<KL, STAGES, G, PAIR>;
@@ -341,13 +343,15 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
     const float qn = qvalid ? __ldg(a.qnorm + q) : 0.f;
     const QueryFilter qf = (a.filters && qvalid) ? load_filter(a.filters, q) : QueryFilter{nullptr, 0u, 0u};
     const float qs = (FP8 && qvalid) ? __ldg(a.qscale + q) : 1.f;
-    // fp8 L2 and inner product: the accumulator is the ranking value in the
-    // table's units (L2: the norm digits fold -||x||^2 / (2 s s_q) into the
-    // dot product), v = sc * acc with sc = -2 s s_q (L2) or -s s_q (IP), a
-    // power of two, so the scaling is exact and no per-row data is read
-    constexpr bool FUSED = FP8 && METRIC != METRIC_COSINE;
-    const float sc = FUSED ? (METRIC == METRIC_L2 ? -2.0f : -1.0f) * qs * __ldg(a.xscale) : 1.f;
-    const float inv_sc = FUSED ? __fdiv_rn(1.0f, sc) : 1.f;
+    // fp8 L2 and inner product over a table-scale table: the accumulator is
+    // the ranking value in the table's units (L2: the norm digits fold
+    // -||x||^2 / (2 s s_q) into the dot product), v = sc * acc with
+    // sc = -2 s s_q (L2) or -s s_q (IP), a power of two, so the scaling is
+    // exact and no per-row data is read. A per-row-scale table reads each
+    // row's scale (and norm) per value instead.
+    constexpr bool fused = FP8 && METRIC != METRIC_COSINE && TS;
+    const float sc = fused ? (METRIC == METRIC_L2 ? -2.0f : -1.0f) * qs * __ldg(a.xscale) : 1.f;
+    const float inv_sc = fused ? __fdiv_rn(1.0f, sc) : 1.f;
     float worst = kSentinelDist;  // this CTA's kl-th best distance (1e30 until the heap is full)
     // admission bound: the query's pre-pass bound, lowered by the shared slots
     float bound = (a.qbound && qvalid) ? __ldg(a.qbound + q) : kSentinelDist;
@@ -381,7 +385,7 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
     auto refresh = [&]() {
       const float w = fminf(worst, bound);
       thr = METRIC == METRIC_L2 ? (w - qn) + 1e-6f * (fabsf(w) + fabsf(qn)) + 1e-30f : w;
-      if (FUSED) {
+      if (fused) {
         thr *= inv_sc;
         thr -= 1e-6f * fabsf(thr) + 1e-37f;
       }
@@ -393,6 +397,10 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
     // registers while tile i is processed (lane l holds columns l + 32 r).
     float* cb = colbuf + (warp - 2) * 2 * TC_N;
     uint32_t* cm = colmask + (warp - 2) * 8;
+    // this group's tiles (first, step) and columns [c_lo, c_hi) of each;
+    // only its own columns' data is staged
+    const uint32_t t_first = col_split ? 0u : (uint32_t)grp, t_step = col_split ? 1u : (uint32_t)G;
+    const int c_lo = col_split ? grp * (TC_N / G) : 0, c_hi = col_split ? c_lo + TC_N / G : TC_N;
     float pre_n[TC_N / 32], pre_s[TC_N / 32];
     uint32_t pre_m = 0;
     auto prefetch = [&](uint32_t tile) {
@@ -400,10 +408,11 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
 #pragma unroll
       for (int r = 0; r < TC_N / 32; ++r) {
         const uint32_t slot = v0n + lane + 32 * r;
-        const bool in = slot < a.n;
-        pre_n[r] = (METRIC != METRIC_INNER_PRODUCT && !FUSED && in) ? __ldg(a.xnorm + slot) : 0.f;
-        // per-column factor of the scaled dot: xs (cosine; fp8 L2 and IP need none)
-        const float xs = (FP8 && !FUSED && in) ? __ldg(a.xscale + slot) : 0.f;
+        const bool in = slot < a.n && 32 * r >= c_lo && 32 * r < c_hi;
+        pre_n[r] = (METRIC != METRIC_INNER_PRODUCT && !fused && in) ? __ldg(a.xnorm + slot) : 0.f;
+        // per-column factor of the scaled dot: -2 xs (L2), -xs (IP), xs
+        // (cosine) for per-row scales; a table-scale table needs none
+        const float xs = (FP8 && !fused && in) ? __ldg(a.xscale + slot) : 0.f;
         pre_s[r] = METRIC == METRIC_L2 ? -2.0f * xs : (METRIC == METRIC_INNER_PRODUCT ? -xs : xs);
       }
       pre_m = 0;
@@ -416,9 +425,6 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
         }
       }
     };
-    // this group's tiles (first, step) and columns [c_lo, c_hi) of each
-    const uint32_t t_first = col_split ? 0u : (uint32_t)grp, t_step = col_split ? 1u : (uint32_t)G;
-    const int c_lo = col_split ? grp * (TC_N / G) : 0, c_hi = col_split ? c_lo + TC_N / G : TC_N;
     if (t_first < my_tiles) prefetch(t_first);
     for (uint32_t i = t_first; i < my_tiles; i += t_step) {
       const uint32_t buf = i & 1, use = i >> 1;
@@ -426,8 +432,9 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
       __syncwarp();
 #pragma unroll
       for (int r = 0; r < TC_N / 32; ++r) {
-        if (METRIC != METRIC_INNER_PRODUCT && !FUSED) cb[lane + 32 * r] = pre_n[r];
-        if (FP8 && !FUSED) cb[TC_N + lane + 32 * r] = pre_s[r];
+        if (32 * r < c_lo || 32 * r >= c_hi) continue;
+        if (METRIC != METRIC_INNER_PRODUCT && !fused) cb[lane + 32 * r] = pre_n[r];
+        if (FP8 && !fused) cb[TC_N + lane + 32 * r] = pre_s[r];
       }
       if (lane < 8) cm[lane] = pre_m;
       __syncwarp();
@@ -459,87 +466,99 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
         tc::tmem_wait_ld(ra);
         tc::reg_fence(rb);
         if (mw == 0ull) continue;
-        // per-column values v, v[0..32) columns c0.., v[32..64) columns
-        // c0+32..; the distance is D(v): L2  D(v) = max(0, ||q||^2 + v) with
-        // v = ||x||^2 - 2 <q, x> (the query's norm is added after the
-        // minimum, D being monotone), IP  D(v) = v = -<q, x>, cosine the
-        // full expression. FP8 cosine dots carry the query and table scales.
-        float v[64];
-        if constexpr (FUSED) {
+        // the chunk's admission test and insertions; FU: the accumulator is
+        // the ranking value (fp8 table-scale tables)
+        auto chunk = [&](auto fu_tag) {
+          constexpr bool FU = decltype(fu_tag)::value;
+          // per-column values v, v[0..32) columns c0.., v[32..64) columns
+          // c0+32..; the distance is D(v): L2  D(v) = max(0, ||q||^2 + v) with
+          // v = ||x||^2 - 2 <q, x> (the query's norm is added after the
+          // minimum, D being monotone), IP  D(v) = v = -<q, x>, cosine the
+          // full expression. FP8 cosine dots carry the query and table scales.
+          float v[64];
+          if constexpr (FU) {
 #pragma unroll
-          for (int j = 0; j < 64; ++j) v[j] = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
-        } else if (METRIC == METRIC_COSINE) {
+            for (int j = 0; j < 64; ++j) v[j] = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
+          } else if (METRIC == METRIC_COSINE) {
 #pragma unroll
-          for (int j = 0; j < 64; ++j) {
-            float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
-            if (FP8) dot = dot * (qs * cb[TC_N + c0 + j]);
-            v[j] = 1.0f - dot / (sqrtf(qn * cb[c0 + j]) + 1e-8f);
-          }
-        } else {
-          const float4* nb = reinterpret_cast<const float4*>(cb + c0);
+            for (int j = 0; j < 64; ++j) {
+              float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
+              if (FP8) dot = dot * (qs * cb[TC_N + c0 + j]);
+              v[j] = 1.0f - dot / (sqrtf(qn * cb[c0 + j]) + 1e-8f);
+            }
+          } else {
+            const float4* nb = reinterpret_cast<const float4*>(cb + c0);
+            const float4* sb = reinterpret_cast<const float4*>(cb + TC_N + c0);
 #pragma unroll
-          for (int j4 = 0; j4 < 16; ++j4) {
-            const float4 n4 = METRIC == METRIC_L2 ? nb[j4] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float nv[4] = {n4.x, n4.y, n4.z, n4.w};
+            for (int j4 = 0; j4 < 16; ++j4) {
+              const float4 n4 = METRIC == METRIC_L2 ? nb[j4] : make_float4(0.f, 0.f, 0.f, 0.f);
+              const float4 s4 = FP8 ? sb[j4] : make_float4(0.f, 0.f, 0.f, 0.f);
+              const float nv[4] = {n4.x, n4.y, n4.z, n4.w};
+              const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              const int j = 4 * j4 + e;
-              const float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
-              v[j] = METRIC == METRIC_L2 ? fmaf(-2.0f, dot, nv[e]) : -dot;
+              for (int e = 0; e < 4; ++e) {
+                const int j = 4 * j4 + e;
+                const float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
+                if (FP8)  // per-row scales: -2 xs (L2) or -xs (IP) in sv
+                  v[j] = METRIC == METRIC_L2 ? fmaf(dot * qs, sv[e], nv[e]) : (dot * qs) * sv[e];
+                else
+                  v[j] = METRIC == METRIC_L2 ? fmaf(-2.0f, dot, nv[e]) : -dot;
+              }
             }
           }
-        }
-        // D: distance from v (fused fp8: from the accumulator, v = sc * acc)
-        auto D = [&](float x) {
-          if (FUSED) x *= sc;
-          return METRIC == METRIC_L2 ? fmaxf(0.f, qn + x) : x;
-        };
-        // better(x, y): the smaller v, i.e. the larger accumulator when fused
-        auto better = [](float x, float y) { return FUSED ? fmaxf(x, y) : fminf(x, y); };
-        auto may = [&](float x) { return FUSED ? x >= thr : x <= thr; };
-        // a tree of three-input bests: a 64-column batch whose best cannot
-        // enter is skipped whole (the common case once warm); the pairwise
-        // bests (j, j + 32) are formed only for a batch that passes
-        // best of three in one instruction (three-input min / max)
-        auto best3 = [](float x, float y, float z) {
-          float d;
-          if (FUSED)
-            asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(x), "f"(y), "f"(z));
-          else
-            asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(x), "f"(y), "f"(z));
-          return d;
-        };
-        float r[22], s8[8];
+          // D: distance from v (fused fp8: from the accumulator, v = sc * acc)
+          auto D = [&](float x) {
+            if (FU) x *= sc;
+            return METRIC == METRIC_L2 ? fmaxf(0.f, qn + x) : x;
+          };
+          // better(x, y): the smaller v, i.e. the larger accumulator when fused
+          auto better = [](float x, float y) { return FU ? fmaxf(x, y) : fminf(x, y); };
+          auto may = [&](float x) { return FU ? x >= thr : x <= thr; };
+          // a tree of three-input bests: a 64-column batch whose best cannot
+          // enter is skipped whole (the common case once warm); the pairwise
+          // bests (j, j + 32) are formed only for a batch that passes
+          // best of three in one instruction (three-input min / max)
+          auto best3 = [](float x, float y, float z) {
+            float d;
+            if (FU)
+              asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(x), "f"(y), "f"(z));
+            else
+              asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(x), "f"(y), "f"(z));
+            return d;
+          };
+          float r[22], s8[8];
 #pragma unroll
-        for (int i = 0; i < 21; ++i) r[i] = best3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
-        r[21] = v[63];
+          for (int i = 0; i < 21; ++i) r[i] = best3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+          r[21] = v[63];
 #pragma unroll
-        for (int i = 0; i < 7; ++i) s8[i] = best3(r[3 * i], r[3 * i + 1], r[3 * i + 2]);
-        s8[7] = r[21];
-        const float top = best3(best3(s8[0], s8[1], s8[2]), best3(s8[3], s8[4], s8[5]), better(s8[6], s8[7]));
-        if (!(mw != 0ull && may(top))) continue;
-        float m1[32];
+          for (int i = 0; i < 7; ++i) s8[i] = best3(r[3 * i], r[3 * i + 1], r[3 * i + 2]);
+          s8[7] = r[21];
+          const float top = best3(best3(s8[0], s8[1], s8[2]), best3(s8[3], s8[4], s8[5]), better(s8[6], s8[7]));
+          if (!(mw != 0ull && may(top))) return;
+          float m1[32];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) m1[j] = better(v[j], v[j + 32]);
-        // pairs (j, j+32) that may hold a candidate, walked lane-parallel
-        uint32_t pass = 0;
+          for (int j = 0; j < 32; ++j) m1[j] = better(v[j], v[j + 32]);
+          // pairs (j, j+32) that may hold a candidate, walked lane-parallel
+          uint32_t pass = 0;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) pass |= (uint32_t)may(m1[j]) << j;
-        pass &= (uint32_t)mw | (uint32_t)(mw >> 32);
-        while (pass) {
-          const int j = __ffs(pass) - 1;
-          pass &= pass - 1;
-          const float dlo = D(select32(v, j));
-          const float dhi = D(select32(v + 32, j));
-          if (((mw >> j) & 1ull) && dlo < worst && dlo <= bound) {
-            keep(dlo, v0 + c0 + j);
-            refresh();
+          for (int j = 0; j < 32; ++j) pass |= (uint32_t)may(m1[j]) << j;
+          pass &= (uint32_t)mw | (uint32_t)(mw >> 32);
+          while (pass) {
+            const int j = __ffs(pass) - 1;
+            pass &= pass - 1;
+            const float dlo = D(select32(v, j));
+            const float dhi = D(select32(v + 32, j));
+            if (((mw >> j) & 1ull) && dlo < worst && dlo <= bound) {
+              keep(dlo, v0 + c0 + j);
+              refresh();
+            }
+            if (((mw >> (j + 32)) & 1ull) && dhi < worst && dhi <= bound) {
+              keep(dhi, v0 + c0 + j + 32);
+              refresh();
+            }
           }
-          if (((mw >> (j + 32)) & 1ull) && dhi < worst && dhi <= bound) {
-            keep(dhi, v0 + c0 + j + 32);
-            refresh();
-          }
-        }
+        };
+        chunk(std::integral_constant<bool, fused>{});
       }
       tc::tc_fence_before();
       __syncwarp();
@@ -584,12 +603,12 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
 }
 
 
-template <bool FP8, int KL, int STAGES, int METRIC, int G, bool PAIR = false>
+template <bool FP8, int KL, int STAGES, int METRIC, int G, bool PAIR = false, bool TS = true>
 cudaError_t launch_scan_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a, uint32_t grid,
                                cudaStream_t stream) {
   using L = ScanSmem<KL, STAGES, G, PAIR>;
   static_assert(L::bytes <= 227 * 1024, "scan shared memory above the 227 KB per-CTA limit");
-  auto kern = tc_scan_kernel<FP8, KL, STAGES, METRIC, G, PAIR>;
+  auto kern = tc_scan_kernel<FP8, KL, STAGES, METRIC, G, PAIR, TS>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes);
   if (e != cudaSuccess) return e;
   if constexpr (PAIR) {
@@ -619,42 +638,50 @@ cudaError_t launch_scan_kernel(const CUtensorMap& ta, const CUtensorMap& tb, con
 // rather than the MMA bounds a tile) halves the stage ring and caps the heap
 // at 48 entries so that two groups' heaps fit next to it. groups == -1
 // selects the CTA-pair variant (grid = 2 CTAs per cluster).
-template <bool FP8, int METRIC>
+template <bool FP8, int METRIC, bool TS>
 cudaError_t dispatch_scan_kl(int kl, int groups, const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a,
                              uint32_t grid, cudaStream_t stream) {
   if (groups == -1) {
     // cta_group::2 pairs (one epilogue group): 16 KB of base per stage frees
     // room for 4-6 stages
     switch (kl) {
-      case 16: return launch_scan_kernel<FP8, 16, 6, METRIC, 1, true>(ta, tb, a, grid, stream);
-      case 32: return launch_scan_kernel<FP8, 32, 5, METRIC, 1, true>(ta, tb, a, grid, stream);
-      case 48: return launch_scan_kernel<FP8, 48, 5, METRIC, 1, true>(ta, tb, a, grid, stream);
-      default: return launch_scan_kernel<FP8, 64, 4, METRIC, 1, true>(ta, tb, a, grid, stream);
+      case 16: return launch_scan_kernel<FP8, 16, 6, METRIC, 1, true, TS>(ta, tb, a, grid, stream);
+      case 32: return launch_scan_kernel<FP8, 32, 5, METRIC, 1, true, TS>(ta, tb, a, grid, stream);
+      case 48: return launch_scan_kernel<FP8, 48, 5, METRIC, 1, true, TS>(ta, tb, a, grid, stream);
+      default: return launch_scan_kernel<FP8, 64, 4, METRIC, 1, true, TS>(ta, tb, a, grid, stream);
     }
   }
   if (groups == 2) {
     switch (kl) {
-      case 16: return launch_scan_kernel<FP8, 16, 3, METRIC, 2>(ta, tb, a, grid, stream);
-      case 32: return launch_scan_kernel<FP8, 32, 2, METRIC, 2>(ta, tb, a, grid, stream);
-      default: return launch_scan_kernel<FP8, 48, 2, METRIC, 2>(ta, tb, a, grid, stream);
+      case 16: return launch_scan_kernel<FP8, 16, 3, METRIC, 2, false, TS>(ta, tb, a, grid, stream);
+      case 32: return launch_scan_kernel<FP8, 32, 2, METRIC, 2, false, TS>(ta, tb, a, grid, stream);
+      default: return launch_scan_kernel<FP8, 48, 2, METRIC, 2, false, TS>(ta, tb, a, grid, stream);
     }
   }
   switch (kl) {
-    case 16: return launch_scan_kernel<FP8, 16, 4, METRIC, 1>(ta, tb, a, grid, stream);
-    case 32: return launch_scan_kernel<FP8, 32, 3, METRIC, 1>(ta, tb, a, grid, stream);
-    case 48: return launch_scan_kernel<FP8, 48, 3, METRIC, 1>(ta, tb, a, grid, stream);
-    default: return launch_scan_kernel<FP8, 64, 3, METRIC, 1>(ta, tb, a, grid, stream);
+    case 16: return launch_scan_kernel<FP8, 16, 4, METRIC, 1, false, TS>(ta, tb, a, grid, stream);
+    case 32: return launch_scan_kernel<FP8, 32, 3, METRIC, 1, false, TS>(ta, tb, a, grid, stream);
+    case 48: return launch_scan_kernel<FP8, 48, 3, METRIC, 1, false, TS>(ta, tb, a, grid, stream);
+    default: return launch_scan_kernel<FP8, 64, 3, METRIC, 1, false, TS>(ta, tb, a, grid, stream);
   }
 }
 
 template <bool FP8>
-cudaError_t dispatch_scan(int kl, int groups, int metric, const CUtensorMap& ta, const CUtensorMap& tb,
-                          const TcScanArgs& a, uint32_t grid, cudaStream_t stream) {
+cudaError_t dispatch_scan(int kl, int groups, int metric, bool table_scale, const CUtensorMap& ta,
+                          const CUtensorMap& tb, const TcScanArgs& a, uint32_t grid, cudaStream_t stream) {
+  // TS (fp8 only): false for a per-row-scale table, whose L2 / IP epilogue
+  // reads each row's scale and norm; cosine reads them either way
+  if constexpr (FP8) {
+    if (!table_scale && metric == METRIC_INNER_PRODUCT)
+      return dispatch_scan_kl<FP8, METRIC_INNER_PRODUCT, false>(kl, groups, ta, tb, a, grid, stream);
+    if (!table_scale && metric == METRIC_L2)
+      return dispatch_scan_kl<FP8, METRIC_L2, false>(kl, groups, ta, tb, a, grid, stream);
+  }
   switch (metric) {
     case METRIC_INNER_PRODUCT:
-      return dispatch_scan_kl<FP8, METRIC_INNER_PRODUCT>(kl, groups, ta, tb, a, grid, stream);
-    case METRIC_COSINE: return dispatch_scan_kl<FP8, METRIC_COSINE>(kl, groups, ta, tb, a, grid, stream);
-    default: return dispatch_scan_kl<FP8, METRIC_L2>(kl, groups, ta, tb, a, grid, stream);
+      return dispatch_scan_kl<FP8, METRIC_INNER_PRODUCT, true>(kl, groups, ta, tb, a, grid, stream);
+    case METRIC_COSINE: return dispatch_scan_kl<FP8, METRIC_COSINE, true>(kl, groups, ta, tb, a, grid, stream);
+    default: return dispatch_scan_kl<FP8, METRIC_L2, true>(kl, groups, ta, tb, a, grid, stream);
   }
 }
 

@@ -47,7 +47,7 @@ class Fp16GpuTables(C.Structure):
 
 class FvFp8GpuTables(C.Structure):
     _fields_ = [("d_vectors_fp8", P), ("d_scales", P), ("d_vec_norms_sq", P), ("d_vectors", P),
-                ("num_vectors", U32), ("dim", U32), ("padded_dim", U32)]
+                ("num_vectors", U32), ("dim", U32), ("padded_dim", U32), ("scale_mode", U32)]
 
 
 class FvIvfOptions(C.Structure):
@@ -144,6 +144,7 @@ SIGNATURES = {
     "fv_fp8_search_batch": (I32, [P, P, U32, U32, I32, P, P, P, P]),
     "fv_encode_fp16_padded": (I32, [P, U32, U32, U32, P, P, P]),
     "fv_encode_fp8": (I32, [P, U32, U32, U32, P, P, P, P]),
+    "fv_encode_fp8_per_vector": (I32, [P, U32, U32, U32, P, P, P, P]),
     "fv_index_create": (I32, [P, P]),
     "fv_index_destroy": (I32, [P]),
     "fv_index_build": (I32, [P, P, U32]),

@@ -124,15 +124,37 @@ class Fp16Table:
                                          self.n, self.dim, self.pd)
 
 
+def encode_fp8_per_vector(vectors, pd=None, stream=None):
+    """fv_encode_fp8_per_vector: e4m3 rows with per-vector scales max|x|/448
+    (the scale_mode 1 layout) + compensated ||x||^2."""
+    n, dim = vectors.shape
+    pd = pd or padded_dim(dim)
+    out = torch.empty((n, pd), dtype=torch.uint8, device=vectors.device)
+    scales = torch.empty((n,), dtype=torch.float32, device=vectors.device)
+    norms = torch.empty((n,), dtype=torch.float32, device=vectors.device)
+    call("fv_encode_fp8_per_vector", _ptr(vectors), n, dim, pd, _ptr(out), _ptr(scales), _ptr(norms),
+         _stream(stream))
+    return out, scales, norms
+
+
 class Fp8Table:
-    def __init__(self, vectors, keep_fp32=True, stream=None):
+    """Device-resident fp8 flat table (+ optional fp32 copy for rescoring).
+    per_vector=False: one power-of-two table scale with norm digits (scale
+    mode 0); True: per-vector scales max|x|/448 (scale mode 1)."""
+
+    def __init__(self, vectors, keep_fp32=True, stream=None, per_vector=False):
         self.n, self.dim = vectors.shape
-        self.pd = fp8_padded_dim(self.dim)
-        self.fp8, self.scales, self.norms = encode_fp8(vectors, self.pd, stream)
+        self.per_vector = per_vector
+        if per_vector:
+            self.pd = padded_dim(self.dim)
+            self.fp8, self.scales, self.norms = encode_fp8_per_vector(vectors, self.pd, stream)
+        else:
+            self.pd = fp8_padded_dim(self.dim)
+            self.fp8, self.scales, self.norms = encode_fp8(vectors, self.pd, stream)
         self.fp32 = vectors if keep_fp32 else None
         self.struct = _lib.FvFp8GpuTables(self.fp8.data_ptr(), self.scales.data_ptr(), self.norms.data_ptr(),
                                           self.fp32.data_ptr() if self.fp32 is not None else None,
-                                          self.n, self.dim, self.pd)
+                                          self.n, self.dim, self.pd, 1 if per_vector else 0)
 
 
 def options(overfetch=0, boundary_fp64=1, boundary_eps=0.0, splits=0):

@@ -197,10 +197,11 @@ int fv_fp16_search_batch_ex(const Fp16GpuTables* tables, const float* d_queries,
                             GpuSearchResult* d_out_results, void* stream);
 
 /* FP8 (E4M3) tensor-core flat scan over a table written by fv_encode_fp8
- * (padded_dim >= dim + 3); same contract as the fp16 scan. Queries get a
- * power-of-two scale (the smallest 2^a with max|q| <= 448 * 2^a, at least
- * 2^(b-8) for the table scale 2^b). No reference counterpart (the
- * reference has no fp8 path). */
+ * (scale_mode 0, padded_dim >= dim + 3) or fv_encode_fp8_per_vector
+ * (scale_mode 1); same contract as the fp16 scan. Queries get a power-of-two
+ * scale over a mode-0 table (the smallest 2^a with max|q| <= 448 * 2^a, at
+ * least 2^(b-8) for the table scale 2^b), max|q| / 448 over a mode-1 table.
+ * No reference counterpart (the reference has no fp8 path). */
 int fv_fp8_search_batch(const FvFp8GpuTables* tables, const float* d_queries,
                         uint32_t num_queries, uint32_t top_k, MetricType metric,
                         const uint32_t* d_valid_mask, const FvScanOptions* options,
@@ -217,6 +218,11 @@ int fv_encode_fp16_padded(const float* d_vectors, uint32_t num_vectors, uint32_t
 int fv_encode_fp8(const float* d_vectors, uint32_t num_vectors, uint32_t dim,
                   uint32_t padded_dim, uint8_t* d_out_fp8, float* d_out_scales,
                   float* d_out_norms_sq, void* stream);
+/* The per-vector-scale fp8 layout (FvFp8GpuTables scale_mode 1):
+ * padded_dim a multiple of 16, >= dim; all three outputs required. */
+int fv_encode_fp8_per_vector(const float* d_vectors, uint32_t num_vectors, uint32_t dim,
+                             uint32_t padded_dim, uint8_t* d_out_fp8, float* d_out_scales,
+                             float* d_out_norms_sq, void* stream);
 
 /* ---- host engine -------------------------------------------------------
  * The reference's GpuVectorIndex (crates/engine/src/index.rs:131-2634) for

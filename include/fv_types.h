@@ -103,7 +103,9 @@ typedef struct {
     uint32_t padded_dim;
 } Fp16GpuTables;
 
-/* FP8 (E4M3) flat tables; no reference counterpart. One power-of-two
+/* FP8 (E4M3) flat tables; no reference counterpart. Two layouts, chosen by
+ * scale_mode.
+ * scale_mode 0 (fv_encode_fp8; the zero default): one power-of-two
  * scale s = 2^b for the table, the smallest with max_v ||x_v||^2 <= 896 s^2
  * (1 for an all-zero table); every d_scales[v] holds s. Row v of
  * d_vectors_fp8 holds round_e4m3(x_v[d] / s) for d < dim (round to nearest
@@ -111,7 +113,11 @@ typedef struct {
  * e4m3 value nearest ||x_v||^2 / (2 s^2), n2 and n3 the e4m3 values nearest
  * what the earlier digits leave), then zero padding up to padded_dim (a
  * multiple of 16, >= dim + 3). d_vec_norms_sq holds ||x_v||^2 of the fp32
- * row (compensated sum). */
+ * row (compensated sum).
+ * scale_mode 1 (fv_encode_fp8_per_vector): per-vector scales d_scales[v] =
+ * max|x_v| / 448 (1 for a zero row), codes round_e4m3(x_v[d] / d_scales[v]),
+ * zero padding from dim (padded_dim a multiple of 16, >= dim); the scan then
+ * applies each row's scale and norm per value. */
 typedef struct {
     const uint8_t* d_vectors_fp8;   /* [num_vectors * padded_dim] E4M3 bytes     */
     const float* d_scales;          /* [num_vectors] per-vector dequant scale    */
@@ -120,6 +126,7 @@ typedef struct {
     uint32_t num_vectors;
     uint32_t dim;
     uint32_t padded_dim;
+    uint32_t scale_mode;            /* 0: table scale + norm digits, 1: per-vector */
 } FvFp8GpuTables;
 
 /* Tuning knobs of the reduced-precision flat scans; no reference

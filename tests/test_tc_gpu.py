@@ -130,6 +130,66 @@ def test_encode_fp8(cuda):
     assert torch.all(z_codes == 0) and torch.all(z_scales == 1.0)
 
 
+def test_encode_fp8_per_vector(cuda):
+    """The per-vector layout: scale max|x|/448 per row (1 for a zero row),
+    codes e4m3(x / scale), zero padding, compensated ||x||^2."""
+    from fvgb300 import scan
+
+    torch = cuda
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((500, 96)).astype(np.float32)
+    x[3] = 0.0
+    codes, scales, norms = scan.encode_fp8_per_vector(torch.from_numpy(x).cuda())
+    amax = np.abs(x).max(axis=1)
+    exp_scale = np.where(amax > 0, amax / np.float32(448.0), 1.0).astype(np.float32)
+    assert np.array_equal(scales.cpu().numpy(), exp_scale)
+    ref = (torch.from_numpy(x).cuda() / scales[:, None]).to(torch.float8_e4m3fn).view(torch.uint8)
+    assert torch.equal(codes[:, :96], ref)
+    assert np.allclose(norms.cpu().numpy(), (x.astype(np.float64) ** 2).sum(1), rtol=1e-6)
+
+
+@pytest.mark.parametrize("metric", ["ip", "l2", "cosine"])
+@pytest.mark.parametrize("n,dim,nq,k", [(20000, 96, 200, 10), (5003, 70, 129, 16), (257, 253, 64, 10)])
+def test_fp8_per_vector_ranking_without_rescore(cuda, metric, n, dim, nq, k):
+    """Per-vector-scale table, no fp32 copy: results are the top-k of the fp8
+    tensor-core distance with each row's scale and norm applied per value,
+    checked against an fp64 evaluation of the same e4m3 products."""
+    from fvgb300 import scan
+
+    torch = cuda
+    rng = np.random.default_rng(n + dim + 1)
+    base = (rng.standard_normal((n, dim)) + rng.standard_normal((32, dim))[rng.integers(0, 32, n)]).astype(np.float32)
+    base *= rng.uniform(0.5, 2.0, (n, 1)).astype(np.float32)
+    queries = (rng.standard_normal((nq, dim)) * 1.3).astype(np.float32)
+    table = scan.Fp8Table(torch.from_numpy(base).cuda(), keep_fp32=False, per_vector=True)
+    res = scan.fp8_search(table, torch.from_numpy(queries).cuda(), k, metric, opts=scan.options(boundary_fp64=0))
+    torch.cuda.synchronize()
+    ids, dist = res_np(res)
+    xs = table.scales.cpu().numpy().astype(np.float64)
+    x8 = table.fp8.view(torch.float8_e4m3fn).double().cpu().numpy()[:, :dim]
+    xn = table.norms.cpu().numpy().astype(np.float64)
+    qn = (queries.astype(np.float64) ** 2).sum(1)
+    amax = np.abs(queries).max(axis=1)
+    qs = np.where(amax > 0, amax / np.float32(448.0), 1.0).astype(np.float32)
+    q8 = (torch.from_numpy(queries).cuda() / torch.from_numpy(qs).cuda()[:, None]).to(torch.float8_e4m3fn)
+    q8 = q8.double().cpu().numpy()
+    dots = (q8 @ x8.T) * qs.astype(np.float64)[:, None] * xs[None, :]
+    if metric == "ip":
+        d64 = -dots
+    elif metric == "l2":
+        d64 = np.maximum(0, qn[:, None] + xn[None, :] - 2 * dots)
+    else:
+        d64 = 1 - dots / (np.sqrt(qn[:, None] * xn[None, :]) + 1e-8)
+    order = np.argsort(d64, axis=1, kind="stable")[:, :k]
+    hit = np.mean([len(set(ids[i]) & set(order[i])) / k for i in range(nq)])
+    assert hit >= 0.995, hit
+    got = np.take_along_axis(d64, ids.astype(np.int64), axis=1)
+    scale = np.abs(d64).max(axis=1, keepdims=True)
+    assert np.all(np.abs(dist - got) <= 2e-5 * np.maximum(scale, 1.0)), np.abs(dist - got).max()
+    assert np.all(dist[:, :-1] <= dist[:, 1:])
+    assert scan.device_status() == 0
+
+
 @pytest.mark.parametrize("metric", ["ip", "l2", "cosine"])
 @pytest.mark.parametrize("n,dim,nq,k", [(20000, 96, 200, 10), (5003, 70, 129, 16), (1000, 128, 1, 5),
                                         (257, 253, 64, 10)])
@@ -326,17 +386,18 @@ def test_fp16_tiny_and_empty(cuda):
     assert scan.device_status() == 0
 
 
+@pytest.mark.parametrize("per_vector", [False, True])
 @pytest.mark.parametrize("k", [10, 100])
-def test_fp8_rescored_recall(cuda, oracle_mod, k):
-    """fp8 E4M3 with per-row scales, fp32 rescore, fp64 boundary band, on
-    data shaped like the 10M x 96 workload (N(0,1) component means, sigma
-    0.5), scaled down."""
+def test_fp8_rescored_recall(cuda, oracle_mod, k, per_vector):
+    """fp8 E4M3 (table scale + norm digits, or per-vector scales), fp32
+    rescore, fp64 boundary band, on data shaped like the 10M x 96 workload
+    (N(0,1) component means, sigma 0.5), scaled down."""
     from fvgb300 import datasets, scan
 
     torch = cuda
     base = datasets.sample_np(datasets.FP8_L2, 60000, seed=2, stream=0)
     queries = datasets.sample_np(datasets.FP8_L2, 96, seed=2, stream=1)
-    table = scan.Fp8Table(torch.from_numpy(base).cuda())
+    table = scan.Fp8Table(torch.from_numpy(base).cuda(), per_vector=per_vector)
     res = scan.fp8_search(table, torch.from_numpy(queries).cuda(), k, "l2")
     torch.cuda.synchronize()
     ids, dist = res_np(res)
