@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
   __shared__ uint32_t s_q, s_cnt;
   __shared__ uint64_t s_tau;
 
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x;
   const bool vec16 = (a.code_bytes % 16u) == 0 && ((uintptr_t)a.codes % 16u) == 0;
   float* mins = tab + a.dim;      // SQ8 only
   float* scales = tab + 2 * a.dim;
