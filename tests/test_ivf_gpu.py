@@ -102,6 +102,32 @@ def test_ivf_mask_and_list_major(cuda, oracle_mod, e2e_case, mode):
     assert np.array_equal(ids, ids2) and np.array_equal(dist, dist2)
 
 
+@pytest.mark.parametrize("mode", MODES)
+def test_ivf_mask_with_an_id_space_beyond_the_lists(cuda, oracle_mod, e2e_case, mode):
+    """num_vectors larger than the lists' posting count (an engine whose
+    slots carry remapped ids reports its id space): the list-order mask pass
+    reads ids only inside the lists, and the answer is the oracle's."""
+    from fvgb300.datasets import pack_bools
+    from fvgb300.ivf import IvfTable
+
+    torch = cuda
+    x, t = e2e_case
+    allowed = np.zeros(x.shape[0] + 5000, dtype=bool)
+    allowed[5:900] = True
+    words = pack_bools(allowed)
+    q = x[:4]
+    table = IvfTable(mode, t, vectors=x)
+    table.struct.num_vectors = table.n + 5000
+    res = table.search(torch.from_numpy(np.ascontiguousarray(q)).cuda(), 5, 8, 64, "l2",
+                       mask=torch.from_numpy(words.view(np.int32)).cuda())
+    torch.cuda.synchronize()
+    ids, dist = res_np(res)
+    fn = oracle_fn(oracle_mod, mode)
+    assert_same(ids, dist, fn(t, x, q, 5, 8, 64, mask=words[:(x.shape[0] + 31) // 32]))
+    valid = ids[ids != 0xFFFFFFFF]
+    assert valid.size > 0 and np.all(allowed[valid])
+
+
 def test_ivf_large_k_sorted(cuda, oracle_mod):
     """python/tests/test_bindings.py:123-138: k=100 over N=1000, d=64,
     nlist=16, m_pq=8, nprobe=16 -> sorted, >= 90% filled."""
