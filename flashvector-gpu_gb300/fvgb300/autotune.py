@@ -40,6 +40,8 @@ SHAPES = {
     "fp16_ip_1M_q1024_k100": ("fp16", "ip", 1_000_000, 768, 1024, 100, "FP16_IP_UNIT", 0.5, (4,)),
     "fp16_ip_1M_q64_k10": ("fp16", "ip", 1_000_000, 768, 64, 10, "FP16_IP_UNIT", 0.5, (4,)),
     "fp16_ip_1M_q1_k10": ("fp16", "ip", 1_000_000, 768, 1, 10, "FP16_IP_UNIT", 0.5, (4,)),
+    "fp16_ip_1M_q64_k100": ("fp16", "ip", 1_000_000, 768, 64, 100, "FP16_IP_UNIT", 0.5, (4,)),
+    "fp16_ip_1M_q1_k100": ("fp16", "ip", 1_000_000, 768, 1, 100, "FP16_IP_UNIT", 0.5, (4,)),
     "fp8_l2_10M_q10000_k100": ("fp8", "l2", 10_000_000, 96, 10_000, 100, "FP8_L2", 0.0, (4, 3, 2)),
 }
 
