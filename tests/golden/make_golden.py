@@ -60,8 +60,9 @@ def make_case(FB, name, seed, n, nq, dim, k, metric, kind, comps, sigma, p_valid
 
 
 def main(argv):
-    ref = Path(argv[1]) if len(argv) > 1 else Path("/root/reference")
-    FB = load_fake_backend(ref)
+    if len(argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/FlashVector-GPU")
+    FB = load_fake_backend(Path(argv[1]))
     make_case(FB, "flat_l2_int", 11, 2500, 32, 128, 10, "l2", "int255", 64, 20.0, 0.5)
     make_case(FB, "flat_l2_int_k100", 12, 2500, 16, 33, 100, "l2", "int255", 16, 8.0, 0.3)
     make_case(FB, "flat_ip_unit", 13, 2000, 32, 96, 16, "ip", "unit", 64, 0.3, 0.5)

@@ -261,3 +261,23 @@ def test_rabitq_gpu_encoder_matches_host_encoder(cuda, oracle_mod, dim):
     assert np.array_equal(enc["rot_centroids"].cpu().numpy().view(np.uint32), t["rot_centroids"].view(np.uint32))
     assert np.array_equal(enc["rabitq_bits"].cpu().numpy().view(np.uint32), t["rabitq_bits"])
     assert np.array_equal(enc["rabitq_meta"].cpu().numpy().view(np.uint32), t["rabitq_meta"].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", ["ivf_e2e", "ivf_zipf"])
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("list_major", [False, True])
+def test_ivf_matches_reference_kernels(cuda, name, mode, list_major):
+    """The drop-in cuda_ivf_{pq,sq,rabitq}_search_batch (reference layout:
+    codes by vector id) and the list-major fv_*_ex path against the
+    reference's own kernels' recorded outputs (tests/golden/ivf_*.npz, made
+    by tests/golden/make_ivf_golden.py on a GB300): every case of the
+    e2e_search_test.rs:231-288 parameters and of the Zipf-skewed 64-list
+    input. Tolerances and the tie rule: tests/ivf_golden.py."""
+    import ivf_golden
+
+    base, queries, mask, t, cases, ref = ivf_golden.load(name)
+    for ci, c in enumerate(cases):
+        ids, dist = run(cuda, t, base, queries, mode, c["k"], c["nprobe"], c["rerank"], c["metric"],
+                        mask=mask if c["mask"] else None, list_major=list_major)
+        bad = ivf_golden.compare(mode, c, ids, dist, *ref[(mode, ci)])
+        assert not bad, (ci, c, bad[:3])

@@ -261,3 +261,45 @@ def test_rabitq_estimate_tracks_distance(oracle_mod, ivf_case):
     ids = res["id"][0]
     exact = ((x[ids] - q[0]) ** 2).sum(1)
     assert np.corrcoef(res["distance"][0], exact)[0, 1] > 0.8
+
+
+@pytest.mark.parametrize("name", ["ivf_e2e", "ivf_zipf"])
+@pytest.mark.parametrize("mode", ["pq", "sq8", "rabitq"])
+def test_oracle_ivf_matches_reference_kernels(oracle_mod, name, mode):
+    """Pins the oracle's IVF-PQ / IVF-SQ8 / IVF-RaBitQ search to the
+    reference's own CUDA kernels: tests/golden/ivf_*.npz hold their outputs
+    (recorded on a GB300 by tests/golden/make_ivf_golden.py) for the
+    e2e_search_test.rs:231-288 parameters and a Zipf-skewed 64-list case,
+    over rerank 0 / 1 / 20 / 256 / 400 / 512, nprobe 8-32, k 10 / 16 / 100,
+    L2 / IP / cosine and masks. Tolerances and the tie rule: tests/ivf_golden.py."""
+    import ivf_golden
+
+    base, queries, mask, t, cases, ref = ivf_golden.load(name)
+    fn = {"pq": oracle_mod.ivf_pq_search, "sq8": oracle_mod.ivf_sq_search,
+          "rabitq": oracle_mod.ivf_rabitq_search}[mode]
+    for ci, c in enumerate(cases):
+        r = fn(t, base, queries, c["k"], c["nprobe"], c["rerank"], c["metric"], mask=mask if c["mask"] else None)
+        bad = ivf_golden.compare(mode, c, r["id"], r["distance"], *ref[(mode, ci)])
+        assert not bad, (ci, c, bad[:3])
+
+
+def test_ivf_reference_compare_rejects_planted_errors(oracle_mod):
+    """The fixture comparison is not vacuous: a swapped id pair outside a tie,
+    a distance one ulp off in an exact case, and a missing neighbour are each
+    reported (mistakes planted in the oracle's output, on the CPU)."""
+    import ivf_golden
+
+    base, queries, mask, t, cases, ref = ivf_golden.load("ivf_e2e")
+    c = cases[0]
+    r = oracle_mod.ivf_pq_search(t, base, queries, c["k"], c["nprobe"], c["rerank"], c["metric"])
+    ids, dist = r["id"].copy(), r["distance"].copy()
+    assert not ivf_golden.compare("pq", c, ids, dist, *ref[("pq", 0)])
+    swapped = ids.copy()
+    swapped[3, [1, 2]] = swapped[3, [2, 1]]
+    assert ivf_golden.compare("pq", c, swapped, dist, *ref[("pq", 0)])
+    ulp = dist.copy()
+    ulp[5, 4] = np.nextafter(ulp[5, 4], np.float32(np.inf))
+    assert ivf_golden.compare("pq", c, ids, ulp, *ref[("pq", 0)])
+    missing = ids.copy()
+    missing[7, 2] = 1499 if missing[7, 2] != 1499 else 1498
+    assert ivf_golden.compare("pq", c, missing, dist, *ref[("pq", 0)])
