@@ -212,6 +212,7 @@ class Index {
     }
   }
   int launch_batch(const BatchLaunch& b, cudaStream_t s);
+  size_t batch_scratch_bytes(const BatchLaunch& b) const;
   int load_snapshot(const snap::File& f, std::string* error);
   int save_snapshot(const char* path, std::string* error);
   uint32_t dim() const { return cfg_.dim; }
@@ -249,6 +250,8 @@ class Index {
   void slot_mask(const uint32_t* user, uint32_t words, std::vector<uint32_t>& out, bool& use) const;
   void delta_mask(const uint32_t* user, uint32_t words, std::vector<uint32_t>& out, bool& use) const;
   void record(double seconds, uint32_t nq);
+  IvfLaunch batch_ivf_launch(const BatchLaunch& b, GpuSearchResult* out) const;
+  TcTables tc_tables(bool fp8) const;
 
   FvIndexConfig cfg_;
   std::vector<std::unique_ptr<Stream>> streams_;
@@ -1138,6 +1141,53 @@ int Index::save_snapshot(const char* path, std::string* error) {
 // words for tombstones, per-query filters over logical ids), the delta
 // scan of the live-insert buffer (validity words over delta slots, filters
 // through the delta ids) and the stable merge, all stream-ordered.
+// The IVF launch of a served batch (list-major tables, the batch's
+// per-query parameters and filters), writing `out`.
+IvfLaunch Index::batch_ivf_launch(const BatchLaunch& b, GpuSearchResult* out) const {
+  const bool pq = b.engine == FV_ENGINE_IVF_PQ, rq = b.engine == FV_ENGINE_IVF_RABITQ;
+  IvfLaunch L{};
+  L.centroids = centroids_.p;
+  L.codebooks = pq ? codebooks_.p : nullptr;
+  L.sq_mins = pq ? nullptr : sq_mins_.p;
+  L.sq_scales = pq ? nullptr : sq_scales_.p;
+  L.codes = pq ? pq_codes_lm_.p : sq_codes_lm_.p;
+  L.offsets = offsets_.p;
+  L.vec_ids = vec_ids_.p;
+  L.vectors = vectors_.p;
+  L.num_vectors = n_;
+  L.dim = cfg_.dim;
+  L.nlist = nlist_;
+  L.m_pq = pq ? cfg_.m_pq : 0;
+  L.sub_dim = pq ? cfg_.dim / cfg_.m_pq : 0;
+  L.list_major = true;
+  L.queries = b.d_queries;
+  L.nq = b.nq;
+  L.top_k = b.top_k;
+  L.nprobe = b.nprobe;
+  L.rerank_k = b.rerank_k;
+  L.metric = (MetricType)cfg_.metric;
+  L.mask = tombstones_.empty() ? nullptr : valid_words_.p;
+  L.out = out;
+  L.q_topk = b.d_topk;
+  L.q_nprobe = b.d_nprobe;
+  L.q_rerank = b.d_rerank;
+  L.filters = b.d_filters;
+  if (rq) {
+    L.codes = nullptr;
+    L.rot_centroids = rq_cent_.p;
+    L.rq_bits = rq_bits_lm_.p;
+    L.rq_meta = rq_meta_lm_.p;
+    L.rot_signs = rq_signs_.p;
+    L.padded_dim = rq_pd_;
+  }
+  return L;
+}
+
+TcTables Index::tc_tables(bool fp8) const {
+  return fp8 ? TcTables{true, fp8_.p, fp8_norms_.p, fp8_scales_.p, vectors_.p, n_, cfg_.dim, pd8_}
+             : TcTables{false, fp16_.p, norms16_.p, nullptr, vectors_.p, n_, cfg_.dim, pd16_};
+}
+
 int Index::launch_batch(const BatchLaunch& b, cudaStream_t s) {
   if (!built_) return FV_ERR_ARG;
   if (b.nq == 0 || b.top_k == 0) return 0;
@@ -1161,9 +1211,7 @@ int Index::launch_batch(const BatchLaunch& b, cudaStream_t s) {
     case FV_ENGINE_FP8: {
       const bool fp8 = b.engine == FV_ENGINE_FP8;
       if (fp8 ? !fp8_.p : !fp16_.p) return FV_ERR_ARG;
-      const TcTables t = fp8 ? TcTables{true, fp8_.p, fp8_norms_.p, fp8_scales_.p, vectors_.p, n_, dim, pd8_}
-                             : TcTables{false, fp16_.p, norms16_.p, nullptr, vectors_.p, n_, dim, pd16_};
-      rc = launch_tc_scan(t, b.d_queries, nq, k, metric, shared_mask, main_out, b.scan, s, b.d_filters);
+      rc = launch_tc_scan(tc_tables(fp8), b.d_queries, nq, k, metric, shared_mask, main_out, b.scan, s, b.d_filters);
       break;
     }
     case FV_ENGINE_IVF_PQ:
@@ -1171,46 +1219,11 @@ int Index::launch_batch(const BatchLaunch& b, cudaStream_t s) {
     case FV_ENGINE_IVF_RABITQ: {
       const bool pq = b.engine == FV_ENGINE_IVF_PQ, rq = b.engine == FV_ENGINE_IVF_RABITQ;
       if (rq ? !rq_pd_ : pq ? !pq_codes_lm_.p : !sq_codes_lm_.p) return FV_ERR_ARG;
-      IvfLaunch L{};
-      L.centroids = centroids_.p;
-      L.codebooks = pq ? codebooks_.p : nullptr;
-      L.sq_mins = pq ? nullptr : sq_mins_.p;
-      L.sq_scales = pq ? nullptr : sq_scales_.p;
-      L.codes = pq ? pq_codes_lm_.p : sq_codes_lm_.p;
-      L.offsets = offsets_.p;
-      L.vec_ids = vec_ids_.p;
-      L.vectors = vectors_.p;
-      L.num_vectors = n_;
-      L.dim = dim;
-      L.nlist = nlist_;
-      L.m_pq = pq ? cfg_.m_pq : 0;
-      L.sub_dim = pq ? dim / cfg_.m_pq : 0;
-      L.list_major = true;
-      L.queries = b.d_queries;
-      L.nq = nq;
-      L.top_k = k;
-      L.nprobe = b.nprobe;
-      L.rerank_k = b.rerank_k;
-      L.metric = metric;
-      L.mask = shared_mask;
-      L.out = main_out;
-      L.q_topk = b.d_topk;
-      L.q_nprobe = b.d_nprobe;
-      L.q_rerank = b.d_rerank;
-      L.filters = b.d_filters;
-      if (rq) {
-        L.codes = nullptr;
-        L.rot_centroids = rq_cent_.p;
-        L.rq_bits = rq_bits_lm_.p;
-        L.rq_meta = rq_meta_lm_.p;
-        L.rot_signs = rq_signs_.p;
-        L.padded_dim = rq_pd_;
-      }
       if (nlist_ == 0 || (pq && cfg_.m_pq == 0)) {
         rc = launch_fill_sentinel(main_out, (size_t)nq * k, s);
         break;
       }
-      rc = launch_ivf_search(rq ? IVF_MODE_RABITQ : pq ? IVF_MODE_PQ : IVF_MODE_SQ8, L, s);
+      rc = launch_ivf_search(rq ? IVF_MODE_RABITQ : pq ? IVF_MODE_PQ : IVF_MODE_SQ8, batch_ivf_launch(b, main_out), s);
       break;
     }
     default:
@@ -1221,6 +1234,38 @@ int Index::launch_batch(const BatchLaunch& b, cudaStream_t s) {
                        delta_.d_live.p, b.d_delta, 0, s, b.d_filters);
   if (rc) return rc;
   return launch_merge_main_delta(b.d_main, b.d_delta, nq, k, b.d_topk, k, b.d_out, s);
+}
+
+// Scratch that launch_batch takes from its stream's arena for `b`: the
+// largest request of its launches (they run in order on one stream, so
+// they share one arena). Only b.engine, nq, top_k, nprobe, rerank_k, scan
+// and whether the per-query arrays are present are read.
+size_t Index::batch_scratch_bytes(const BatchLaunch& b) const {
+  if (!built_ || b.nq == 0 || b.top_k == 0) return 0;
+  const MetricType metric = (MetricType)cfg_.metric;
+  size_t need = 0;
+  switch (b.engine) {
+    case FV_ENGINE_FLAT:
+      need = plan_flat_f32(n_, b.nq, std::min(b.top_k, 256u), 0).scratch_bytes;
+      break;
+    case FV_ENGINE_FP16:
+    case FV_ENGINE_FP8:
+      need = tc_scan_scratch_bytes(tc_tables(b.engine == FV_ENGINE_FP8), b.nq, b.top_k, metric, b.scan);
+      break;
+    case FV_ENGINE_IVF_PQ:
+    case FV_ENGINE_IVF_SQ8:
+    case FV_ENGINE_IVF_RABITQ: {
+      const bool pq = b.engine == FV_ENGINE_IVF_PQ, rq = b.engine == FV_ENGINE_IVF_RABITQ;
+      need = ivf_search_scratch_bytes(rq ? IVF_MODE_RABITQ : pq ? IVF_MODE_PQ : IVF_MODE_SQ8,
+                                      batch_ivf_launch(b, nullptr));
+      break;
+    }
+    default:
+      return 0;
+  }
+  if (delta_.len() > 0)
+    need = std::max(need, plan_flat_f32(delta_.len(), b.nq, std::min(b.top_k, 256u), 0).scratch_bytes);
+  return need;
 }
 
 // ------------------------------------------------------------- metrics
@@ -1343,6 +1388,7 @@ uint32_t index_nlist(const Index* index) { return index->nlist(); }
 void index_pin(Index* index) { index->pin(); }
 void index_unpin(Index* index) { index->unpin(); }
 int index_launch_batch(Index* index, const BatchLaunch& b, cudaStream_t stream) { return index->launch_batch(b, stream); }
+size_t index_batch_scratch_bytes(const Index* index, const BatchLaunch& b) { return index->batch_scratch_bytes(b); }
 }  // namespace fv
 
 extern "C" {

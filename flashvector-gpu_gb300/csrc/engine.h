@@ -56,5 +56,10 @@ void index_unpin(Index* index);
 // has passed the batch). Returns 0 or an error code; nothing is launched
 // on an argument error.
 int index_launch_batch(Index* index, const BatchLaunch& b, cudaStream_t stream);
+// The stream scratch (bytes) index_launch_batch takes for `b` (its device
+// pointers are not read; the per-query parameter arrays only count as
+// present or absent). The state may change with build / add / delete: a
+// caller that relies on the figure holds a pin from estimate to launch.
+size_t index_batch_scratch_bytes(const Index* index, const BatchLaunch& b);
 
 }  // namespace fv

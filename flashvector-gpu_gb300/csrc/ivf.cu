@@ -683,21 +683,32 @@ __global__ void relayout_codes_kernel(const uint8_t* __restrict__ by_id, const u
 
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
-}  // namespace
+// Every size of one IVF search call, computed once: launch_ivf_search
+// launches from it and the serving loop admits a batch by scratch_bytes.
+// rc: 0 to launch, 1 when the call has nothing to do, else an error code.
+struct IvfPlan {
+  int rc = 0;
+  uint32_t P = 0, top_k = 0, nprobe = 0, shortlist = 0, G = 1, sms = 0, list_n = 0;
+  FlatPlan cp;
+  size_t coarse_bytes = 0, probe_bytes = 0, part_bytes = 0, allow_bytes = 0, scratch_bytes = 0;
+};
 
-int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
-  if (L.nq == 0 || L.top_k == 0 || L.nlist == 0) return 0;
-  if (mode == IVF_PQ && L.m_pq == 0) return 0;
-  if (L.dim == 0) return 0;
+IvfPlan plan_ivf_search(int mode, const IvfLaunch& L) {
+  IvfPlan Q{};
+  auto refuse = [&](int rc) {
+    Q.rc = rc;
+    return Q;
+  };
+  if (L.nq == 0 || L.top_k == 0 || L.nlist == 0 || L.dim == 0 || (mode == IVF_PQ && L.m_pq == 0)) return refuse(1);
   const uint32_t P = mode == IVF_RABITQ ? L.padded_dim : 0;
-  if (mode == IVF_RABITQ && (P < 32 || P > 4096 || (P & (P - 1)) || P < L.dim)) return FV_ERR_ARG;
+  if (mode == IVF_RABITQ && (P < 32 || P > 4096 || (P & (P - 1)) || P < L.dim)) return refuse(FV_ERR_ARG);
   // uniform batch: the clamps of the call; heterogeneous batch: top_k,
   // nprobe and rerank_k are the batch maxima and bound every query's values
   uint32_t top_k = L.top_k, nprobe = L.nprobe;
   uint32_t shortlist = ivf_clamps(top_k, nprobe, L.rerank_k, L.nlist);
   if (L.q_rerank) shortlist = std::min(std::max(std::max(L.rerank_k, top_k), shortlist), MAX_SHORTLIST);
-  if (nprobe > (uint32_t)kMaxTopK) return FV_ERR_ARG;  // coarse selection keeps <= 256 lists
-  if (mode == IVF_PQ && (L.sub_dim == 0 || L.m_pq * L.sub_dim > L.dim)) return FV_ERR_ARG;
+  if (nprobe > (uint32_t)kMaxTopK) return refuse(FV_ERR_ARG);  // coarse selection keeps <= 256 lists
+  if (mode == IVF_PQ && (L.sub_dim == 0 || L.m_pq * L.sub_dim > L.dim)) return refuse(FV_ERR_ARG);
 
   // Work items: with fewer queries than ~4 CTAs per SM, each query's probed
   // postings are cut into G equal ranges (a Zipf-giant list spreads over G
@@ -719,8 +730,37 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   const size_t part_bytes = G > 1 ? align256((size_t)L.nq * G * shortlist * 8) : 0;
   const uint32_t list_n = L.mask ? L.num_vectors : 0u;
   const size_t allow_bytes = align256(((size_t)list_n + 31) / 32 * 4);
-  uint8_t* scratch =
-      static_cast<uint8_t*>(scratch_get(stream, coarse_bytes + probe_bytes + part_bytes + 256 + allow_bytes));
+  Q.P = P;
+  Q.top_k = top_k;
+  Q.nprobe = nprobe;
+  Q.shortlist = shortlist;
+  Q.G = G;
+  Q.sms = sms;
+  Q.list_n = list_n;
+  Q.cp = cp;
+  Q.coarse_bytes = coarse_bytes;
+  Q.probe_bytes = probe_bytes;
+  Q.part_bytes = part_bytes;
+  Q.allow_bytes = allow_bytes;
+  Q.scratch_bytes = coarse_bytes + probe_bytes + part_bytes + 256 + allow_bytes;
+  return Q;
+}
+
+}  // namespace
+
+size_t ivf_search_scratch_bytes(int mode, const IvfLaunch& L) {
+  const IvfPlan Q = plan_ivf_search(mode, L);
+  return Q.rc == 0 ? Q.scratch_bytes : 0;
+}
+
+int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
+  const IvfPlan Q = plan_ivf_search(mode, L);
+  if (Q.rc) return Q.rc == 1 ? 0 : Q.rc;
+  const uint32_t P = Q.P, top_k = Q.top_k, nprobe = Q.nprobe, shortlist = Q.shortlist, G = Q.G, sms = Q.sms;
+  const uint32_t list_n = Q.list_n;
+  const FlatPlan& cp = Q.cp;
+  const size_t coarse_bytes = Q.coarse_bytes, probe_bytes = Q.probe_bytes, part_bytes = Q.part_bytes;
+  uint8_t* scratch = static_cast<uint8_t*>(scratch_get(stream, Q.scratch_bytes));
   if (!scratch) return (int)cudaErrorMemoryAllocation;
   uint32_t* list_allow =
       list_n ? reinterpret_cast<uint32_t*>(scratch + coarse_bytes + probe_bytes + part_bytes + 256) : nullptr;

@@ -117,6 +117,9 @@ cudaError_t dispatch_tc_scan_fp8(int kl, int groups, int metric, bool table_scal
 int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
                    const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream,
                    const QueryFilter* filters = nullptr);
+// The scratch bytes launch_tc_scan takes from the stream's arena for the
+// same arguments (same plan, same tuning knobs).
+size_t tc_scan_scratch_bytes(const TcTables& t, uint32_t nq, uint32_t k, MetricType metric, const FvScanOptions& opt);
 
 // IVF-PQ / IVF-SQ8 search (ivf.cu)
 struct IvfLaunch {
@@ -152,6 +155,9 @@ struct IvfLaunch {
 };
 enum { IVF_MODE_PQ = 0, IVF_MODE_SQ8 = 1, IVF_MODE_RABITQ = 2 };
 int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream);
+// The scratch bytes launch_ivf_search takes from the stream's arena for the
+// same arguments (0 when the call launches nothing or is refused).
+size_t ivf_search_scratch_bytes(int mode, const IvfLaunch& L);
 int launch_relayout_codes(const uint8_t* by_id, const uint32_t* vec_ids, uint32_t n, uint32_t row_bytes,
                           uint8_t* by_list, cudaStream_t stream);
 

@@ -49,6 +49,7 @@ class Server;
 namespace {
 
 constexpr uint32_t kMaxTopK = 256;  // reference clamp (streams.rs:14)
+constexpr size_t kDefaultScratchBudget = (size_t)512 << 20;  // FvServeConfig.scratch_budget_kb = 0
 
 uint64_t now_ns() {
   return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
@@ -120,6 +121,8 @@ struct Slot {
   std::vector<Req*> reqs;
   uint32_t kstride = 0;
   bool pinned_index = false;
+  // this batch's part of the server's scratch pool (index-backed servers)
+  size_t scratch_off = 0, scratch_bytes = 0;
   // executor-backed servers: a worker thread per slot
   std::vector<float> x_q;
   std::vector<FvRequest> x_reqs;
@@ -140,10 +143,19 @@ class Server {
     if (cfg_.max_batch == 0) cfg_.max_batch = 256;
     if (cfg_.inflight == 0) cfg_.inflight = 4;
     max_wait_ns_ = (uint64_t)cfg_.max_wait_us * 1000ull;
+    pool_bytes_ = cfg_.scratch_budget_kb ? (size_t)cfg_.scratch_budget_kb * 1024 : kDefaultScratchBudget;
+    pool_bytes_ = pool_bytes_ / 256 * 256;
   }
 
   int init() {
     const Layout lay(cfg_.max_batch, dim_);
+    if (index_) {
+      // the scratch pool every batch in flight takes its part of
+      if (pool_bytes_ < 256) return FV_ERR_ARG;
+      cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&pool_), pool_bytes_);
+      if (e != cudaSuccess) return (int)e;
+      pool_free_[0] = pool_bytes_;
+    }
     const size_t out_n = (size_t)cfg_.max_batch * kMaxTopK;
     slots_.resize(cfg_.inflight);
     for (uint32_t i = 0; i < cfg_.inflight; ++i) {
@@ -207,6 +219,36 @@ class Server {
       if (s->d_in) cudaFree(s->d_in);
       if (s->d_out) cudaFree(s->d_out);
     }
+    if (pool_) cudaFree(pool_);
+  }
+
+  // The scratch bytes one batch of `nq` requests takes: the plan of the
+  // launches index_launch_batch makes (rounded as the stream arena rounds).
+  size_t batch_scratch(uint32_t engine, uint32_t nq, uint32_t kmax, uint32_t npmax, uint32_t rrmax) const {
+    static const uint32_t kPresent = 0;  // marks the per-query arrays as present; never read
+    BatchLaunch b;
+    b.engine = engine;
+    b.nq = nq;
+    b.top_k = kmax;
+    b.nprobe = npmax;
+    b.rerank_k = rrmax;
+    if (is_ivf(engine)) b.d_topk = b.d_nprobe = b.d_rerank = &kPresent;
+    const size_t need = index_batch_scratch_bytes(index_, b);
+    return (std::max<size_t>(need, 256) + 255) / 256 * 256;
+  }
+
+  int scratch_estimate(const FvRequest* rq, uint32_t nq, uint64_t* out) {
+    if (!rq || !out) return FV_ERR_NULL;
+    if (!index_) {
+      *out = 0;
+      return 0;
+    }
+    if (rq->engine > FV_ENGINE_IVF_RABITQ || rq->top_k == 0 || rq->top_k > (uint32_t)kMaxTopK || nq == 0)
+      return FV_ERR_ARG;
+    index_pin(index_);
+    *out = batch_scratch(rq->engine, nq, rq->top_k, rq->nprobe, rq->rerank_k);
+    index_unpin(index_);
+    return 0;
   }
 
   // ------------------------------------------------------------ filters
@@ -342,6 +384,10 @@ class Server {
         *mean = sum / (double)n;
       }
     };
+    s->scratch_waits = scratch_waits_;
+    s->scratch_split = scratch_split_;
+    s->scratch_peak_bytes = pool_peak_;
+    s->scratch_pool_bytes = index_ ? pool_bytes_ : 0;
     pct(lat_us_, &s->p50_us, &s->p90_us, &s->p99_us, &s->p999_us, &s->max_us, &s->mean_us);
     pct(queue_us_, &s->queue_p50_us, nullptr, &s->queue_p99_us, nullptr, nullptr, nullptr);
   }
@@ -350,6 +396,8 @@ class Server {
     std::lock_guard<std::mutex> g(mu_);
     total_requests_ = total_batches_ = completed_ = failed_ = 0;
     max_inflight_ = 0;
+    scratch_waits_ = scratch_split_ = 0;
+    pool_peak_ = pool_used_;
     first_arrival_ = UINT64_MAX;
     last_done_ = 0;
     lat_us_.clear();
@@ -367,6 +415,50 @@ class Server {
     if (cfg_.group_by_params) return ClassKey{p.engine, p.top_k, p.nprobe, p.rerank_k};
     if (is_ivf(p.engine)) return ClassKey{p.engine, 0, 0, 0};
     return ClassKey{p.engine, p.top_k, 0, 0};
+  }
+
+  // First-fit allocator over the scratch pool (offsets and sizes in
+  // multiples of 256 bytes); called with mu_ held. SIZE_MAX: no room.
+  size_t pool_alloc(size_t bytes) {
+    for (auto it = pool_free_.begin(); it != pool_free_.end(); ++it) {
+      if (it->second < bytes) continue;
+      const size_t off = it->first, left = it->second - bytes;
+      pool_free_.erase(it);
+      if (left) pool_free_[off + bytes] = left;
+      pool_used_ += bytes;
+      pool_peak_ = std::max(pool_peak_, pool_used_);
+      return off;
+    }
+    return SIZE_MAX;
+  }
+
+  void pool_release(size_t off, size_t bytes) {
+    pool_used_ -= bytes;
+    auto it = pool_free_.emplace(off, bytes).first;
+    auto next = std::next(it);
+    if (next != pool_free_.end() && it->first + it->second == next->first) {
+      it->second += next->second;
+      pool_free_.erase(next);
+    }
+    if (it != pool_free_.begin()) {
+      auto prev = std::prev(it);
+      if (prev->first + prev->second == it->first) {
+        prev->second += it->second;
+        pool_free_.erase(it);
+      }
+    }
+  }
+
+  // Fails the oldest request of a class without launching it; mu_ held.
+  void reject_front(std::deque<Req*>* q, int rc) {
+    Req* r = q->front();
+    q->pop_front();
+    --pending_;
+    r->status = rc;
+    r->done = now_ns();
+    r->finished = true;
+    ++failed_;
+    req_cv_.notify_all();
   }
 
   void batcher_loop() {
@@ -406,10 +498,49 @@ class Server {
         work_cv_.wait_until(lk, at_ns(due));
         continue;
       }
+      size_t n = std::min<size_t>(pick->size(), cfg_.max_batch);
+      size_t off = 0, need = 0;
+      if (index_) {
+        // admission by scratch memory: the batch's exact scratch must fit
+        // in the free part of the pool; a batch larger than the whole pool
+        // is cut down; a single request larger than it fails
+        index_pin(index_);  // the estimate and the launch see one index state
+        auto estimate = [&](size_t cnt) {
+          uint32_t kmax = 0, npmax = 0, rrmax = 0;
+          for (size_t i = 0; i < cnt; ++i) {
+            const FvRequest& p = (*pick)[i]->p;
+            kmax = std::max(kmax, p.top_k);
+            npmax = std::max(npmax, p.nprobe);
+            rrmax = std::max(rrmax, p.rerank_k);
+          }
+          return batch_scratch(key.engine, (uint32_t)cnt, kmax, npmax, rrmax);
+        };
+        need = estimate(n);
+        const size_t asked = n;
+        while (need > pool_bytes_ && n > 1) {
+          n = (n + 1) / 2;
+          need = estimate(n);
+        }
+        if (n < asked) ++scratch_split_;
+        if (need > pool_bytes_) {
+          index_unpin(index_);
+          reject_front(pick, FV_ERR_SCRATCH_LIMIT);
+          continue;
+        }
+        off = pool_alloc(need);
+        if (off == SIZE_MAX) {
+          index_unpin(index_);
+          ++scratch_waits_;
+          work_cv_.wait(lk);  // a finishing batch returns its part of the pool
+          continue;
+        }
+      }
       const int si = free_slots_.back();
       free_slots_.pop_back();
       Slot* s = slots_[si].get();
-      const size_t n = std::min<size_t>(pick->size(), cfg_.max_batch);
+      s->scratch_off = off;
+      s->scratch_bytes = need;
+      s->pinned_index = index_ != nullptr;
       s->reqs.assign(pick->begin(), pick->begin() + n);
       pick->erase(pick->begin(), pick->begin() + n);
       pending_ -= n;
@@ -484,9 +615,10 @@ class Server {
     b.d_out = s->d_out;
     b.d_main = s->d_main;
     b.d_delta = s->d_delta;
-    index_pin(index_);
-    s->pinned_index = true;
-    int rc = (int)cudaMemcpyAsync(s->d_in, s->h_in, lay.total, cudaMemcpyHostToDevice, s->stream);
+    // the batch's part of the pool is the stream's scratch arena for its
+    // launches (the batch before it on this stream has completed)
+    int rc = fv_set_stream_scratch(s->stream, pool_ + s->scratch_off, s->scratch_bytes);
+    if (!rc) rc = (int)cudaMemcpyAsync(s->d_in, s->h_in, lay.total, cudaMemcpyHostToDevice, s->stream);
     if (!rc) rc = index_launch_batch(index_, b, s->stream);
     if (!rc)
       rc = (int)cudaMemcpyAsync(s->h_out, s->d_out, (size_t)nq * kmax * sizeof(GpuSearchResult),
@@ -559,6 +691,10 @@ class Server {
         }
       }
       s->reqs.clear();
+      if (s->scratch_bytes) {
+        pool_release(s->scratch_off, s->scratch_bytes);
+        s->scratch_bytes = 0;
+      }
       free_slots_.push_back(s->idx);
       --inflight_;
     }
@@ -585,6 +721,11 @@ class Server {
   uint32_t inflight_ = 0;
   std::vector<std::unique_ptr<Slot>> slots_;
   std::vector<int> free_slots_;
+  // scratch pool (index-backed servers): free ranges by offset
+  uint8_t* pool_ = nullptr;
+  size_t pool_bytes_ = 0, pool_used_ = 0, pool_peak_ = 0;
+  std::map<size_t, size_t> pool_free_;
+  uint64_t scratch_waits_ = 0, scratch_split_ = 0;
 
   uint64_t total_requests_ = 0, total_batches_ = 0, completed_ = 0, failed_ = 0;
   uint32_t max_inflight_ = 0;
@@ -672,6 +813,11 @@ int fv_serve_replay(FvServe* server, const FvRequest* requests, const float* que
                     uint32_t num_requests, GpuSearchResult* out, uint32_t out_stride, int32_t* out_status) {
   if (!server) return FV_ERR_NULL;
   return server->impl->replay(requests, queries, arrival_ns, num_requests, out, out_stride, out_status);
+}
+
+int fv_serve_scratch_estimate(FvServe* server, const FvRequest* request, uint32_t nq, uint64_t* out_bytes) {
+  if (!server) return FV_ERR_NULL;
+  return server->impl->scratch_estimate(request, nq, out_bytes);
 }
 
 int fv_serve_stats(FvServe* server, FvServeStats* out) {

@@ -398,9 +398,22 @@ uint32_t fill_waves(uint32_t s_min, uint32_t nqb, uint32_t ntiles, uint32_t sms,
 
 }  // namespace
 
-int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
-                   const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream,
-                   const QueryFilter* filters) {
+// Every launch parameter of one tensor-core scan call and the scratch it
+// takes, computed once: launch_tc_scan launches from it and the serving
+// loop admits a batch by its scratch_bytes (tc_scan_scratch_bytes).
+struct TcPlan {
+  bool fp8 = false, pair = false, prepass = false;
+  uint32_t elem = 0, kblocks = 0, shortlist = 0, kl = 0, kl_tmpl = 0;
+  int groups = 1;
+  uint32_t nqb = 0, nqb_grid = 0, splits = 0, tps = 0;
+  uint32_t pstride = 0, pr = 0, pkl_tmpl = 0, psplits = 0, ptps = 0;
+  uint32_t nq_rows = 0, slot_stride = 0;
+  size_t q_bytes = 0, qn_bytes = 0, part_bytes = 0, slot_bytes = 0, ppart_bytes = 0, tau_bytes = 0;
+  size_t scratch_bytes = 0;
+};
+
+TcPlan plan_tc_scan(const TcTables& t, uint32_t nq, uint32_t k, MetricType metric, const FvScanOptions& opt) {
+  TcPlan P{};
   const bool fp8 = t.fp8;
   const uint32_t elem = fp8 ? 1 : 2;
   const uint32_t kb_elems = fp8 ? 128 : 64;
@@ -480,8 +493,55 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   const size_t slot_bytes = align_up((size_t)nq * slot_stride * 4, 256);
   const size_t ppart_bytes = prepass ? align_up((size_t)nq * psplits * groups * pr * 8, 256) : 0;
   const size_t tau_bytes = prepass ? 2 * qn_bytes : 0;
-  uint8_t* scratch = static_cast<uint8_t*>(
-      scratch_get(stream, q_bytes + 2 * qn_bytes + part_bytes + slot_bytes + ppart_bytes + tau_bytes));
+  P.fp8 = fp8;
+  P.elem = elem;
+  P.kblocks = kblocks;
+  P.shortlist = shortlist;
+  P.groups = groups;
+  P.kl = kl;
+  P.kl_tmpl = kl_tmpl;
+  P.nqb = nqb;
+  P.pair = pair;
+  P.nqb_grid = nqb_grid;
+  P.splits = splits;
+  P.tps = tps;
+  P.prepass = prepass;
+  P.pstride = pstride;
+  P.pr = pr;
+  P.pkl_tmpl = pkl_tmpl;
+  P.psplits = psplits;
+  P.ptps = ptps;
+  P.nq_rows = nq_rows;
+  P.q_bytes = q_bytes;
+  P.qn_bytes = qn_bytes;
+  P.part_bytes = part_bytes;
+  P.slot_stride = slot_stride;
+  P.slot_bytes = slot_bytes;
+  P.ppart_bytes = ppart_bytes;
+  P.tau_bytes = tau_bytes;
+  P.scratch_bytes = q_bytes + 2 * qn_bytes + part_bytes + slot_bytes + ppart_bytes + tau_bytes;
+  return P;
+}
+
+size_t tc_scan_scratch_bytes(const TcTables& t, uint32_t nq, uint32_t k, MetricType metric,
+                             const FvScanOptions& opt) {
+  return plan_tc_scan(t, nq, k, metric, opt).scratch_bytes;
+}
+
+int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
+                   const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream,
+                   const QueryFilter* filters) {
+  const TcPlan P = plan_tc_scan(t, nq, k, metric, opt);
+  const bool fp8 = P.fp8;
+  const uint32_t elem = P.elem, kblocks = P.kblocks, shortlist = P.shortlist, kl = P.kl, kl_tmpl = P.kl_tmpl;
+  const int groups = P.groups;
+  const uint32_t nqb = P.nqb, nqb_grid = P.nqb_grid, splits = P.splits, tps = P.tps;
+  const bool pair = P.pair, prepass = P.prepass;
+  const uint32_t pstride = P.pstride, pr = P.pr, pkl_tmpl = P.pkl_tmpl, psplits = P.psplits, ptps = P.ptps;
+  const uint32_t nq_rows = P.nq_rows, slot_stride = P.slot_stride;
+  const size_t q_bytes = P.q_bytes, qn_bytes = P.qn_bytes, part_bytes = P.part_bytes, slot_bytes = P.slot_bytes;
+  const size_t ppart_bytes = P.ppart_bytes;
+  uint8_t* scratch = static_cast<uint8_t*>(scratch_get(stream, P.scratch_bytes));
   if (!scratch) return (int)cudaErrorMemoryAllocation;
   void* qprep = scratch;
   float* qnorm = reinterpret_cast<float*>(scratch + q_bytes);

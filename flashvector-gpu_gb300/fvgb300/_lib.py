@@ -82,7 +82,7 @@ class FvIndexInfo(C.Structure):
 
 class FvServeConfig(C.Structure):
     _fields_ = [("max_batch", U32), ("max_wait_us", U32), ("inflight", U32), ("group_by_params", U32),
-                ("queue_capacity", U32), ("reserved", U32 * 3)]
+                ("queue_capacity", U32), ("scratch_budget_kb", U32), ("reserved", U32 * 2)]
 
 
 class FvRequest(C.Structure):
@@ -95,7 +95,8 @@ class FvServeStats(C.Structure):
                 ("completed", C.c_uint64), ("failed", C.c_uint64)] + \
                [(n, C.c_double) for n in ("qps", "p50_us", "p90_us", "p99_us", "p999_us", "max_us", "mean_us",
                                           "queue_p50_us", "queue_p99_us")] + \
-               [("max_inflight", U32), ("reserved", U32)]
+               [("max_inflight", U32), ("reserved", U32), ("scratch_waits", C.c_uint64),
+                ("scratch_split", C.c_uint64), ("scratch_peak_bytes", C.c_uint64), ("scratch_pool_bytes", C.c_uint64)]
 
 
 # int (*)(void* user, const FvRequest*, const float* queries, uint32_t nq, uint32_t dim, uint32_t k_stride,
@@ -185,6 +186,7 @@ SIGNATURES = {
     "fv_serve_submit": (I32, [P, P, P, P]),
     "fv_serve_wait": (I32, [P, C.c_uint64, P, U32, U32, P]),
     "fv_serve_replay": (I32, [P, P, P, P, U32, P, U32, P]),
+    "fv_serve_scratch_estimate": (I32, [P, P, U32, P]),
     "fv_serve_stats": (I32, [P, P]),
     "fv_serve_reset_stats": (I32, [P]),
 }

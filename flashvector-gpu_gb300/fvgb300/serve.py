@@ -49,9 +49,9 @@ class BatcherStats:
     avg_batch_size: float
 
 
-def _config(max_wait_us, max_batch_size, inflight, group_by_params, queue_capacity):
+def _config(max_wait_us, max_batch_size, inflight, group_by_params, queue_capacity, scratch_budget_kb=0):
     return _lib.FvServeConfig(max_batch_size, max_wait_us, inflight, 1 if group_by_params else 0, queue_capacity,
-                              (_lib.U32 * 3)())
+                              scratch_budget_kb, (_lib.U32 * 2)())
 
 
 class SearchBatcher:
@@ -62,10 +62,13 @@ class SearchBatcher:
 
     @classmethod
     def for_index(cls, index, max_wait_us: int = 350, max_batch_size: int = 64, inflight: int = 4,
-                  group_by_params: bool = False, queue_capacity: int = 0) -> "SearchBatcher":
-        """batcher.rs:89-125 (defaults: 350 us window, 64 requests)."""
+                  group_by_params: bool = False, queue_capacity: int = 0,
+                  scratch_budget_kb: int = 0) -> "SearchBatcher":
+        """batcher.rs:89-125 (defaults: 350 us window, 64 requests). Batches
+        are admitted by scratch memory: together those in flight hold at most
+        scratch_budget_kb KiB (0: 512 MiB) of device scratch."""
         h = C.c_void_p()
-        cfg = _config(max_wait_us, max_batch_size, inflight, group_by_params, queue_capacity)
+        cfg = _config(max_wait_us, max_batch_size, inflight, group_by_params, queue_capacity, scratch_budget_kb)
         call("fv_serve_create", index._h, C.byref(cfg), C.byref(h))
         return cls(h, index.config.dim, keepalive=index)
 
@@ -178,6 +181,14 @@ class SearchBatcher:
 
     def reset_stats(self) -> None:
         call("fv_serve_reset_stats", self._h)
+
+    def scratch_estimate(self, key: BatchKey, num_queries: int) -> int:
+        """Scratch bytes one batch of `num_queries` requests like `key` takes
+        (what admission charges against the budget)."""
+        out = C.c_uint64(0)
+        req = key.request()
+        call("fv_serve_scratch_estimate", self._h, C.byref(req), num_queries, C.byref(out))
+        return out.value
 
 
 __all__ = ["ALGORITHM", "BatchKey", "BatcherStats", "FvError", "SearchBatcher"]

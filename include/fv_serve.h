@@ -25,6 +25,15 @@
  *   - Completion is signalled from the stream (a host function), so no
  *     thread blocks on a stream; latency is measured from arrival (submit,
  *     or the scheduled time of a replayed trace) to completion.
+ *   - Admission by scratch memory (the reference gives each stream a fixed
+ *     scratch budget, crates/engine/src/streams.rs:43-69): the server owns
+ *     one device pool of scratch_budget_kb; a batch is launched only when
+ *     its scratch (the exact size its launches take, computed from the same
+ *     plan the kernels use) fits in the free part of the pool, else it waits
+ *     for batches in flight to finish. A batch whose scratch exceeds the
+ *     whole pool is cut into smaller batches; a single request that still
+ *     exceeds it fails with FV_ERR_SCRATCH_LIMIT. Device memory therefore
+ *     never grows with the load.
  *
  * The index must outlive the server; build / add / delete on the index
  * wait for the batches in flight.
@@ -47,7 +56,9 @@ typedef struct {
     uint32_t group_by_params; /* 1: batch only equal (engine, top_k, nprobe, rerank_k)       */
     uint32_t queue_capacity;  /* pending requests admitted (0: unbounded); beyond it submit
                                  returns FV_ERR_QUEUE_FULL                                  */
-    uint32_t reserved[3];
+    uint32_t scratch_budget_kb; /* device scratch of all batches in flight together, KiB (0:
+                                   512 MiB); one pool of this size is allocated at create  */
+    uint32_t reserved[2];
 } FvServeConfig;
 
 typedef struct {
@@ -72,6 +83,11 @@ typedef struct {
     double queue_p50_us, queue_p99_us;                         /* arrival -> launch     */
     uint32_t max_inflight;
     uint32_t reserved;
+    /* admission by scratch memory */
+    uint64_t scratch_waits;       /* times a ready batch waited for scratch to free up      */
+    uint64_t scratch_split;       /* batches cut smaller to fit the budget                  */
+    uint64_t scratch_peak_bytes;  /* most scratch held by the batches in flight at once     */
+    uint64_t scratch_pool_bytes;  /* the budget (pool size)                                 */
 } FvServeStats;
 
 /* A batch executor for a server without an index (host-only use and
@@ -112,6 +128,10 @@ int fv_serve_wait(FvServe* server, uint64_t ticket, GpuSearchResult* out, uint32
  * (out_stride >= every top_k), out_status[i] (optional) its status. */
 int fv_serve_replay(FvServe* server, const FvRequest* requests, const float* queries, const uint64_t* arrival_ns,
                     uint32_t num_requests, GpuSearchResult* out, uint32_t out_stride, int32_t* out_status);
+
+/* The scratch bytes one launched batch of `nq` requests like `request`
+ * takes (what admission charges against scratch_budget_kb). */
+int fv_serve_scratch_estimate(FvServe* server, const FvRequest* request, uint32_t nq, uint64_t* out_bytes);
 
 int fv_serve_stats(FvServe* server, FvServeStats* out);
 int fv_serve_reset_stats(FvServe* server);

@@ -120,3 +120,51 @@ def test_serving_survives_index_updates(served):
         assert after[0] == new_id and before[0] != new_id
         idx.delete_ids([new_id])
         assert b.search(key, marker[0])[0][0] != new_id
+
+
+def _burst(b, key, q):
+    return b.replay([key] * q.shape[0], q, np.zeros(q.shape[0], dtype=np.uint64))
+
+
+def test_batches_admitted_by_scratch_memory(served):
+    """A budget that holds one full batch's scratch (plus a little): a burst
+    of batches is held back until scratch frees up instead of growing device
+    memory; the scratch held in flight never exceeds the budget; the answers
+    are still those of the blocking search. A budget below one full batch
+    cuts batches smaller; a budget below one request fails the requests with
+    FV_ERR_SCRATCH_LIMIT."""
+    from fvgb300.serve import BatchKey, SearchBatcher
+
+    idx, rows = served
+    key = BatchKey("fp16", 100)
+    with SearchBatcher.for_index(idx, max_wait_us=0, max_batch_size=64, inflight=4) as probe:
+        full, single = probe.scratch_estimate(key, 64), probe.scratch_estimate(key, 1)
+    assert full > 4 * single > 0
+    q = gen_clustered(320, 64, 24, 31)
+
+    budget_kb = (full * 3 // 2 + 1023) // 1024
+    with SearchBatcher.for_index(idx, max_wait_us=0, max_batch_size=64, inflight=4,
+                                 scratch_budget_kb=budget_kb) as b:
+        ids, dist, status = _burst(b, key, q)
+        s = b.serve_stats()
+    assert np.all(status == 0) and s["completed"] == q.shape[0]
+    assert s["scratch_pool_bytes"] == budget_kb * 1024
+    assert full <= s["scratch_peak_bytes"] <= s["scratch_pool_bytes"]
+    assert s["scratch_waits"] > 0 and s["max_inflight"] <= 2
+    for i in range(0, q.shape[0], 23):
+        a_ids, a_dist = alone(idx, key, q[i], None)
+        assert np.array_equal(ids[i], a_ids[0]) and np.array_equal(dist[i], a_dist[0]), i
+
+    small_kb = (full // 2 + 1023) // 1024
+    with SearchBatcher.for_index(idx, max_wait_us=0, max_batch_size=64, inflight=4,
+                                 scratch_budget_kb=small_kb) as b:
+        ids2, dist2, status2 = _burst(b, key, q)
+        s2 = b.serve_stats()
+    assert np.all(status2 == 0) and s2["scratch_split"] > 0
+    assert s2["scratch_peak_bytes"] <= s2["scratch_pool_bytes"]
+    assert np.array_equal(ids2, ids) and np.array_equal(dist2, dist)
+
+    with SearchBatcher.for_index(idx, max_wait_us=0, max_batch_size=64, inflight=4, scratch_budget_kb=1) as b:
+        _, _, status3 = _burst(b, key, q[:8])
+        s3 = b.serve_stats()
+    assert np.all(status3 == -6) and s3["failed"] == 8 and s3["scratch_peak_bytes"] == 0
