@@ -21,6 +21,7 @@
 //    to scratch and a second kernel merges them.
 #include <mutex>
 
+#include "../../include/fv_bridge.h"
 #include "common.cuh"
 #include "kernels.h"
 #include "topk.cuh"
@@ -438,6 +439,9 @@ int launch_flat_f32_planned(const FlatPlan& p, const float* vectors, const uint3
 // address handed to the kernels is looked up once per device with
 // cudaGetSymbolAddress (with that device current) on the first call made
 // on the device; make that first call before any stream capture begins.
+// The looked-up address is kept for the life of the process: after a
+// cudaDeviceReset the array may sit elsewhere in the new context, so a
+// process that resets a device must not call this entry point on it again.
 // All calls share the one array and it keeps whatever the last call wrote;
 // the scan writes every slot it later reads, so nothing needs clearing, but
 // calls whose work overlaps on the GPU (different streams, or host threads
@@ -474,51 +478,15 @@ cudaError_t noalloc_scratch_address(uint64_t** out) {
 int launch_flat_f32_noalloc(const float* vectors, const uint32_t* vec_ids, uint32_t n, uint32_t dim,
                             const float* queries, uint32_t nq, uint32_t k, MetricType metric, const uint32_t* mask,
                             GpuSearchResult* out, cudaStream_t stream) {
-  const uint32_t nqb = (nq + QT - 1) / QT;
-  const uint32_t ntiles = (n + VT - 1) / VT;
-  int sms = device_sm_count();
-  uint32_t splits = (uint32_t)((2 * sms + nqb - 1) / nqb);
-  const uint32_t pow2k = next_pow2(k);
-  splits = std::max(1u, std::min(splits, std::min(ntiles, 8192u / pow2k)));
-  uint32_t tps = (ntiles + splits - 1) / splits;
-  splits = (ntiles + tps - 1) / tps;
-
-  FlatArgs a{vectors, vec_ids, n, dim, queries, nq, k, mask, out, nullptr, splits, tps};
-  if (splits > 1) {
-    const size_t need = (size_t)nq * splits * k * 8;
-    if (need > kNoAllocScratchBytes) return -6;  // FV_ERR_SCRATCH_LIMIT
-    uint64_t* p = nullptr;
-    cudaError_t e = noalloc_scratch_address(&p);
+  const FlatPlan p = plan_flat_f32(n, nq, k, 0);
+  if (p.scratch_bytes > kNoAllocScratchBytes) return FV_ERR_SCRATCH_LIMIT;
+  uint64_t* heaps = nullptr;
+  if (p.scratch_bytes) {
+    cudaError_t e = noalloc_scratch_address(&heaps);
     if (e != cudaSuccess) return (int)e;
-    a.partial = p;
   }
-  const size_t smem = flat_f32_smem_bytes(k);
-  const bool vec4 = (dim % 4 == 0) && ((uintptr_t)vectors % 16 == 0) && ((uintptr_t)queries % 16 == 0);
-  dim3 grid(nqb, splits);
-  auto go = [&](auto kern) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<grid, NT, smem, stream>>>(a);
-  };
-  switch (metric) {
-    case METRIC_INNER_PRODUCT:
-      vec4 ? go(flat_f32_scan_kernel<METRIC_INNER_PRODUCT, true>) : go(flat_f32_scan_kernel<METRIC_INNER_PRODUCT, false>);
-      break;
-    case METRIC_COSINE:
-      vec4 ? go(flat_f32_scan_kernel<METRIC_COSINE, true>) : go(flat_f32_scan_kernel<METRIC_COSINE, false>);
-      break;
-    default:
-      vec4 ? go(flat_f32_scan_kernel<METRIC_L2, true>) : go(flat_f32_scan_kernel<METRIC_L2, false>);
-      break;
-  }
-  note_launch();
-  if (splits > 1) {
-    const uint32_t pow2 = next_pow2(splits * k);
-    const size_t msmem = (size_t)pow2 * 8;
-    cudaFuncSetAttribute(merge_partial_topk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msmem);
-    merge_partial_topk_kernel<<<nq, 256, msmem, stream>>>(a.partial, splits, k, pow2, vec_ids, out, k);
-    note_launch();
-  }
-  return (int)cudaGetLastError();
+  return launch_flat_f32_planned(p, vectors, vec_ids, n, dim, queries, nq, k, metric, mask, out, false, heaps,
+                                 stream);
 }
 
 }  // namespace fv

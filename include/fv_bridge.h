@@ -80,8 +80,10 @@ int cuda_flat_scan_batch(const float* d_vectors, const uint32_t* d_vec_ids,
  * outputs. A call whose heaps (num_queries x splits x top_k x 8 bytes)
  * would exceed the array is refused with FV_ERR_SCRATCH_LIMIT and
  * launches nothing. The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) and caches it: make that first call
- * before any stream capture. All calls share the array, which keeps the
+ * address (cudaGetSymbolAddress) and caches it for the life of the process:
+ * make that first call before any stream capture, and do not call this
+ * entry point again on a device after cudaDeviceReset (the new context may
+ * place the array elsewhere). All calls share the array, which keeps the
  * last call's contents; calls whose GPU work overlaps (other streams, other
  * host threads on the same device) race on it and must be serialised. */
 int fv_flat_scan_batch_noalloc(const float* d_vectors, const uint32_t* d_vec_ids,

@@ -66,3 +66,26 @@ def test_noalloc_refuses_work_beyond_the_array(cuda):
     torch.cuda.synchronize()
     assert rc == -6  # FV_ERR_SCRATCH_LIMIT
     assert torch.all(out == -7)  # outputs untouched
+
+
+def test_noalloc_at_the_array_limit(cuda):
+    """k = 256 over 20,000 rows: the scan splits the base into 32 ranges
+    (the merge sorts at most 8,192 keys per query, 8,192 / 256 = 32), so 128
+    queries need 128 x 32 x 256 x 8 bytes = exactly the 8 MiB array -- run,
+    bit-identical to cuda_flat_scan_batch, twice, for L2 and cosine -- and
+    129 queries need more -- refused, nothing written."""
+    torch = cuda
+    g = torch.Generator(device="cuda").manual_seed(11)
+    base = torch.randn((20000, 48), generator=g, device="cuda")
+    for metric in (0, 1):
+        for rep in range(2):
+            queries = torch.randn((128, 48), generator=g, device="cuda")
+            rc_ref, ref = _call("cuda_flat_scan_batch", base, queries, 256, metric)
+            rc, got = _call("fv_flat_scan_batch_noalloc", base, queries, 256, metric)
+            torch.cuda.synchronize()
+            assert rc_ref == 0 and rc == 0, (metric, rep, rc)
+            assert torch.equal(ref, got), (metric, rep)
+    queries = torch.randn((129, 48), generator=g, device="cuda")
+    rc, out = _call("fv_flat_scan_batch_noalloc", base, queries, 256, 0)
+    torch.cuda.synchronize()
+    assert rc == -6 and torch.all(out == -7)
