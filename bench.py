@@ -10,9 +10,21 @@ Synthetic data of that shape stands in for the benchmark corpus.
 
 A step is one call of the drop-in entry point cuda_fp16_tc_search_batch over
 one batch. `value` times K steps with the queries already in HBM (CUDA
-events on the call's stream); `e2e` times K steps that each copy the batch
-from pinned host memory, search, and copy the results back. The base set
-(1.54 GB fp16 + 3.07 GB fp32) is far larger than L2, so no flush is needed.
+events on the call's stream), the steady state replayed from CUDA graphs
+captured from that call (one graph per query buffer; --no-graph times the
+eager calls); the per-kernel split and the roofline's kernel time come from
+a second pass of the same K steps with the library's per-kernel event hook,
+so the hook never runs inside the timed region. `e2e` times K steps that
+each copy the batch from pinned host memory, search, and copy the results
+back; `p50_ms` / `p99_ms` time such batches one by one, each waited for.
+The base set (1.54 GB fp16 + 3.07 GB fp32) is far larger than L2, so no
+flush is needed.
+
+`fp8_c2` (same line) measures the fp8 configuration: 10,000,000 x 96 rows
+(16,384 components, N(0,1) means, sigma 0.5), 10,000-query batches, k = 100,
+fp8 e4m3 scan + fp32 rescore + fp64 boundary, against the project's exact
+fp32 scan on the same rows and queries, with recall@10 against fp64 and the
+scan's tensor roofline (both fp8 layouts: table scale, per-vector scales).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -62,6 +74,11 @@ def parse_args():
     ap.add_argument("--nprobe", type=str, default="8,32,128", help="ivf_pq / ivf_rabitq: comma-separated nprobe sweep")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-graph", action="store_true", help="fp16_ip: time eager calls instead of CUDA graphs")
+    ap.add_argument("--no-fp8-block", action="store_true",
+                    help="fp16_ip: leave out the 10M x 96 fp8 block of the default line")
+    ap.add_argument("--fp8-steps", type=int, default=5, help="fp16_ip: timed steps of the fp8 block")
+    ap.add_argument("--latency-steps", type=int, default=200, help="fp16_ip: batches timed one by one for p50/p99")
     a = ap.parse_args()
     defaults = {"fp16_ip": (1_000_000, 768, 1024, 10), "fp8_l2": (10_000_000, 96, 10_000, 100),
                 "ivf_pq": (10_000_000, 128, 10_000, 10), "ivf_rabitq": (10_000_000, 128, 10_000, 10),
@@ -259,7 +276,10 @@ def run_ours(a, world, rank, local):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=dev)
-    stream = torch.cuda.current_stream()
+    # a created stream (the legacy default stream cannot be captured)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    graph_note = "steady state replayed from CUDA graphs captured from cuda_fp16_tc_search_batch (one per buffer)"
 
     mix = dataclasses.replace(datasets.FP16_IP_UNIT, dim=a.dim)
     base = datasets.sample_torch(mix, a.n, seed=1, stream=0, device=dev)
@@ -286,28 +306,48 @@ def run_ours(a, world, rank, local):
 
             dist.barrier()
 
-    # ---- device-resident timed region
+    # ---- steady state as CUDA graphs: one graph per query buffer, each
+    # captured from the drop-in call (the arena is already grown by the warm-up)
+    graphs = None
+    if not a.no_graph:
+        try:
+            graphs = [scan.Graph.capture(lambda i=i: step(i), stream) for i in range(nbatches)]
+        except Exception as exc:  # capture is refused on some drivers: time the eager calls
+            graphs = None
+            graph_note = f"eager launches (capture failed: {exc})"
+    run = (lambda i: graphs[i % nbatches].launch(stream)) if graphs else step
+    for i in range(nbatches):
+        run(i)
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region (no per-kernel hook)
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
     barrier()
     torch.cuda.synchronize()
-    scan.profile_summary()
-    scan.profile_enable(True)
     l0 = scan.launch_count()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     for i in range(a.steps):
-        step(i)
+        run(i)
     ev1.record(stream)
     torch.cuda.synchronize()
     launches = scan.launch_count() - l0
-    scan.profile_enable(False)
-    prof = scan.profile_summary()
     barrier()
     clk = clocks.stop()
     dev_ms = ev0.elapsed_time(ev1)
+
+    # ---- kernel split: the same steps again with the library's per-kernel
+    # event hook (eager calls, every event on the call's stream)
+    scan.profile_summary()
+    scan.profile_enable(True)
+    for i in range(a.steps):
+        step(i)
+    torch.cuda.synchronize()
+    scan.profile_enable(False)
+    prof = scan.profile_summary()
 
     # ---- end-to-end through the C ABI with host buffers
     host_q = [b.cpu().pin_memory() for b in batches]
@@ -327,6 +367,43 @@ def run_ours(a, world, rank, local):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     barrier()
+
+    # ---- per-batch latency: each batch copied in, searched, copied out and
+    # waited for on its own (a caller that blocks on every batch)
+    lat = []
+    for i in range(max(a.latency_steps, a.steps)):
+        t1 = time.perf_counter()
+        dq.copy_(host_q[i % nbatches], non_blocking=True)
+        step(i, dq)
+        host_out.copy_(out, non_blocking=True)
+        torch.cuda.synchronize()
+        lat.append((time.perf_counter() - t1) * 1e3)
+    lat.sort()
+    p50 = lat[len(lat) // 2]
+    p99 = lat[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))]
+    latency = {"p50_ms": p50, "p99_ms": p99, "max_ms": lat[-1], "batches": len(lat),
+               "what": "per batch of the headline: H2D of the queries, cuda_fp16_tc_search_batch, D2H of the "
+                       "results, stream synchronize (wall clock)"}
+
+    # ---- the fp8 configuration: 10M x 96 e4m3 scan + rescore against the
+    # project's exact fp32 scan, 10,000-query batches, k = 100
+    fp8_block = None
+    if not a.no_fp8_block:
+        r = fp8_measure(10_000_000, 96, 10_000, 100, dev, stream, a.fp8_steps, 3, *measured_peaks(), local=local)
+        r.pop("_base")
+        r.pop("_q0")
+        fp8_s, f32_s = replica_max([r["dev_s"], 1.0 / r["fp32_exact_scan"]["value"]], world, dev)
+        fp8_block = {"metric": "QPS at recall@10>=0.99 vs FP64 exact, FP8+rescore vs the project's FP32 scan",
+                     "value": 10_000 * a.fp8_steps * world / fp8_s, "unit": UNIT,
+                     "ms_per_step": fp8_s / a.fp8_steps * 1e3, "steps": a.fp8_steps,
+                     "recall_at_10": r["recall_at_10"], "recall_at_k": r["recall_at_k"],
+                     "recall_sample": r["recall_sample"],
+                     "fp32_exact_scan_qps": world / f32_s,
+                     "speedup_over_fp32_scan": (10_000 * a.fp8_steps / fp8_s) / (1.0 / f32_s),
+                     "roofline": r["roofline"], "kernels": r["kernels"], "gpu_launches": r["gpu_launches"],
+                     "clocks": r["clocks"], "per_vector_scales": r["per_vector_scales"], "config": r["config"]}
+        del r
+        torch.cuda.empty_cache()
 
     # ---- max over ranks
     dev_s, e2e_s = replica_max([dev_ms / 1e3, e2e_s], world, dev)
@@ -373,6 +450,7 @@ def run_ours(a, world, rank, local):
             "frac": (achieved / peak) if achieved and peak else None,
             "traffic": traffic.get("bytes_per_launch") if traffic else None,
             "kernel": scan_name, "kernel_ms": scan_ms, "algorithmic_flops_per_launch": flops,
+            "kernel_ms_source": "CUDA events around each launch on the call's stream, second pass of the K steps",
             "peak_source": f"{peak_kind} dense bf16 burst (fp16 dense rate is the same)"}
     kernels = {k: {"launches": v["launches"], "ms_per_launch": v["ms"] / max(1, v["launches"])} for k, v in prof.items()}
 
@@ -387,11 +465,12 @@ def run_ours(a, world, rank, local):
 
     line = {"metric": METRIC, "value": qps, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": dev_s / a.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f16", "data": "synthetic", "config": config(a),
+            "dtype": "f16", "data": "synthetic", "config": config(a, {"steady_state": graph_note}),
             "recall_at_k": recall, "max_dist_err_vs_fp64": maxerr,
             "e2e": {"value": e2e_qps, "unit": UNIT, "h2d_bytes_per_step": a.batch * a.dim * 4,
                     "d2h_bytes_per_step": a.batch * a.k * 8, "ms_per_step": e2e_s / a.steps * 1e3},
-            "gpu_launches": launches, "roofline": roof, "kernels": kernels, "clocks": clk, "cpu_baseline": cpu}
+            "gpu_launches": launches, "roofline": roof, "kernels": kernels, "clocks": clk, "cpu_baseline": cpu,
+            "p50_ms": latency["p50_ms"], "p99_ms": latency["p99_ms"], "latency": latency, "fp8_c2": fp8_block}
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -459,6 +538,120 @@ def _line(a, world, metric_value, unit, dev_s, e2e, launches, roof, kernels, clk
 
 def _kernels(prof):
     return {k: {"launches": v["launches"], "ms_per_launch": v["ms"] / max(1, v["launches"])} for k, v in prof.items()}
+
+
+def fp8_measure(n, dim, batch, k, dev, stream, steps, warmup, peaks, peak_kind, overfetch=None, local=0,
+                e2e=False, f32_steps=2, nsub=100):
+    """The fp8 e4m3 L2 configuration: n x dim rows from 16,384 components
+    (N(0,1) means, sigma 0.5), batches of `batch` queries, top-k with fp32
+    rescore and fp64 boundary, against the project's exact fp32 scan on the
+    same data and queries. Both fp8 layouts are measured: the power-of-two
+    table scale with norm digits in the MMA (the fast one) and the per-vector
+    max|x| / 448 scales. Returns a dict of the measured numbers."""
+    import numpy as np
+    import torch
+
+    from fvgb300 import datasets, scan
+
+    mix = dataclasses.replace(datasets.FP8_L2, dim=dim)
+    base = datasets.sample_torch(mix, n, seed=2, stream=0, device=dev)
+    qpool = datasets.sample_torch(mix, batch * 2, seed=2, stream=1, device=dev)
+    qb = [qpool[:batch].contiguous(), qpool[batch:].contiguous()]
+    table = scan.Fp8Table(base)
+    out = scan.empty_results(batch, k, dev)
+    # over-fetch 0: the committed autotuner's value for this shape
+    fp8_overfetch = 0 if overfetch is None else overfetch
+    opts = scan.options(overfetch=fp8_overfetch, boundary_fp64=1)
+    tuned_knobs = scan.tune_lookup("fp8", "l2", dim, n, batch, k)
+    step = lambda i, qq=None: scan.fp8_search(table, qb[i % 2] if qq is None else qq, k, "l2",  # noqa: E731
+                                               opts=opts, out=out)
+    for i in range(max(3, warmup)):
+        step(i)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    l0 = scan.launch_count()
+    dev_s = _dev_time(step, steps, stream)
+    launches = scan.launch_count() - l0
+    clk = clocks.stop()
+    # kernel split: a separate pass with the per-kernel event hook
+    scan.profile_summary()
+    scan.profile_enable(True)
+    _dev_time(step, steps, stream)
+    scan.profile_enable(False)
+    prof = scan.profile_summary()
+    step(0)
+    torch.cuda.synchronize()
+    res = out.cpu().numpy()
+    ids = res[..., 0].view(np.uint32)
+    truth, _ = _fp64_topk(base, qb[0][:nsub], k, "l2")
+    rec10 = _recall(ids[:nsub, :10], truth[:, :10])
+    rec_k = _recall(ids[:nsub], truth)
+    # the project's exact fp32 scan on the same data and queries
+    fout = scan.empty_results(batch, min(k, 256), dev)
+    scan.flat_scan(base, qb[0], k, "l2", out=fout)
+    torch.cuda.synchronize()
+    f32_s = _dev_time(lambda i: scan.flat_scan(base, qb[i % 2], k, "l2", out=fout), f32_steps, stream)
+    f32_qps = batch * f32_steps / f32_s
+    qps = batch * steps / dev_s
+    e2e_line = None
+    if e2e:
+        hq = [b.cpu().pin_memory() for b in qb]
+        hout = torch.empty(out.shape, dtype=out.dtype).pin_memory()
+        dq = torch.empty_like(qb[0])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(steps):
+            dq.copy_(hq[i % 2], non_blocking=True)
+            step(i, dq)
+            hout.copy_(out, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        e2e_line = {"value": batch * steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": batch * dim * 4,
+                    "d2h_bytes_per_step": batch * k * 8}
+    # the same workload over the per-vector-scale layout (scales max|x| / 448,
+    # each row's scale and norm applied per value in the epilogue)
+    pv_table = scan.Fp8Table(base, per_vector=True)
+    pv_step = lambda i: scan.fp8_search(pv_table, qb[i % 2], k, "l2", opts=opts, out=out)  # noqa: E731
+    for i in range(max(3, warmup)):
+        pv_step(i)
+    torch.cuda.synchronize()
+    pv_s = _dev_time(pv_step, steps, stream)
+    scan.profile_summary()
+    scan.profile_enable(True)
+    _dev_time(pv_step, steps, stream)
+    scan.profile_enable(False)
+    pv_prof = scan.profile_summary()
+    pv_step(0)
+    torch.cuda.synchronize()
+    pids = out.cpu().numpy()[..., 0].view(np.uint32)
+    kname = "tc_scan_fp8"
+    flops = 2.0 * n * dim * batch
+    peak = 2.0 * peaks.get("bf16_tflops", 1900.0)
+    pv_kms = pv_prof[kname]["ms"] / pv_prof[kname]["launches"]
+    per_vector = {"value": batch * steps / pv_s, "unit": UNIT, "scan_ms": pv_kms,
+                  "scan_roofline_frac": flops / (pv_kms / 1e3) / 1e12 / peak,
+                  "recall_at_10": _recall(pids[:nsub, :10], truth[:, :10]), "recall_at_k": _recall(pids[:nsub], truth),
+                  "speedup_over_fp32": batch * steps / pv_s / f32_qps,
+                  "layout": "per-vector scales max|x|/448, padded_dim " + str(pv_table.pd)}
+    del pv_table
+    kms = prof[kname]["ms"] / prof[kname]["launches"]
+    roof = {"bound": "tensor", "achieved": flops / (kms / 1e3) / 1e12, "peak": peak, "unit": "TFLOP/s",
+            "frac": flops / (kms / 1e3) / 1e12 / peak, "traffic": None, "kernel": kname, "kernel_ms": kms,
+            "peak_source": f"2 x {peak_kind} dense bf16 burst (dense fp8 rate is twice the fp16 rate)"}
+    eff_overfetch = fp8_overfetch or (tuned_knobs or {}).get("overfetch") or 4
+    cfg = {"workload": "fp8 e4m3 flat L2 scan (power-of-two scales, row norms as e4m3 digits inside the MMA) + "
+                       "fp32 rescore (autotuned over-fetch) + fp64 boundary", "N": n, "dim": dim,
+           "padded_dim": table.pd, "batch": batch, "k": k, "overfetch": eff_overfetch, "autotuned": tuned_knobs,
+           "mixture": "16384 comps, N(0,1) means, sigma 0.5",
+           "l2": f"inputs larger than L2 ({n * table.pd / 1e9:.2f} GB fp8 base streamed per step)"}
+    return {"value": qps, "dev_s": dev_s, "ms_per_step": dev_s / steps * 1e3, "e2e": e2e_line,
+            "gpu_launches": launches, "roofline": roof, "kernels": _kernels(prof), "clocks": clk, "config": cfg,
+            "recall_at_10": rec10, "recall_at_k": rec_k, "recall_sample": nsub,
+            "fp32_exact_scan": {"value": f32_qps, "unit": UNIT, "steps": f32_steps,
+                                "speedup_fp8_over_fp32": qps / f32_qps},
+            "per_vector_scales": per_vector, "_base": base, "_q0": qb[0]}
 
 
 def run_workload(a, world, rank, local):
@@ -547,113 +740,26 @@ def run_workload(a, world, rank, local):
         return
 
     if a.workload == "fp8_l2":
-        mix = dataclasses.replace(datasets.FP8_L2, dim=a.dim)
-        base = datasets.sample_torch(mix, a.n, seed=2, stream=0, device=dev)
-        qpool = datasets.sample_torch(mix, a.batch * 2, seed=2, stream=1, device=dev)
-        qb = [qpool[:a.batch].contiguous(), qpool[a.batch:].contiguous()]
-        table = scan.Fp8Table(base)
-        out = scan.empty_results(a.batch, a.k, dev)
-        # over-fetch 0: the committed autotuner's value for this shape
-        fp8_overfetch = 0 if a.overfetch_fp8 is None else a.overfetch_fp8
-        opts = scan.options(overfetch=fp8_overfetch, boundary_fp64=1)
-        tuned_knobs = scan.tune_lookup("fp8", "l2", a.dim, a.n, a.batch, a.k)
-        step = lambda i, qq=None: scan.fp8_search(table, qb[i % 2] if qq is None else qq, a.k, "l2",  # noqa: E731
-                                                   opts=opts, out=out)
-        for i in range(max(3, a.warmup)):
-            step(i)
-        torch.cuda.synchronize()
-        clocks = ClockSampler(local)
-        clocks.start()
-        time.sleep(0.3)
-        scan.profile_summary()
-        scan.profile_enable(True)
-        l0 = scan.launch_count()
-        dev_s = _dev_time(step, a.steps, stream)
-        launches = scan.launch_count() - l0
-        scan.profile_enable(False)
-        prof = scan.profile_summary()
-        clk = clocks.stop()
-        step(0)
-        torch.cuda.synchronize()
-        res = out.cpu().numpy()
-        ids, dist = res[..., 0].view(np.uint32), res[..., 1].view(np.float32)
-        nsub = 100
-        truth, tdist = _fp64_topk(base, qb[0][:nsub], a.k, "l2")
-        rec10 = _recall(ids[:nsub, :10], truth[:, :10])
-        rec_k = _recall(ids[:nsub], truth)
-        # the project's exact fp32 scan on the same data and queries
-        fout = scan.empty_results(a.batch, min(a.k, 256), dev)
-        scan.flat_scan(base, qb[0], a.k, "l2", out=fout)
-        torch.cuda.synchronize()
-        f32_steps = 2
-        f32_s = _dev_time(lambda i: scan.flat_scan(base, qb[i % 2], a.k, "l2", out=fout), f32_steps, stream)
-        f32_qps = a.batch * f32_steps / f32_s
-        # end to end through the C ABI with host buffers
-        hq = [b.cpu().pin_memory() for b in qb]
-        hout = torch.empty(out.shape, dtype=out.dtype).pin_memory()
-        dq = torch.empty_like(qb[0])
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for i in range(a.steps):
-            dq.copy_(hq[i % 2], non_blocking=True)
-            step(i, dq)
-            hout.copy_(out, non_blocking=True)
-        torch.cuda.synchronize()
-        e2e_s = time.perf_counter() - t0
-        # the same workload over the per-vector-scale layout (scales max|x| / 448,
-        # each row's scale and norm applied per value in the epilogue)
-        pv_table = scan.Fp8Table(base, per_vector=True)
-        pv_step = lambda i: scan.fp8_search(pv_table, qb[i % 2], a.k, "l2", opts=opts, out=out)  # noqa: E731
-        for i in range(max(3, a.warmup)):
-            pv_step(i)
-        torch.cuda.synchronize()
-        scan.profile_summary()
-        scan.profile_enable(True)
-        pv_s = _dev_time(pv_step, a.steps, stream)
-        scan.profile_enable(False)
-        pv_prof = scan.profile_summary()
-        pv_step(0)
-        torch.cuda.synchronize()
-        pres = out.cpu().numpy()
-        pids = pres[..., 0].view(np.uint32)
-        per_vector = {"value": a.batch * a.steps / pv_s, "unit": UNIT,
-                      "scan_ms": pv_prof["tc_scan_fp8"]["ms"] / pv_prof["tc_scan_fp8"]["launches"],
-                      "recall_at_10": _recall(pids[:nsub, :10], truth[:, :10]), "recall_at_k": _recall(pids[:nsub], truth),
-                      "layout": "per-vector scales max|x|/448, padded_dim " + str(pv_table.pd)}
-        del pv_table
-        kname = "tc_scan_fp8"
-        kms = prof[kname]["ms"] / prof[kname]["launches"]
-        flops = 2.0 * a.n * a.dim * a.batch
-        peak = 2.0 * peaks.get("bf16_tflops", 1900.0)
-        qps = a.batch * a.steps / dev_s
-        roof = {"bound": "tensor", "achieved": flops / (kms / 1e3) / 1e12, "peak": peak, "unit": "TFLOP/s",
-                "frac": flops / (kms / 1e3) / 1e12 / peak, "traffic": None, "kernel": kname, "kernel_ms": kms,
-                "peak_source": f"2 x {peak_kind} dense bf16 burst (dense fp8 rate is twice the fp16 rate)"}
+        r = fp8_measure(a.n, a.dim, a.batch, a.k, dev, stream, a.steps, a.warmup, peaks, peak_kind,
+                        overfetch=a.overfetch_fp8, local=local, e2e=True)
         cpu = None
         if not a.no_cpu_baseline:
             sys.path.insert(0, str(ROOT / "oracle"))
             import oracle
 
             oracle.build()
-            bnp, qnp = base.cpu().numpy(), qb[0][:threads].cpu().numpy()
+            bnp, qnp = r.pop("_base").cpu().numpy(), r.pop("_q0")[:threads].cpu().numpy()
             t0 = time.perf_counter()
             oracle.exact_knn(bnp, qnp, a.k, "l2", threads=threads)
             cdt = time.perf_counter() - t0
             cpu = {"value": threads / cdt, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"{threads} queries, exact fp32 search of the full base, {cdt:.1f} s"}
-        eff_overfetch = fp8_overfetch or (tuned_knobs or {}).get("overfetch") or 4
-        cfg = {"workload": "fp8 e4m3 flat L2 scan (power-of-two scales, row norms as e4m3 digits inside the MMA) + "
-                           "fp32 rescore (autotuned over-fetch) + fp64 boundary", "N": a.n, "dim": a.dim,
-               "padded_dim": table.pd, "batch": a.batch, "k": a.k, "overfetch": eff_overfetch,
-               "autotuned": tuned_knobs,
-               "mixture": "16384 comps, N(0,1) means, sigma 0.5",
-               "l2": f"inputs larger than L2 ({a.n * table.pd / 1e9:.2f} GB fp8 base streamed per step)"}
-        _line(a, world, qps, UNIT, dev_s,
-              {"value": a.batch * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": a.batch * a.dim * 4,
-               "d2h_bytes_per_step": a.batch * a.k * 8}, launches, roof, _kernels(prof), clk, cpu, "e4m3", cfg,
-              recall_at_10=rec10, recall_at_k=rec_k, recall_sample=nsub,
-              fp32_exact_scan={"value": f32_qps, "unit": UNIT, "steps": f32_steps, "speedup_fp8_over_fp32": qps / f32_qps},
-              per_vector_scales=per_vector)
+        r.pop("_base", None)
+        r.pop("_q0", None)
+        _line(a, world, r["value"], UNIT, r["dev_s"], r["e2e"], r["gpu_launches"], r["roofline"], r["kernels"],
+              r["clocks"], cpu, "e4m3", r["config"], recall_at_10=r["recall_at_10"], recall_at_k=r["recall_at_k"],
+              recall_sample=r["recall_sample"], fp32_exact_scan=r["fp32_exact_scan"],
+              per_vector_scales=r["per_vector_scales"])
         return
 
     if a.workload in ("ivf_pq", "ivf_rabitq"):
