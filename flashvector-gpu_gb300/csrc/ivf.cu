@@ -73,6 +73,12 @@ struct IvfArgs {
   // mask-word load per posting
   const uint32_t* list_allow;
   uint32_t list_n;
+  // the admitted list positions in list order (compacted from list_allow),
+  // and per bit word the count of admitted positions before it: a list
+  // whose mask admits under half of its postings is scanned over these
+  // positions only (null when there is no mask)
+  const uint32_t* adm_pos;
+  const uint32_t* adm_prefix;  // [ceil(list_n / 32) + 1]
   const uint32_t* q_topk;         // per-query top_k / nprobe / rerank_k, or null (uniform)
   const uint32_t* q_nprobe;
   const uint32_t* q_rerank;
@@ -92,6 +98,29 @@ struct IvfArgs {
   uint32_t P, W;                  // rotated dimension (power of two), words of bits per row
   float inv_sqrt_p;               // 1.0f / sqrtf(P), correctly rounded
 };
+
+// Index of list position p in the compacted admitted positions (the count of
+// admitted positions before p). p <= list_n.
+__device__ __forceinline__ uint32_t adm_index(const IvfArgs& a, uint32_t p) {
+  const uint32_t w = p >> 5, b = p & 31u;
+  return __ldg(a.adm_prefix + w) + (b ? __popc(__ldg(a.list_allow + w) & ((1u << b) - 1u)) : 0u);
+}
+
+// The postings of list l as the scan walks them: [beg, end) list positions
+// (compact = false), or [beg, end) indices into adm_pos (compact = true)
+// when the list-order mask admits under half of the list.
+struct ListSpan {
+  uint32_t beg, end;
+  bool compact;
+};
+__device__ __forceinline__ ListSpan list_span(const IvfArgs& a, uint32_t l) {
+  const uint32_t lbeg = __ldg(a.offsets + l), lend = __ldg(a.offsets + l + 1);
+  if (a.adm_pos != nullptr && lend > lbeg) {
+    const uint32_t a0 = adm_index(a, lbeg), a1 = adm_index(a, lend);
+    if (2 * (a1 - a0) < lend - lbeg) return ListSpan{a0, a1, true};
+  }
+  return ListSpan{lbeg, lend, false};
+}
 
 // Rerank of a query's shortlist keys[0, S) (sorted, sentinels last) with the
 // reference's warp-order fp32 distance, sort, and the query's top k into
@@ -353,7 +382,7 @@ __device__ __forceinline__ float sq8_row(const float* __restrict__ qres, const f
 // meta rows), scanned by the register-prefetching loop with R postings per
 // thread per round, software-pipelined across rounds (PIPE).
 template <int MODE, int MW, int R = 4, bool PIPE = false>
-__global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
+__global__ void __launch_bounds__(IVF_THREADS, (MODE == IVF_RABITQ && MW == 1) ? 4 : 1) ivf_scan_kernel(IvfArgs a) {
   // a round offers at most IVF_THREADS * R candidates, appended after the
   // shortlist; the buffer is flushed between rounds, so one round must fit
   static_assert((uint32_t)IVF_THREADS * R <= IVF_BUF, "a round of postings must fit the candidate buffer");
@@ -411,7 +440,10 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
       if (G > 1)
         for (uint32_t p = 0; p < npq; ++p) {
           const uint32_t l = a.probes[(size_t)q * a.nprobe + p].id;
-          if (l < a.nlist) total += __ldg(a.offsets + l + 1) - __ldg(a.offsets + l);
+          if (l < a.nlist) {
+            const ListSpan sp = list_span(a, l);
+            total += sp.end - sp.beg;
+          }
         }
       s_total = total;
     }
@@ -456,7 +488,9 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
     for (uint32_t p = 0; p < npq; ++p) {
       const uint32_t l = a.probes[(size_t)q * a.nprobe + p].id;
       if (l >= a.nlist) continue;  // uniform over the block
-      const uint32_t lbeg = __ldg(a.offsets + l), llen = __ldg(a.offsets + l + 1) - lbeg;
+      const ListSpan sp = list_span(a, l);
+      const uint32_t lbeg = sp.beg, llen = sp.end - sp.beg;
+      const bool compact = sp.compact;  // uniform over the block
       const uint64_t s0 = max(lo, cum), s1 = min(hi, cum + llen);
       const uint64_t at = cum;
       cum += llen;
@@ -533,17 +567,24 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
           // the mask admits it -- known from the bit word alone, so the code
           // rows (list-major: addressed by position) load alongside the ids
           bool bits[R], in[R];
+          uint32_t pos[R];
 #pragma unroll
           for (int r = 0; r < R; ++r) {
             const uint32_t i = b0 + r * IVF_THREADS + tid;
-            bits[r] = a.list_allow != nullptr && i < a.list_n;
-            in[r] = i < end && (!bits[r] || ((__ldg(a.list_allow + (i >> 5)) >> (i & 31u)) & 1u));
-            v[r] = in[r] ? __ldg(a.vec_ids + i) : 0xFFFFFFFFu;
+            if (compact) {  // i indexes the admitted positions: all pass the mask
+              bits[r] = true;
+              in[r] = i < end;
+              pos[r] = in[r] ? __ldg(a.adm_pos + i) : 0u;
+            } else {
+              bits[r] = a.list_allow != nullptr && i < a.list_n;
+              in[r] = i < end && (!bits[r] || ((__ldg(a.list_allow + (i >> 5)) >> (i & 31u)) & 1u));
+              pos[r] = i;
+            }
+            v[r] = in[r] ? __ldg(a.vec_ids + pos[r]) : 0xFFFFFFFFu;
           }
 #pragma unroll
           for (int r = 0; r < R; ++r) {
-            const uint32_t i = b0 + r * IVF_THREADS + tid;
-            const size_t row_i = a.list_major ? i : v[r];
+            const size_t row_i = a.list_major ? pos[r] : v[r];
             const uint4* row = reinterpret_cast<const uint4*>(a.codes + row_i * (16u * MW));
 #pragma unroll
             for (int j = 0; j < MWW; ++j) c[r][j] = in[r] ? __ldg(row + j) : make_uint4(0u, 0u, 0u, 0u);
@@ -598,9 +639,10 @@ __global__ void __launch_bounds__(IVF_THREADS) ivf_scan_kernel(IvfArgs a) {
         }
       } else {
         for (uint32_t base = beg; base < end; base += IVF_THREADS) {
-          const uint32_t i = base + tid;
-          const bool bits = a.list_allow != nullptr && i < a.list_n;
-          if (i < end && (!bits || ((__ldg(a.list_allow + (i >> 5)) >> (i & 31u)) & 1u))) {
+          const uint32_t j = base + tid;
+          const bool bits = compact || (a.list_allow != nullptr && j < a.list_n);
+          const uint32_t i = compact ? (j < end ? __ldg(a.adm_pos + j) : 0u) : j;
+          if (j < end && (compact || !bits || ((__ldg(a.list_allow + (i >> 5)) >> (i & 31u)) & 1u))) {
             const uint32_t vid = __ldg(a.vec_ids + i);
             if ((bits || mask_allows(a.mask, vid)) && filter_allows(qf, vid)) {
               const size_t row_i = a.list_major ? i : vid;
@@ -672,6 +714,74 @@ __global__ void __launch_bounds__(256) ivf_list_mask_kernel(const uint32_t* __re
   if ((threadIdx.x & 31u) == 0 && i < n) out[i >> 5] = w;
 }
 
+// Compaction of the list-order mask (three launches): per 1,024-word block
+// the count of admitted positions; an exclusive scan of those counts; per
+// word the exclusive prefix count and the admitted positions themselves,
+// in list order.
+constexpr uint32_t ADM_BLOCK = 1024;
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  return x;
+}
+
+// exclusive prefix of v over the block (ADM_BLOCK threads), plus the block total
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t s_warp[ADM_BLOCK / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t x = warp_incl_scan(v, lane);
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) s_warp[lane] = warp_incl_scan(s_warp[lane], lane);
+  __syncthreads();
+  const uint32_t excl = (warp ? s_warp[warp - 1] : 0u) + x - v;
+  *total = s_warp[ADM_BLOCK / 32 - 1];
+  __syncthreads();
+  return excl;
+}
+
+__global__ void __launch_bounds__(ADM_BLOCK) adm_count_kernel(const uint32_t* __restrict__ words, uint32_t nwords,
+                                                              uint32_t* __restrict__ block_sums) {
+  const uint32_t w = blockIdx.x * ADM_BLOCK + threadIdx.x;
+  uint32_t total;
+  block_excl_scan(w < nwords ? __popc(__ldg(words + w)) : 0u, &total);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// in place, one block, ADM_BLOCK entries at a time with a running carry
+__global__ void __launch_bounds__(ADM_BLOCK) adm_scan_kernel(uint32_t* __restrict__ sums, uint32_t n) {
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < n; base += ADM_BLOCK) {
+    const uint32_t i = base + threadIdx.x;
+    uint32_t total;
+    const uint32_t excl = block_excl_scan(i < n ? sums[i] : 0u, &total);
+    if (i < n) sums[i] = carry + excl;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(ADM_BLOCK) adm_compact_kernel(const uint32_t* __restrict__ words, uint32_t nwords,
+                                                                const uint32_t* __restrict__ block_off,
+                                                                uint32_t* __restrict__ prefix,
+                                                                uint32_t* __restrict__ pos) {
+  const uint32_t w = blockIdx.x * ADM_BLOCK + threadIdx.x;
+  uint32_t bits = w < nwords ? __ldg(words + w) : 0u, total;
+  const uint32_t o = __ldg(block_off + blockIdx.x) + block_excl_scan(__popc(bits), &total);
+  if (w < nwords) {
+    prefix[w] = o;
+    if (w == nwords - 1) prefix[nwords] = o + __popc(bits);
+    for (uint32_t k = o; bits; ++k) {
+      const uint32_t b = __ffs(bits) - 1;
+      bits &= bits - 1;
+      pos[k] = w * 32 + b;
+    }
+  }
+}
+
 __global__ void relayout_codes_kernel(const uint8_t* __restrict__ by_id, const uint32_t* __restrict__ vec_ids,
                                       uint32_t n, uint32_t row_bytes, uint8_t* __restrict__ by_list) {
   const uint64_t total = (uint64_t)n * row_bytes;
@@ -688,7 +798,7 @@ size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 // rc: 0 to launch, 1 when the call has nothing to do, else an error code.
 struct IvfPlan {
   int rc = 0;
-  uint32_t P = 0, top_k = 0, nprobe = 0, shortlist = 0, G = 1, sms = 0, list_n = 0;
+  uint32_t P = 0, top_k = 0, nprobe = 0, shortlist = 0, G = 1, sms = 0, list_n = 0, nwords = 0, adm_blocks = 0;
   FlatPlan cp;
   size_t coarse_bytes = 0, probe_bytes = 0, part_bytes = 0, allow_bytes = 0, scratch_bytes = 0;
 };
@@ -729,7 +839,14 @@ IvfPlan plan_ivf_search(int mode, const IvfLaunch& L) {
   const size_t probe_bytes = align256((size_t)L.nq * nprobe * sizeof(GpuSearchResult));
   const size_t part_bytes = G > 1 ? align256((size_t)L.nq * G * shortlist * 8) : 0;
   const uint32_t list_n = L.mask ? L.num_vectors : 0u;
-  const size_t allow_bytes = align256(((size_t)list_n + 31) / 32 * 4);
+  const size_t nwords = ((size_t)list_n + 31) / 32;
+  const size_t allow_bytes = align256(nwords * 4);
+  // compaction of the admitted positions ("ivf.compact" 0 turns it off)
+  const bool compact = list_n > 0 && tune_value("ivf.compact", 1) != 0;
+  const uint32_t adm_blocks = compact ? (uint32_t)((nwords + ADM_BLOCK - 1) / ADM_BLOCK) : 0u;
+  const size_t adm_bytes = compact ? align256((size_t)adm_blocks * 4) + align256((nwords + 1) * 4) +
+                                         align256((size_t)list_n * 4)
+                                   : 0;
   Q.P = P;
   Q.top_k = top_k;
   Q.nprobe = nprobe;
@@ -742,7 +859,9 @@ IvfPlan plan_ivf_search(int mode, const IvfLaunch& L) {
   Q.probe_bytes = probe_bytes;
   Q.part_bytes = part_bytes;
   Q.allow_bytes = allow_bytes;
-  Q.scratch_bytes = coarse_bytes + probe_bytes + part_bytes + 256 + allow_bytes;
+  Q.adm_blocks = adm_blocks;
+  Q.nwords = (uint32_t)nwords;
+  Q.scratch_bytes = coarse_bytes + probe_bytes + part_bytes + 256 + allow_bytes + adm_bytes;
   return Q;
 }
 
@@ -779,6 +898,17 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
                                                                      list_allow);
     note_launch();
   }
+  uint32_t *adm_prefix = nullptr, *adm_pos = nullptr;
+  if (Q.adm_blocks) {
+    uint32_t* adm_sums = list_allow + Q.allow_bytes / 4;
+    adm_prefix = adm_sums + align256((size_t)Q.adm_blocks * 4) / 4;
+    adm_pos = adm_prefix + align256(((size_t)Q.nwords + 1) * 4) / 4;
+    ProfScope ps("ivf_mask_compact", stream);
+    adm_count_kernel<<<Q.adm_blocks, ADM_BLOCK, 0, stream>>>(list_allow, Q.nwords, adm_sums);
+    adm_scan_kernel<<<1, ADM_BLOCK, 0, stream>>>(adm_sums, Q.adm_blocks);
+    adm_compact_kernel<<<Q.adm_blocks, ADM_BLOCK, 0, stream>>>(list_allow, Q.nwords, adm_sums, adm_prefix, adm_pos);
+    note_launch(3);
+  }
 
   IvfArgs a{};
   a.centroids = L.centroids;
@@ -814,6 +944,8 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   a.mask = L.mask;
   a.list_allow = list_allow;
   a.list_n = list_n;
+  a.adm_pos = adm_pos;
+  a.adm_prefix = adm_prefix;
   a.q_topk = L.q_topk;
   a.q_nprobe = L.q_nprobe;
   a.q_rerank = L.q_rerank;

@@ -352,6 +352,11 @@ int fv_profile_summary(char* buf, size_t len);
  *                       SM cut each query's probed postings into G equal
  *                       ranges scanned by separate CTAs and merged (same
  *                       answer); 0 or 1: never; G > 1: always G ranges
+ *   "ivf.compact"       1 (default): with a validity mask, each call compacts
+ *                       the mask-admitted list positions once, and a probed
+ *                       list whose mask admits under half of it is walked
+ *                       over those positions only (same answer); 0: every
+ *                       posting is walked and tested against the mask bits
  * Unknown keys return FV_ERR_ARG. Values apply to launches issued after the
  * call. */
 int fv_tune_set(const char* key, int64_t value);
