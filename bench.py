@@ -65,6 +65,9 @@ def parse_args():
     ap.add_argument("--rates", type=str, default="5000,20000,50000,100000,200000",
                     help="serve: offered request rates (requests/s)")
     ap.add_argument("--serve-seconds", type=float, default=0.5, help="serve: trace length per rate")
+    ap.add_argument("--serve-means", default="unit", choices=["unit", "raw"],
+                    help="serve: component means normalised (unit, the default reading of the configuration) "
+                         "or left N(0, I) (raw, the fp8 configuration's convention)")
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--dim", type=int, default=None)
     ap.add_argument("--batch", type=int, default=None)
@@ -1001,7 +1004,8 @@ def run_serve(a, world, rank, local, dev, peaks, peak_kind):
     from fvgb300.index import BUILD_FP16, BUILD_IVF_SQ8, GpuVectorIndex, IndexConfig
     from fvgb300.serve import BatchKey, SearchBatcher
 
-    mix = dataclasses.replace(datasets.FP16_IP_UNIT, dim=a.dim)
+    mix = dataclasses.replace(datasets.FP16_IP_UNIT if a.serve_means == "unit" else datasets.FP16_IP_UNIT_RAWMEANS,
+                              dim=a.dim)
     t0 = time.perf_counter()
     base = datasets.sample_torch(mix, a.n, seed=1, stream=0, device=dev)
     idx = GpuVectorIndex(IndexConfig(dim=a.dim, nlist=4096, metric="ip", build_flags=BUILD_FP16 | BUILD_IVF_SQ8,
@@ -1057,20 +1061,28 @@ def run_serve(a, world, rank, local, dev, peaks, peak_kind):
                            "recall_at_10": rec}
         launches = scan.launch_count() - l0
         clk = clocks.stop()
+        st = b.serve_stats()
+        scratch_waits, scratch_peak, scratch_pool = st["scratch_waits"], st["scratch_peak_bytes"], \
+            st["scratch_pool_bytes"]
     top = sweep[rates[-1]]
     cfg = {"workload": "continuous batching: fp16 flat (1M x 768, IP) + IVF-SQ8 (nlist 4096) resident; requests "
                        "k in {10,100}, nprobe in {16,64}, filter in {none, 20%}; Poisson arrivals",
            "N": a.n, "dim": a.dim, "rates": rates, "max_batch": 1024, "max_wait_us": 200, "inflight": 4,
            "build_seconds": build_s, "l2": "inputs larger than L2 (fp16 base 1.54 GB, SQ8 codes 0.77 GB)",
-           "ivf_recall_note": "the mixture is nearly isotropic (unit centres, sigma 0.3 x sqrt(768) noise): true "
-                              "neighbours spread over almost all 4096 lists, so IVF at nprobe 16-64 finds few; "
-                              "the IVF requests measure serving latency, the fp16 requests carry recall@10"}
+           "component_means": a.serve_means,
+           "scratch_budget": "512 MiB pool per server (FvServeConfig.scratch_budget_kb = 0)"}
+    if a.serve_means == "unit":
+        cfg["ivf_recall_note"] = ("the mixture is nearly isotropic (unit centres, sigma 0.3 x sqrt(768) noise): true "
+                                  "neighbours spread over almost all 4096 lists, so IVF at nprobe 16-64 finds few; "
+                                  "the IVF requests measure serving latency, the fp16 requests carry recall@10; "
+                                  "--serve-means raw draws the means N(0, I) and the rows cluster")
     per_req_in = a.dim * 4 + 24
     _line(a, world, top["sustained_qps"], UNIT, top["requests"] / max(top["sustained_qps"], 1e-9),
           {"value": top["sustained_qps"], "unit": UNIT, "h2d_bytes_per_step": per_req_in,
            "d2h_bytes_per_step": 8 * 55, "note": "the served path starts from host queries; value is end to end"},
           launches, None, None, clk, None, "f16+u8", cfg, p50_ms=top["p50_ms"], p99_ms=top["p99_ms"],
-          serve_sweep=sweep, gpu_launches_note="kernels launched over the whole rate sweep (every rate's trace)")
+          serve_sweep=sweep, gpu_launches_note="kernels launched over the whole rate sweep (every rate's trace)",
+          scratch={"waits": scratch_waits, "peak_bytes": scratch_peak, "pool_bytes": scratch_pool})
 
 
 def main():

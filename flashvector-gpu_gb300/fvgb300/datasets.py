@@ -32,6 +32,11 @@ class Mixture:
 FLAT_L2_INT = Mixture(dim=128, components=1024, sigma=20.0, center_kind="uniform255", post="int255")
 # FP16 flat inner product: unit vectors from 4,096 components, sigma 0.3.
 FP16_IP_UNIT = Mixture(dim=768, components=4096, sigma=0.3, center_kind="normal", post="unit", center_norm=True)
+# The same shape with the component means left un-normalised (N(0, I),
+# norm ~ sqrt(768)): the configuration's text leaves the means unspecified;
+# against these means the sigma 0.3 noise is small, so rows cluster tightly
+# (the convention of the fp8 configuration's mixture).
+FP16_IP_UNIT_RAWMEANS = Mixture(dim=768, components=4096, sigma=0.3, center_kind="normal", post="unit")
 # FP8 flat L2: 16,384 components with N(0,1) means, sigma 0.5.
 FP8_L2 = Mixture(dim=96, components=16384, sigma=0.5, center_kind="normal", post="none")
 
