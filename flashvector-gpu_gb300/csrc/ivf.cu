@@ -37,6 +37,8 @@
 // shortlist is kept in shared memory: rows whose key cannot beat the
 // current shortlist's worst key are dropped, the rest are appended to a
 // buffer that is bitonic-merged into the shortlist when it fills.
+#include <cuda_fp16.h>
+
 #include "../../include/fv_bridge.h"
 #include "common.cuh"
 #include "kernels.h"
@@ -782,6 +784,167 @@ __global__ void __launch_bounds__(ADM_BLOCK) adm_compact_kernel(const uint32_t* 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-core coarse probe (large nlist). The exact coarse probe is a Q x
+// nlist fp32 scan; here an fp16 tensor-core scan of the centred queries
+// (q - mu) against the centred centroids (c - mu; L2 distances do not move
+// under the shift, the fp16 rounding error shrinks with the magnitudes)
+// returns each query's K best lists by that approximate distance, their
+// exact distances are recomputed with the exact probe's arithmetic (fmaf of
+// q - c in dimension order), and the first nprobe by (distance, list) are
+// kept. That is the exact probe list whenever no list outside the K can
+// reach the nprobe-th place: every list outside has approximate distance
+// >= t16 (the K-th approximate distance), an approximate distance is within
+// `err` of the exact one (a bound from the fp16 unit roundoff, the fp32
+// accumulation and the norms), so d_nprobe < (t16 - err) (1 - dim 2^-22)
+// proves it. A query that fails the test, or whose candidate heaps may have
+// dropped a key, is recomputed by the exact scan (coarse_exact_kernel).
+constexpr int CO_THREADS = 256;
+constexpr uint32_t CO_CHUNK = 2048;  // centroids per step of the exact fallback
+
+// mu: the mean of up to 1,024 evenly spaced centroids (any shift is exact
+// for L2; the mean keeps the fp16 values small)
+__global__ void __launch_bounds__(CO_THREADS) coarse_mu_kernel(const float* __restrict__ cent, uint32_t nlist,
+                                                               uint32_t dim, float* __restrict__ mu) {
+  const uint32_t d = blockIdx.x * CO_THREADS + threadIdx.x;
+  if (d >= dim) return;
+  const uint32_t s = min(nlist, 1024u);
+  float acc = 0.f;
+  for (uint32_t i = 0; i < s; ++i) acc += __ldg(cent + (size_t)((uint64_t)i * nlist / s) * dim + d);
+  mu[d] = acc / (float)s;
+}
+
+// One block per row: rows [0, nlist) are centroids -> fp16 (c - mu) padded to
+// pd, ||c - mu||^2, and the largest ||c - mu|| (float bits, atomicMax);
+// rows [nlist, nlist + nq) are queries -> q - mu in fp32.
+__global__ void __launch_bounds__(128) coarse_prep_kernel(const float* __restrict__ cent, uint32_t nlist,
+                                                          const float* __restrict__ queries, uint32_t nq,
+                                                          uint32_t dim, uint32_t pd, const float* __restrict__ mu,
+                                                          __half* __restrict__ c16, float* __restrict__ cnorm,
+                                                          uint32_t* __restrict__ cmax, float* __restrict__ qc) {
+  const uint32_t r = blockIdx.x;
+  if (r >= nlist) {
+    const uint32_t q = r - nlist;
+    for (uint32_t d = threadIdx.x; d < dim; d += 128)
+      qc[(size_t)q * dim + d] = __fsub_rn(__ldg(queries + (size_t)q * dim + d), mu[d]);
+    return;
+  }
+  __shared__ float s_red[4];
+  float part = 0.f;
+  for (uint32_t d = threadIdx.x; d < pd; d += 128) {
+    const float v = d < dim ? __fsub_rn(__ldg(cent + (size_t)r * dim + d), mu[d]) : 0.f;
+    c16[(size_t)r * pd + d] = __float2half_rn(v);
+    part = fmaf(v, v, part);
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = part;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const float n2 = (s_red[0] + s_red[1]) + (s_red[2] + s_red[3]);
+    cnorm[r] = n2;
+    atomicMax(cmax, __float_as_uint(sqrtf(n2)));
+  }
+}
+
+// exact coarse distance of query row qv (shared) to centroid c: the exact
+// probe's arithmetic (flat_f32_scan_kernel, FUSED)
+__device__ __forceinline__ float coarse_exact(const float* qv, const float* __restrict__ c, uint32_t dim) {
+  float acc = 0.f;
+  for (uint32_t d = 0; d < dim; ++d) {
+    const float diff = __fsub_rn(qv[d], __ldg(c + d));
+    acc = fmaf(diff, diff, acc);
+  }
+  return acc;
+}
+
+// Per query: exact distances of the K candidates, the first nprobe, and the
+// exactness test. flags[q] = 1 sends the query to the exact fallback.
+__global__ void __launch_bounds__(CO_THREADS) coarse_finish_kernel(const float* __restrict__ queries,
+                                                                   const float* __restrict__ cent, uint32_t nlist,
+                                                                   uint32_t dim, const GpuSearchResult* __restrict__ cand,
+                                                                   uint32_t K, uint32_t nprobe,
+                                                                   const float* __restrict__ qc,
+                                                                   const uint32_t* __restrict__ cmax,
+                                                                   uint32_t force_exact, uint32_t* __restrict__ flags,
+                                                                   GpuSearchResult* __restrict__ probes) {
+  extern __shared__ __align__(16) uint8_t co_smem[];
+  uint64_t* keys = reinterpret_cast<uint64_t*>(co_smem);          // [256]
+  float* qv = reinterpret_cast<float*>(co_smem + 256 * 8);        // [dim]
+  __shared__ float s_red[CO_THREADS / 32];
+  const uint32_t q = blockIdx.x;
+  const int tid = threadIdx.x;
+  float part = 0.f;
+  for (uint32_t d = tid; d < dim; d += CO_THREADS) {
+    qv[d] = __ldg(queries + (size_t)q * dim + d);
+    const float c = __ldg(qc + (size_t)q * dim + d);
+    part = fmaf(c, c, part);
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if ((tid & 31) == 0) s_red[tid >> 5] = part;
+  __syncthreads();
+  const GpuSearchResult* cq = cand + (size_t)q * K;
+  if (tid < (int)K) {
+    const uint32_t id = cq[tid].id;
+    keys[tid] = id < nlist ? make_key(coarse_exact(qv, cent + (size_t)id * dim, dim), id) : kSentinelKey;
+  } else if (tid < 256) {
+    keys[tid] = kSentinelKey;
+  }
+  __syncthreads();
+  block_bitonic_sort(keys, 256);
+  for (uint32_t j = tid; j < nprobe; j += CO_THREADS) probes[(size_t)q * nprobe + j] = key_to_result(keys[j], nullptr);
+  if (tid == 0 && K < nlist) {
+    float qn2 = 0.f;
+    for (int w = 0; w < CO_THREADS / 32; ++w) qn2 += s_red[w];
+    const float qn = sqrtf(qn2), cm = __uint_as_float(*cmax);
+    const GpuSearchResult last = cq[K - 1];
+    const float dnp = key_dist(keys[nprobe - 1]);
+    bool ok = last.id < nlist && keys[nprobe - 1] != kSentinelKey && qn < 3.0e4f && cm < 3.0e4f;
+    if (ok) {
+      const float t16 = last.distance;
+      const float fd = (float)dim;
+      // |q.c - fp16(q).fp16(c)| <= (2.01 u16 + dim 2^-23) |q| |c| + dim 2^-25 (|q| + |c|)
+      const float e_dot = (2.01f * 4.8828125e-4f + fd * 1.1920929e-7f) * qn * cm + fd * 2.9802322e-8f * (qn + cm);
+      const float e_norm = fd * 1.1920929e-7f * (qn2 + cm * cm);
+      const float e_add = 4.7683716e-7f * (qn2 + cm * cm + 2.f * qn * cm);
+      const float err = 2.f * e_dot + e_norm + e_add;
+      ok = dnp < (t16 - err) * (1.f - fd * 2.3841858e-7f);
+    }
+    if (!ok || force_exact) flags[q] = 1u;
+  }
+}
+
+// The exact probe of a flagged query (the others return at once): every
+// centroid's exact distance, the running best nprobe kept by sorting it
+// with each chunk of CO_CHUNK new keys.
+__global__ void __launch_bounds__(CO_THREADS) coarse_exact_kernel(const float* __restrict__ queries,
+                                                                  const float* __restrict__ cent, uint32_t nlist,
+                                                                  uint32_t dim, uint32_t nprobe,
+                                                                  const uint32_t* __restrict__ flags,
+                                                                  GpuSearchResult* __restrict__ probes) {
+  const uint32_t q = blockIdx.x;
+  if (flags[q] == 0u) return;
+  extern __shared__ __align__(16) uint8_t co_smem[];
+  constexpr uint32_t NK = 4096;                                    // pow2 >= 256 + CO_CHUNK
+  uint64_t* keys = reinterpret_cast<uint64_t*>(co_smem);          // [NK]
+  float* qv = reinterpret_cast<float*>(co_smem + NK * 8);         // [dim]
+  const int tid = threadIdx.x;
+  for (uint32_t d = tid; d < dim; d += CO_THREADS) qv[d] = __ldg(queries + (size_t)q * dim + d);
+  for (uint32_t i = tid; i < 256; i += CO_THREADS) keys[i] = kSentinelKey;
+  __syncthreads();
+  for (uint32_t c0 = 0; c0 < nlist; c0 += CO_CHUNK) {
+    for (uint32_t i = tid; i < NK - 256; i += CO_THREADS) {
+      const uint32_t c = c0 + i;
+      keys[256 + i] = (i < CO_CHUNK && c < nlist) ? make_key(coarse_exact(qv, cent + (size_t)c * dim, dim), c)
+                                                  : kSentinelKey;
+    }
+    __syncthreads();
+    block_bitonic_sort(keys, NK);
+  }
+  for (uint32_t j = tid; j < nprobe; j += CO_THREADS) probes[(size_t)q * nprobe + j] = key_to_result(keys[j], nullptr);
+}
+
 __global__ void relayout_codes_kernel(const uint8_t* __restrict__ by_id, const uint32_t* __restrict__ vec_ids,
                                       uint32_t n, uint32_t row_bytes, uint8_t* __restrict__ by_list) {
   const uint64_t total = (uint64_t)n * row_bytes;
@@ -793,12 +956,54 @@ __global__ void relayout_codes_kernel(const uint8_t* __restrict__ by_id, const u
 
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// Committed autotuner results for the IVF scans (tuning/gb300.json
+// "ivf_entries", compiled in by build.py as tuning_ivf.inc): per shape range
+// the list-scan pipelining, the posting-range split and the coarse probe
+// that searched fastest (every choice gives the same answer). Knobs set
+// with fv_tune_set take precedence; "tc.table" = 0 ignores the table.
+struct IvfTuneEntry {
+  int mode;
+  uint32_t dim_lo, dim_hi;
+  uint64_t n_lo, n_hi;
+  uint32_t nlist_lo, nlist_hi, nq_lo, nq_hi, np_lo, np_hi;
+  int pipeline, split, tc_coarse;
+};
+const IvfTuneEntry kIvfTuneTable[] = {
+#include "tuning_ivf.inc"
+    {-1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, -1, -1, -1}};
+
+const IvfTuneEntry* ivf_tune_lookup(int mode, uint32_t dim, uint64_t n, uint32_t nlist, uint32_t nq,
+                                    uint32_t nprobe) {
+  if (tune_value("tc.table", 1) == 0) return nullptr;
+  for (const IvfTuneEntry& e : kIvfTuneTable) {
+    if (e.mode < 0) break;
+    if (e.mode == mode && dim >= e.dim_lo && dim <= e.dim_hi && n >= e.n_lo && n <= e.n_hi && nlist >= e.nlist_lo &&
+        nlist <= e.nlist_hi && nq >= e.nq_lo && nq <= e.nq_hi && nprobe >= e.np_lo && nprobe <= e.np_hi)
+      return &e;
+  }
+  return nullptr;
+}
+
+// A knob's value: the explicit setting, else the table entry's, else `dflt`
+// (-1 in both means automatic).
+int64_t ivf_knob(const char* key, int table_value, int64_t dflt) {
+  const int64_t v = tune_value(key, -1);
+  if (v >= 0) return v;
+  if (table_value >= 0) return table_value;
+  return dflt;
+}
+
 // Every size of one IVF search call, computed once: launch_ivf_search
 // launches from it and the serving loop admits a batch by scratch_bytes.
 // rc: 0 to launch, 1 when the call has nothing to do, else an error code.
 struct IvfPlan {
   int rc = 0;
   uint32_t P = 0, top_k = 0, nprobe = 0, shortlist = 0, G = 1, sms = 0, list_n = 0, nwords = 0, adm_blocks = 0;
+  // tensor-core coarse probe: candidates per query and the byte offsets of
+  // its buffers in the coarse part of the scratch
+  bool tcc = false, force_exact = false, pipeline = false;
+  uint32_t K = 0;
+  size_t co_mu = 0, co_c16 = 0, co_cnorm = 0, co_qc = 0, co_cand = 0, co_flags = 0, co_cmax = 0, co_tc = 0;
   FlatPlan cp;
   size_t coarse_bytes = 0, probe_bytes = 0, part_bytes = 0, allow_bytes = 0, scratch_bytes = 0;
 };
@@ -825,7 +1030,9 @@ IvfPlan plan_ivf_search(int mode, const IvfLaunch& L) {
   // CTAs); each range keeps its own shortlist and ivf_merge_kernel joins
   // them. "ivf.split": -1 automatic, 0 / 1 never, G > 1 force G.
   const uint32_t sms = (uint32_t)device_sm_count();
-  const int64_t split_knob = tune_value("ivf.split", -1);
+  const IvfTuneEntry* te = ivf_tune_lookup(mode, L.dim, L.num_vectors, L.nlist, L.nq, nprobe);
+  Q.pipeline = ivf_knob("ivf.pipeline", te ? te->pipeline : -1, 0) == 1;
+  const int64_t split_knob = ivf_knob("ivf.split", te ? te->split : -1, -1);
   uint32_t G = 1;
   if (split_knob > 1)
     G = (uint32_t)split_knob;
@@ -833,9 +1040,38 @@ IvfPlan plan_ivf_search(int mode, const IvfLaunch& L) {
     G = (4 * sms + L.nq - 1) / L.nq;
   G = std::max(1u, std::min<uint32_t>(std::min(G, 64u), 16384u / next_pow2(shortlist)));
 
+  // coarse probe: exact fp32 scan, or the tensor-core candidates + exact
+  // rescore ("ivf.tc_coarse": -1 automatic, 0 off, 1 on, 2 on with every
+  // query sent to the exact fallback -- a check of the fallback)
+  const int64_t tcc_knob = ivf_knob("ivf.tc_coarse", te ? te->tc_coarse : -1, -1);
+  const uint32_t K = std::min<uint32_t>(std::min(256u, nprobe + 16), L.nlist);
+  // (tables of at least one 256-row tile and one 64-element K block, so no
+  // TMA box is larger than the tensor it reads)
+  const bool tcc_fits = L.nlist >= 256 && L.dim >= 64;
+  const bool tcc = tcc_fits && (tcc_knob > 0 || (tcc_knob < 0 && L.nlist >= 2048 && L.nq >= 256 &&
+                                                  K == nprobe + 16 && K < L.nlist));
+  const uint32_t pd16 = (L.dim + 15) / 16 * 16;
+  TcTables ct{false, nullptr, nullptr, nullptr, nullptr, L.nlist, L.dim, pd16};
+  const FvScanOptions copt{0, 0, 0.f, 0};
+  size_t tc_bytes = 0;
+  if (tcc) {
+    Q.co_mu = 0;
+    Q.co_c16 = align256(Q.co_mu + (size_t)L.dim * 4);
+    Q.co_cnorm = (Q.co_c16 + (size_t)L.nlist * pd16 * 2 + 1023) / 1024 * 1024;
+    Q.co_qc = align256(Q.co_cnorm + (size_t)L.nlist * 4);
+    Q.co_cand = align256(Q.co_qc + (size_t)L.nq * L.dim * 4);
+    Q.co_flags = align256(Q.co_cand + (size_t)L.nq * K * 8);
+    Q.co_cmax = align256(Q.co_flags + (size_t)L.nq * 4);
+    Q.co_tc = (Q.co_cmax + 256 + 1023) / 1024 * 1024;
+    tc_bytes = Q.co_tc + tc_scan_scratch_bytes(ct, L.nq, K, METRIC_L2, copt);
+  }
+  Q.tcc = tcc;
+  Q.K = K;
+  Q.force_exact = tcc_knob == 2;
+
   // scratch: coarse heaps | probes | range shortlists | work counter
   const FlatPlan cp = plan_flat_f32(L.nlist, L.nq, nprobe, 0);
-  const size_t coarse_bytes = align256(cp.scratch_bytes);
+  const size_t coarse_bytes = tcc ? (tc_bytes + 1023) / 1024 * 1024 : align256(cp.scratch_bytes);
   const size_t probe_bytes = align256((size_t)L.nq * nprobe * sizeof(GpuSearchResult));
   const size_t part_bytes = G > 1 ? align256((size_t)L.nq * G * shortlist * 8) : 0;
   const uint32_t list_n = L.mask ? L.num_vectors : 0u;
@@ -867,6 +1103,55 @@ IvfPlan plan_ivf_search(int mode, const IvfLaunch& L) {
 
 }  // namespace
 
+// The tensor-core coarse probe of one call into probes[nq][nprobe] (exact:
+// see coarse_finish_kernel); its buffers are the coarse part of `scratch`.
+static int launch_coarse_tc(const IvfPlan& Q, const IvfLaunch& L, uint8_t* scratch, GpuSearchResult* probes,
+                     cudaStream_t stream) {
+  ProfScope ps("coarse_tc", stream);
+  float* mu = reinterpret_cast<float*>(scratch + Q.co_mu);
+  __half* c16 = reinterpret_cast<__half*>(scratch + Q.co_c16);
+  float* cnorm = reinterpret_cast<float*>(scratch + Q.co_cnorm);
+  float* qc = reinterpret_cast<float*>(scratch + Q.co_qc);
+  GpuSearchResult* cand = reinterpret_cast<GpuSearchResult*>(scratch + Q.co_cand);
+  uint32_t* flags = reinterpret_cast<uint32_t*>(scratch + Q.co_flags);
+  uint32_t* cmax = reinterpret_cast<uint32_t*>(scratch + Q.co_cmax);
+  const uint32_t pd16 = (L.dim + 15) / 16 * 16;
+  cudaError_t e = cudaMemsetAsync(flags, 0, (size_t)L.nq * 4, stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(cmax, 0, 4, stream);
+  if (e != cudaSuccess) return (int)e;
+  coarse_mu_kernel<<<(L.dim + CO_THREADS - 1) / CO_THREADS, CO_THREADS, 0, stream>>>(L.centroids, L.nlist, L.dim, mu);
+  coarse_prep_kernel<<<L.nlist + L.nq, 128, 0, stream>>>(L.centroids, L.nlist, L.queries, L.nq, L.dim, pd16, mu, c16,
+                                                         cnorm, cmax, qc);
+  note_launch(2);
+  const TcTables ct{false, c16, cnorm, nullptr, nullptr, L.nlist, L.dim, pd16};
+  const FvScanOptions copt{0, 0, 0.f, 0};
+  int rc = launch_tc_scan_ext(ct, qc, L.nq, Q.K, METRIC_L2, nullptr, cand, copt, stream, nullptr, scratch + Q.co_tc,
+                              flags);
+  if (rc != 0) return rc;
+  const size_t fsmem = 256 * 8 + (size_t)L.dim * 4;
+  const size_t xsmem = 4096 * 8 + (size_t)L.dim * 4;
+  e = cudaFuncSetAttribute(coarse_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(coarse_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xsmem);
+  if (e != cudaSuccess) return (int)e;
+  coarse_finish_kernel<<<L.nq, CO_THREADS, fsmem, stream>>>(L.queries, L.centroids, L.nlist, L.dim, cand, Q.K, Q.nprobe,
+                                                           qc, cmax, Q.force_exact ? 1u : 0u, flags, probes);
+  coarse_exact_kernel<<<L.nq, CO_THREADS, xsmem, stream>>>(L.queries, L.centroids, L.nlist, L.dim, Q.nprobe, flags,
+                                                          probes);
+  note_launch(2);
+  return (int)cudaGetLastError();
+}
+
+int ivf_tune_query(int mode, uint32_t dim, uint64_t n, uint32_t nlist, uint32_t nq, uint32_t nprobe,
+                   int32_t* out3) {
+  const IvfTuneEntry* e = ivf_tune_lookup(mode, dim, n, nlist, nq, nprobe);
+  if (!e) return FV_ERR_ARG;
+  out3[0] = e->pipeline;
+  out3[1] = e->split;
+  out3[2] = e->tc_coarse;
+  return 0;
+}
+
 size_t ivf_search_scratch_bytes(int mode, const IvfLaunch& L) {
   const IvfPlan Q = plan_ivf_search(mode, L);
   return Q.rc == 0 ? Q.scratch_bytes : 0;
@@ -887,8 +1172,13 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   uint64_t* partial = G > 1 ? reinterpret_cast<uint64_t*>(scratch + coarse_bytes + probe_bytes) : nullptr;
   uint32_t* work = reinterpret_cast<uint32_t*>(scratch + coarse_bytes + probe_bytes + part_bytes);
 
-  int rc = launch_flat_f32_planned(cp, L.centroids, nullptr, L.nlist, L.dim, L.queries, L.nq, nprobe, METRIC_L2,
-                                   nullptr, probes, true, cp.scratch_bytes ? scratch : nullptr, stream);
+  int rc = 0;
+  if (Q.tcc) {
+    rc = launch_coarse_tc(Q, L, scratch, probes, stream);
+  } else {
+    rc = launch_flat_f32_planned(cp, L.centroids, nullptr, L.nlist, L.dim, L.queries, L.nq, nprobe, METRIC_L2,
+                                 nullptr, probes, true, cp.scratch_bytes ? scratch : nullptr, stream);
+  }
   if (rc != 0) return rc;
   cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t), stream);
   if (e != cudaSuccess) return (int)e;
@@ -966,7 +1256,7 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream) {
   // thread per round, next round's loads in flight while scoring). Off by
   // default: its 78 registers allow 3 CTAs per SM where the plain loop
   // (60 registers, 4 postings per round) runs 4, which measured 7% faster.
-  const bool pipe = tune_value("ivf.pipeline", 0) != 0;
+  const bool pipe = Q.pipeline;
   auto kern = ivf_scan_kernel<IVF_SQ8, 0>;
   if (mode == IVF_RABITQ) {
     // bits rows of P/8 bytes as 16-byte words when they and the meta rows
@@ -1016,3 +1306,9 @@ int launch_relayout_codes(const uint8_t* by_id, const uint32_t* vec_ids, uint32_
 }
 
 }  // namespace fv
+
+extern "C" int fv_tune_lookup_ivf(int mode, uint32_t dim, uint64_t num_vectors, uint32_t nlist, uint32_t num_queries,
+                                  uint32_t nprobe, int32_t* out_knobs) {
+  if (!out_knobs) return FV_ERR_NULL;
+  return fv::ivf_tune_query(mode, dim, num_vectors, nlist, num_queries, nprobe, out_knobs);
+}

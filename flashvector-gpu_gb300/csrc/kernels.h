@@ -117,6 +117,13 @@ cudaError_t dispatch_tc_scan_fp8(int kl, int groups, int metric, bool table_scal
 int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
                    const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream,
                    const QueryFilter* filters = nullptr);
+// launch_tc_scan with the scratch given by the caller (ext_scratch: at
+// least tc_scan_scratch_bytes, 1 KB aligned; null: the stream's arena) and
+// an optional per-query flag array set for a query whose merged shortlist
+// may have lost keys to a full range heap (the caller zeroes it).
+int launch_tc_scan_ext(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
+                       const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream,
+                       const QueryFilter* filters, void* ext_scratch, uint32_t* incomplete_q);
 // The scratch bytes launch_tc_scan takes from the stream's arena for the
 // same arguments (same plan, same tuning knobs).
 size_t tc_scan_scratch_bytes(const TcTables& t, uint32_t nq, uint32_t k, MetricType metric, const FvScanOptions& opt);
@@ -158,6 +165,9 @@ int launch_ivf_search(int mode, const IvfLaunch& L, cudaStream_t stream);
 // The scratch bytes launch_ivf_search takes from the stream's arena for the
 // same arguments (0 when the call launches nothing or is refused).
 size_t ivf_search_scratch_bytes(int mode, const IvfLaunch& L);
+// The committed IVF autotuner entry for a shape: out3 = {pipeline, split,
+// tc_coarse} (-1: automatic); FV_ERR_ARG when none applies.
+int ivf_tune_query(int mode, uint32_t dim, uint64_t n, uint32_t nlist, uint32_t nq, uint32_t nprobe, int32_t* out3);
 int launch_relayout_codes(const uint8_t* by_id, const uint32_t* vec_ids, uint32_t n, uint32_t row_bytes,
                           uint8_t* by_list, cudaStream_t stream);
 

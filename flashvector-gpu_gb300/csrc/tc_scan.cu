@@ -165,6 +165,7 @@ struct SelectArgs {
   const float* tau;          // per-query admission bound of the scan (null: none)
   uint32_t* redo;            // set for a bounded query whose shortlist came up short
   const uint32_t* only;      // process only the flagged queries (null: all)
+  uint32_t* incomplete_q;    // per-query flag set when a range heap may have dropped keys (or null)
 };
 
 constexpr int SEL_THREADS = 256;
@@ -203,7 +204,10 @@ __global__ void __launch_bounds__(SEL_THREADS) tc_select_kernel(SelectArgs s) {
     }
   }
   __syncthreads();
-  if (incomplete && threadIdx.x == 0) set_status(s.status, kStatusOverflow);
+  if (incomplete && threadIdx.x == 0) {
+    set_status(s.status, kStatusOverflow);
+    if (s.incomplete_q) s.incomplete_q[q] = 1u;
+  }
   // a bounded scan admitted fewer than kp rows: the bound from the sample was
   // below the query's kp-th distance, so the query is scanned again unbounded
   if (s.redo && threadIdx.x == 0 && keys[kp - 1] == kSentinelKey && s.tau[q] < kSentinelDist) s.redo[q] = 1u;
@@ -531,6 +535,12 @@ size_t tc_scan_scratch_bytes(const TcTables& t, uint32_t nq, uint32_t k, MetricT
 int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
                    const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream,
                    const QueryFilter* filters) {
+  return launch_tc_scan_ext(t, queries, nq, k, metric, mask, out, opt, stream, filters, nullptr, nullptr);
+}
+
+int launch_tc_scan_ext(const TcTables& t, const float* queries, uint32_t nq, uint32_t k, MetricType metric,
+                       const uint32_t* mask, GpuSearchResult* out, const FvScanOptions& opt, cudaStream_t stream,
+                       const QueryFilter* filters, void* ext_scratch, uint32_t* incomplete_q) {
   const TcPlan P = plan_tc_scan(t, nq, k, metric, opt);
   const bool fp8 = P.fp8;
   const uint32_t elem = P.elem, kblocks = P.kblocks, shortlist = P.shortlist, kl = P.kl, kl_tmpl = P.kl_tmpl;
@@ -541,7 +551,7 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
   const uint32_t nq_rows = P.nq_rows, slot_stride = P.slot_stride;
   const size_t q_bytes = P.q_bytes, qn_bytes = P.qn_bytes, part_bytes = P.part_bytes, slot_bytes = P.slot_bytes;
   const size_t ppart_bytes = P.ppart_bytes;
-  uint8_t* scratch = static_cast<uint8_t*>(scratch_get(stream, P.scratch_bytes));
+  uint8_t* scratch = static_cast<uint8_t*>(ext_scratch ? ext_scratch : scratch_get(stream, P.scratch_bytes));
   if (!scratch) return (int)cudaErrorMemoryAllocation;
   void* qprep = scratch;
   float* qnorm = reinterpret_cast<float*>(scratch + q_bytes);
@@ -634,7 +644,7 @@ int launch_tc_scan(const TcTables& t, const float* queries, uint32_t nq, uint32_
 
   SelectArgs s{partial, splits * groups, kl, next_pow2(splits * groups * kl), shortlist, k, queries, t.vectors, t.dim,
                (int)metric,
-               opt.boundary_fp64 ? 1u : 0u, 0.f, out, status_word(), tau, redo, nullptr};
+               opt.boundary_fp64 ? 1u : 0u, 0.f, out, status_word(), tau, redo, nullptr, incomplete_q};
   s.eps = opt.boundary_eps > 0.f ? opt.boundary_eps : (float)((t.dim + 31) / 32 + 5) * 2.0f * 5.960464477539063e-08f;
   const size_t sel_smem = (size_t)std::max(s.pow2, next_pow2(shortlist)) * 8;
   e = cudaFuncSetAttribute(tc_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sel_smem);

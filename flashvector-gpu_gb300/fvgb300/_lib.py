@@ -177,6 +177,7 @@ SIGNATURES = {
     "fv_tune_set": (I32, [C.c_char_p, C.c_int64]),
     "fv_tune_get": (I32, [C.c_char_p, P]),
     "fv_tune_lookup": (I32, [I32, I32, U32, C.c_uint64, U32, U32, P]),
+    "fv_tune_lookup_ivf": (I32, [I32, U32, C.c_uint64, U32, U32, U32, P]),
     "fv_release_stream_scratch": (I32, [P]),
     "fv_serve_create": (I32, [P, P, P]),
     "fv_serve_create_with_executor": (I32, [U32, P, FvServeExecutor, P, P]),

@@ -205,6 +205,15 @@ def tune_lookup(precision: str, metric: str, dim: int, n: int, nq: int, k: int):
     return {"pair": out[0], "prepass": out[1], "stride": out[2], "overfetch": out[3]}
 
 
+def tune_lookup_ivf(mode: str, dim: int, n: int, nlist: int, nq: int, nprobe: int):
+    """The committed IVF autotuner knobs the library applies to this shape, or None."""
+    out = (C.c_int32 * 3)()
+    code = _lib.lib().fv_tune_lookup_ivf({"pq": 0, "sq8": 1, "rabitq": 2}[mode], dim, n, nlist, nq, nprobe, out)
+    if code != 0:
+        return None
+    return {"pipeline": out[0], "split": out[1], "tc_coarse": out[2]}
+
+
 class tuned:
     """Context manager that sets knobs and restores them on exit."""
 

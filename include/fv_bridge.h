@@ -345,9 +345,10 @@ int fv_profile_summary(char* buf, size_t len);
  *   "tc.table"          1 (default): knobs left automatic and a zero
  *                       over-fetch take the committed autotuner results
  *                       for the call's shape (tuning/gb300.json); 0: ignore
- *   "ivf.pipeline"      0 (default): the IVF-PQ list scan loads and scores
- *                       4 postings per thread per round; 1: 2 per round
- *                       with the next round's loads in flight
+ *   "ivf.pipeline"      -1 (default): the committed autotuner's choice for
+ *                       the call's shape, else 0; 0: the IVF-PQ list scan
+ *                       loads and scores 4 postings per thread per round;
+ *                       1: 2 per round with the next round's loads in flight
  *   "ivf.split"         -1 (default): batches of fewer than 4 queries per
  *                       SM cut each query's probed postings into G equal
  *                       ranges scanned by separate CTAs and merged (same
@@ -357,13 +358,29 @@ int fv_profile_summary(char* buf, size_t len);
  *                       list whose mask admits under half of it is walked
  *                       over those positions only (same answer); 0: every
  *                       posting is walked and tested against the mask bits
- * Unknown keys return FV_ERR_ARG. Values apply to launches issued after the
- * call. */
+ *   "ivf.tc_coarse"     -1 (default): the committed autotuner's choice for
+ *                       the call's shape, else: calls with nlist >= 2048 and >= 256
+ *                       queries find the probed lists with an fp16 tensor-
+ *                       core scan of the centred queries and centroids, the
+ *                       exact distances of each query's best candidates and
+ *                       a proof that no other list can enter (else the exact
+ *                       scan for that query): the same lists as the exact
+ *                       scan; 0: always the exact fp32 scan; 1: the tensor-
+ *                       core path whenever nlist >= 256 and dim >= 64;
+ *                       2: as 1 with every query sent to the exact fallback
+ * "ivf.split" and "ivf.tc_coarse" left at -1 also take the autotuner's
+ * choice where an entry covers the call. Unknown keys return FV_ERR_ARG.
+ * Values apply to launches issued after the call. */
 int fv_tune_set(const char* key, int64_t value);
 int fv_tune_get(const char* key, int64_t* value);
 /* The committed autotuner entry a tensor-core scan of this shape uses
  * (fp8: 0 fp16 rows, 1 e4m3 rows): out_knobs[4] = {pair, prepass, stride,
  * overfetch}. FV_ERR_ARG when no entry applies (or "tc.table" is 0). */
+/* The committed autotuner entry an IVF search of this shape uses (mode: 0
+ * PQ, 1 SQ8, 2 RaBitQ): out_knobs[3] = {pipeline, split, tc_coarse}, -1 for
+ * automatic. FV_ERR_ARG when no entry applies (or "tc.table" is 0). */
+int fv_tune_lookup_ivf(int mode, uint32_t dim, uint64_t num_vectors, uint32_t nlist, uint32_t num_queries,
+                       uint32_t nprobe, int32_t* out_knobs);
 int fv_tune_lookup(int fp8, MetricType metric, uint32_t dim, uint64_t num_vectors, uint32_t num_queries,
                    uint32_t top_k, int32_t* out_knobs);
 /* Installs a caller-owned device buffer as the scratch arena of `stream`

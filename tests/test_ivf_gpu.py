@@ -281,3 +281,47 @@ def test_ivf_matches_reference_kernels(cuda, name, mode, list_major):
                         mask=mask if c["mask"] else None, list_major=list_major)
         bad = ivf_golden.compare(mode, c, ids, dist, *ref[(mode, ci)])
         assert not bad, (ci, c, bad[:3])
+
+
+def given_centroid_tables(oracle_mod, x, nlist, m_pq, seed):
+    """IVF tables around `nlist` rows picked as centroids (no k-means: large
+    nlist stays quick on the CPU), in the reference's layout."""
+    rng = np.random.default_rng(seed)
+    cent = (x[rng.choice(x.shape[0], nlist, replace=False)]
+            + np.float32(0.01) * rng.standard_normal((nlist, x.shape[1]))).astype(np.float32)
+    assign = oracle_mod.coarse_probe(cent, x, 1)[0][:, 0].copy()
+    res = oracle_mod.residuals(x, cent, assign)
+    offsets, vec_ids = oracle_mod.ivf_lists(assign, nlist)
+    cb = oracle_mod.pq_train(res, m_pq, 5, seed)
+    mins, scales = oracle_mod.sq8_fit(res)
+    t = {"centroids": cent, "offsets": offsets, "vec_ids": vec_ids, "nlist": nlist, "codebooks": cb,
+         "pq_codes": oracle_mod.pq_encode(res, cb), "sq_mins": mins, "sq_scales": scales,
+         "sq_codes": oracle_mod.sq8_encode(res, mins, scales)}
+    t.update(oracle_mod.rabitq_encode(x, cent, assign))
+    return t
+
+
+@pytest.fixture(scope="module")
+def wide_nlist_case(oracle_mod):
+    x = gen_clustered(40000, 96, 64, 404)
+    q = gen_clustered(300, 96, 64, 405)
+    return x, q, given_centroid_tables(oracle_mod, x, 2048, 12, 7)
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_ivf_tensor_core_coarse_probe_is_exact(cuda, oracle_mod, wide_nlist_case, mode):
+    """The tensor-core coarse probe (fp16 candidates of the centred queries and
+    centroids, their exact distances, a proof that no other list can enter or
+    the exact scan for that query) probes exactly the lists of the exact fp32
+    scan: results bit-identical to the oracle with the path automatic (2,048
+    lists, 300 queries), forced, forced with every query sent to the exact
+    fallback, and off."""
+    from fvgb300 import scan
+
+    x, q, t = wide_nlist_case
+    ref = oracle_fn(oracle_mod, mode)(t, x, q, 10, 32, 256)
+    for knob in (-1, 1, 2, 0):
+        with scan.tuned(ivf_tc_coarse=knob):
+            ids, dist = run(cuda, t, x, q, mode, 10, 32, 256, list_major=True)
+        assert_same(ids, dist, ref)
+    assert scan.device_status() == 0
