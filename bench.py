@@ -774,49 +774,10 @@ def run_workload(a, world, rank, local):
 
 
 def zipf_ivf_data(n, dim, nlist, seed, device):
-    """Rows around 16,384 list centres whose sizes follow Zipf(1.1) with a
-    floor of 64; list centres scattered around the 1,024 components of the
-    integer-valued mixture (centres U[0,255], sigma 20); rows rounded and
-    clipped to [0, 255]. Returns (rows, list centres, queries sampler)."""
-    import numpy as np
-    import torch
+    """The IVF configuration's rows and lists (fvgb300.datasets.zipf_ivf_data)."""
+    from fvgb300 import datasets
 
-    rng = np.random.default_rng([seed, 3])
-    comps = rng.uniform(0, 255, size=(1024, dim)).astype(np.float32)
-    centers = comps[rng.integers(0, 1024, size=nlist)] + np.float32(20.0) * rng.standard_normal((nlist, dim),
-                                                                                              dtype=np.float32)
-    w = np.arange(1, nlist + 1, dtype=np.float64) ** -1.1
-    sizes = np.maximum(64, np.floor(n * w / w.sum())).astype(np.int64)
-    excess = int(sizes.sum() - n)
-    order = np.argsort(-sizes)
-    i = 0
-    while excess != 0:  # take the excess from (or give the deficit to) the largest lists
-        j = order[i % 8]
-        d = min(excess, sizes[j] - 64) if excess > 0 else excess
-        sizes[j] -= d
-        excess -= d
-        i += 1
-    sizes = sizes[rng.permutation(nlist)]
-    c_dev = torch.from_numpy(centers).to(device)
-    lists = torch.repeat_interleave(torch.arange(nlist, device=device), torch.from_numpy(sizes).to(device))
-    g = torch.Generator(device=device)
-    g.manual_seed(seed * 7919 + 11)
-    rows = torch.empty((n, dim), dtype=torch.float32, device=device)
-    for s in range(0, n, 1 << 20):
-        e = min(n, s + (1 << 20))
-        x = c_dev[lists[s:e]] + 8.0 * torch.randn((e - s, dim), generator=g, device=device)
-        rows[s:e] = x.round_().clamp_(0.0, 255.0)
-    perm = torch.randperm(n, generator=g, device=device)
-    rows = rows[perm].contiguous()
-    probs = torch.from_numpy(sizes.astype(np.float64) / sizes.sum()).to(device)
-
-    def queries(count, qseed):
-        gq = torch.Generator(device=device)
-        gq.manual_seed(qseed)
-        li = torch.multinomial(probs, count, replacement=True, generator=gq)
-        return (c_dev[li] + 8.0 * torch.randn((count, dim), generator=gq, device=device)).round_().clamp_(0.0, 255.0)
-
-    return rows, c_dev, queries, sizes
+    return datasets.zipf_ivf_data(n, dim, nlist, seed, device)
 
 
 def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind, mode="pq"):

@@ -38,6 +38,8 @@ def _nvcc() -> str:
 
 TUNING = PKG / "tuning" / "gb300.json"
 TUNE_INC = OBJ / "tuning_table.inc"
+TUNE_IVF_INC = OBJ / "tuning_ivf.inc"
+IVF_MODES = {"pq": 0, "sq8": 1, "rabitq": 2}
 METRICS = {"l2": 0, "cosine": 1, "ip": 2}
 
 
@@ -57,10 +59,22 @@ def _tuning_table() -> None:
     text = "// generated by build.py from tuning/gb300.json\n" + "\n".join(lines) + ("\n" if lines else "")
     if not TUNE_INC.exists() or TUNE_INC.read_text() != text:
         TUNE_INC.write_text(text)
+    # IVF entries: one IvfTuneEntry initialiser each (see csrc/ivf.cu)
+    lines = []
+    if TUNING.exists():
+        for e in json.loads(TUNING.read_text()).get("ivf_entries", []):
+            k = e["knobs"]
+            lines.append("    {%d, %du, %du, %dull, %dull, %du, %du, %du, %du, %du, %du, %d, %d, %d},"
+                         % (IVF_MODES[e["mode"]], e["dim"][0], e["dim"][1], e["n"][0], e["n"][1], e["nlist"][0],
+                            e["nlist"][1], e["nq"][0], e["nq"][1], e["nprobe"][0], e["nprobe"][1],
+                            k.get("pipeline", -1), k.get("split", -1), k.get("tc_coarse", -1)))
+    text = "// generated by build.py from tuning/gb300.json\n" + "\n".join(lines) + ("\n" if lines else "")
+    if not TUNE_IVF_INC.exists() or TUNE_IVF_INC.read_text() != text:
+        TUNE_IVF_INC.write_text(text)
 
 
 def _headers() -> list[Path]:
-    return list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h")) + [TUNE_INC]
+    return list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h")) + [TUNE_INC, TUNE_IVF_INC]
 
 
 def _stale(src: Path, obj: Path, newest_header: float) -> bool:

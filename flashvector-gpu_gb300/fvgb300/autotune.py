@@ -1,6 +1,7 @@
-"""Autotuner of the tensor-core scans; its results are committed to
-flashvector-gpu_gb300/tuning/gb300.json and compiled into libfvgb300 by
-build.py, where launch_tc_scan consults them for calls of a matching shape.
+"""Autotuner of the tensor-core scans and the IVF list scans; its results are
+committed to flashvector-gpu_gb300/tuning/gb300.json and compiled into
+libfvgb300 by build.py, where launch_tc_scan and launch_ivf_search consult
+them for calls of a matching shape.
 
 For each benchmark shape it sweeps
   * tc.pair          one-SM CTAs or cta_group::2 pairs (long rows only),
@@ -13,7 +14,21 @@ fastest whose recall@10 and recall@k are both >= the target (0.99); the
 pair / pre-pass / stride knobs never change the answer (the tests check
 this), the over-fetch can.
 
-    python -m fvgb300.autotune [--shapes all|fp16|fp8] [--out tuning/gb300.json]
+For each IVF benchmark shape (the 10M-row IVF-PQ / IVF-RaBitQ list scans over
+Zipf-skewed lists at nprobe 8 / 32 / 128, the serving configuration's
+IVF-SQ8 at nprobe 16 / 64) it sweeps
+  * ivf.pipeline     the PQ list scan's plain or software-pipelined loop,
+  * ivf.split        posting ranges spread over CTAs for small batches
+                     (automatic) or one CTA per query,
+  * ivf.tc_coarse    the exact fp32 coarse probe or the tensor-core one
+                     (candidates, exact rescore, proof or exact fallback),
+all of which give the same answer (the tests check it), and keeps the
+fastest. The tile shape of the tensor-core scans is fixed by the hardware
+layout (128 TMEM lanes of queries per CTA, 256 base rows per MMA, two
+accumulator buffers in the 512 TMEM columns); the CTA-pair knob is the
+queries-per-tile choice (128 or 256).
+
+    python -m fvgb300.autotune [--shapes all|fp16|fp8|ivf] [--out tuning/gb300.json]
 
 Data: the seeded synthetic mixtures of the benchmark configurations
 (fvgb300.datasets), queries fresh draws from the same mixture.
@@ -44,6 +59,110 @@ SHAPES = {
     "fp16_ip_1M_q1_k100": ("fp16", "ip", 1_000_000, 768, 1, 100, "FP16_IP_UNIT", 0.5, (4,)),
     "fp8_l2_10M_q10000_k100": ("fp8", "l2", 10_000_000, 96, 10_000, 100, "FP8_L2", 0.0, (4, 3, 2)),
 }
+
+
+# mode, N, dim, nlist, m_pq (PQ), queries, k, nprobe, rerank_k, mask fraction, rows
+IVF_SHAPES = {
+    f"ivf_{mode}_10M_nprobe{npb}": (mode, 10_000_000, 128, 16384, 32, 10_000, 10, npb, 400, 0.10, "zipf")
+    for mode in ("pq", "rabitq") for npb in (8, 32, 128)
+}
+IVF_SHAPES.update({
+    f"ivf_sq8_1M_768_nprobe{npb}": ("sq8", 1_000_000, 768, 4096, 0, 1024, 10, npb, 0, 0.0, "FP16_IP_UNIT_RAWMEANS")
+    for npb in (16, 64)
+})
+
+
+def _ivf_ranges(n, dim, nlist, nq, nprobe):
+    """The shape range an IVF entry applies to: base within 4x, nlist within
+    2x, dimension within 1.5x, batch within 2x (batches of 1-64 form one
+    range), nprobe halfway to the neighbouring tuned values."""
+    nq_range = [1, 64] if nq <= 64 else [nq // 2, nq * 2]
+    np_range = [max(1, (nprobe * 2) // 3), min(256, nprobe + nprobe // 2)]
+    return {"dim": [max(1, int(dim / 1.5)), int(dim * 1.5)], "n": [max(1, n // 4), n * 4],
+            "nlist": [max(1, nlist // 2), nlist * 2], "nq": nq_range, "nprobe": np_range}
+
+
+def tune_ivf_shape(name, spec, runs=3, nsub=100, log=print):
+    import ctypes as C
+
+    import torch
+
+    from . import _lib, datasets, scan
+    from .index import BUILD_IVF_PQ, BUILD_IVF_RABITQ, BUILD_IVF_SQ8, GpuVectorIndex, IndexConfig
+
+    mode, n, dim, nlist, m_pq, nq, k, nprobe, rerank, mask_frac, rows_kind = spec
+    dev = torch.device("cuda", 0)
+    metric = "l2" if rows_kind == "zipf" else "ip"
+    if rows_kind == "zipf":
+        rows, centers, qgen, _ = datasets.zipf_ivf_data(n, dim, nlist, 3, dev)
+        queries = qgen(nq, 4242).contiguous()
+        flags = {"pq": BUILD_IVF_PQ, "rabitq": BUILD_IVF_RABITQ}[mode]
+        idx = GpuVectorIndex(IndexConfig(dim=dim, nlist=nlist, m_pq=m_pq, metric=metric, build_flags=flags,
+                                         kmeans_iters_given=2, train_rows=min(n, 4 * nlist * 64), pq_iters=10,
+                                         seed=3))
+        idx.build_device(rows, centers)
+    else:
+        mix = getattr(datasets, rows_kind)
+        rows = datasets.sample_torch(mix, n, seed=1, stream=0, device=dev)
+        queries = datasets.sample_torch(mix, nq, seed=1, stream=1, device=dev).contiguous()
+        idx = GpuVectorIndex(IndexConfig(dim=dim, nlist=nlist, metric=metric, build_flags=BUILD_IVF_SQ8,
+                                         kmeans_iters=6, train_rows=min(n, 262144), seed=4))
+        idx.build_device(rows)
+    torch.cuda.synchronize()
+    if mode == "rabitq":
+        tab, opt = idx.rabitq_tables()
+    else:
+        pq_t, sq_t, opt = idx.ivf_tables()
+        tab = pq_t if mode == "pq" else sq_t
+    fn = {"pq": "fv_ivf_pq_search_ex", "sq8": "fv_ivf_sq_search_ex", "rabitq": "fv_ivf_rabitq_search_ex"}[mode]
+    mask = allowed = None
+    if mask_frac > 0:
+        words = datasets.bernoulli_mask_words(n, mask_frac, seed=3)
+        mask = torch.from_numpy(words.view(np.int32)).to(dev)
+        allowed = torch.from_numpy(datasets.unpack_words(words, n)).to(dev)
+    truth = _fp64_topk(rows, queries[:nsub], k, metric, allowed)
+    out = scan.empty_results(nq, k, dev)
+    stream = torch.cuda.current_stream()
+
+    def search():
+        _lib.call(fn, C.byref(tab), C.byref(opt), C.c_void_p(queries.data_ptr()), nq, k, nprobe, rerank,
+                  {"l2": 0, "ip": 2}[metric], None if mask is None else C.c_void_p(mask.data_ptr()),
+                  C.c_void_p(out.data_ptr()), C.c_void_p(stream.cuda_stream))
+
+    results, answer = [], None
+    for pipeline in ((0, 1) if mode == "pq" else (0,)):
+        for split in (-1, 0):
+            for tcc in (0, 1):
+                with scan.tuned(tc_table=0, ivf_pipeline=pipeline, ivf_split=split, ivf_tc_coarse=tcc):
+                    for _ in range(2):
+                        search()
+                    torch.cuda.synchronize()
+                    times = []
+                    for _ in range(runs):
+                        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                        e0.record(stream)
+                        search()
+                        e1.record(stream)
+                        e1.synchronize()
+                        times.append(e0.elapsed_time(e1))
+                res = out.clone()
+                same = answer is None or torch.equal(res, answer)
+                answer = res if answer is None else answer
+                ms = statistics.median(times)
+                results.append({"pipeline": pipeline, "split": split, "tc_coarse": tcc, "ms": ms, "same_answer": same})
+                log(f"{name} pipeline {pipeline} split {split} tc_coarse {tcc}: {ms:.3f} ms same {same}")
+    ids = answer.cpu().numpy()[..., 0].view(np.uint32)
+    best = min(results, key=lambda r: r["ms"])
+    default = next(r for r in results if r["pipeline"] == 0 and r["split"] == -1 and r["tc_coarse"] == 0)
+    del idx
+    torch.cuda.empty_cache()
+    return {"name": name, "mode": mode, **_ivf_ranges(n, dim, nlist, nq, nprobe),
+            "shape": {"n": n, "dim": dim, "nlist": nlist, "m_pq": m_pq, "nq": nq, "k": k, "nprobe": nprobe,
+                      "rerank_k": rerank, "mask_fraction": mask_frac, "rows": rows_kind},
+            "knobs": {"pipeline": best["pipeline"], "split": best["split"], "tc_coarse": best["tc_coarse"]},
+            "measured": {"ms": best["ms"], "qps": nq / (best["ms"] / 1e3), "untuned_ms": default["ms"],
+                         "recall_at_k": _recall(ids[:nsub], truth), "all_answers_equal":
+                             all(r["same_answer"] for r in results), "candidates": len(results)}}
 
 
 def _ranges(n, dim, nq, k):
@@ -158,16 +277,26 @@ def main(argv=None):
     a = ap.parse_args(argv)
     import torch
 
-    names = list(SHAPES) if a.shapes == "all" else [s for s in SHAPES if s.startswith(a.shapes)] \
-        if a.shapes in ("fp16", "fp8") else a.shapes.split(",")
-    entries = [tune_shape(nm, SHAPES[nm], runs=a.runs) for nm in names]
+    every = list(SHAPES) + list(IVF_SHAPES)
+    if a.shapes == "all":
+        names = every
+    elif a.shapes in ("fp16", "fp8", "ivf"):
+        names = [s for s in every if s.startswith(a.shapes)]
+    else:
+        names = a.shapes.split(",")
+    entries = [tune_shape(nm, SHAPES[nm], runs=a.runs) for nm in names if nm in SHAPES]
+    ivf_entries = [tune_ivf_shape(nm, IVF_SHAPES[nm]) for nm in names if nm in IVF_SHAPES]
     out = Path(a.out)
     prev = json.loads(out.read_text()) if out.exists() else {"entries": []}
     keep = [e for e in prev.get("entries", []) if e.get("name") not in {x["name"] for x in entries}]
+    keep_ivf = [e for e in prev.get("ivf_entries", []) if e.get("name") not in {x["name"] for x in ivf_entries}]
     doc = {"device": torch.cuda.get_device_name(0), "date": time.strftime("%Y-%m-%d"),
            "method": "fastest configuration with recall@10 and recall@k >= target vs fp64 exact search "
                      "(median of CUDA-event times around the whole search call)",
-           "entries": keep + entries}
+           "entries": keep + entries,
+           "ivf_method": "fastest of the knob settings, all of which return the same answer (median of CUDA-event "
+                         "times around the whole search call)",
+           "ivf_entries": keep_ivf + ivf_entries}
     out.parent.mkdir(parents=True, exist_ok=True)
     out.write_text(json.dumps(doc, indent=1) + "\n")
     print(f"wrote {len(doc['entries'])} entries to {out}")
