@@ -34,8 +34,10 @@ constexpr int QT = 64;    // queries per CTA
 constexpr int VT = 128;   // base rows per tile
 constexpr int DK = 32;    // dimensions per staged chunk
 constexpr int NT = 256;   // threads per CTA
-constexpr int QS = QT + 1;  // padded row strides (bank-conflict free)
-constexpr int VS = VT + 1;
+// padded row strides of the staged chunks: multiples of 4 floats so that
+// every operand read of the inner loop is one 16-byte shared load
+constexpr int QS = QT + 4;
+constexpr int VS = VT + 4;
 
 struct FlatArgs {
   const float* vectors;
@@ -207,11 +209,13 @@ __global__ void __launch_bounds__(NT) flat_f32_scan_kernel(FlatArgs a) {
       }
 
       auto step = [&](int dd) {
-        float qv[4], xv[8];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) qv[i] = qs[dd * QS + ty * 4 + i];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) xv[j] = xs[dd * VS + tx + 16 * j];
+        // this thread's 4 queries and 8 rows (columns 4 tx.. and 64 + 4 tx..)
+        // of dimension dd: three 16-byte loads
+        const float4 q4 = *reinterpret_cast<const float4*>(qs + dd * QS + ty * 4);
+        const float4 xa = *reinterpret_cast<const float4*>(xs + dd * VS + 4 * tx);
+        const float4 xb = *reinterpret_cast<const float4*>(xs + dd * VS + 64 + 4 * tx);
+        const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
+        const float xv[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -244,7 +248,7 @@ __global__ void __launch_bounds__(NT) flat_f32_scan_kernel(FlatArgs a) {
       const uint64_t wk = wq[qi];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        const int vi = tx + 16 * j;
+        const int vi = (j < 4 ? 0 : 64) + 4 * tx + (j & 3);  // the row of acc[.][j] (see step)
         float dist;
         if (METRIC == METRIC_L2) {
           dist = acc[i][j];
