@@ -383,8 +383,16 @@ __device__ __forceinline__ float sq8_row(const float* __restrict__ qres, const f
 // aligned rows (PQ m_pq = 16, 32, 64; RaBitQ P = 128 MW with 16-byte-aligned
 // meta rows), scanned by the register-prefetching loop with R postings per
 // thread per round, software-pipelined across rounds (PIPE).
+// Resident CTAs per SM each variant is compiled for (its register budget:
+// 4 -> 64, 3 -> 85, 2 -> 128 registers per thread): the list scans are
+// load-latency bound, so occupancy is worth more than registers.
+template <int MODE, int MW, bool PIPE>
+constexpr int ivf_min_blocks() {
+  return (MODE == IVF_PQ && (MW == 4 || (PIPE && MW == 2))) ? 2 : (PIPE || (MODE == IVF_RABITQ && MW >= 4)) ? 3 : 4;
+}
+
 template <int MODE, int MW, int R = 4, bool PIPE = false>
-__global__ void __launch_bounds__(IVF_THREADS, (MODE == IVF_RABITQ && MW == 1) ? 4 : 1) ivf_scan_kernel(IvfArgs a) {
+__global__ void __launch_bounds__(IVF_THREADS, ivf_min_blocks<MODE, MW, PIPE>()) ivf_scan_kernel(IvfArgs a) {
   // a round offers at most IVF_THREADS * R candidates, appended after the
   // shortlist; the buffer is flushed between rounds, so one round must fit
   static_assert((uint32_t)IVF_THREADS * R <= IVF_BUF, "a round of postings must fit the candidate buffer");

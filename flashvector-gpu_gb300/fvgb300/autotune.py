@@ -18,8 +18,11 @@ For each IVF benchmark shape (the 10M-row IVF-PQ / IVF-RaBitQ list scans over
 Zipf-skewed lists at nprobe 8 / 32 / 128, the serving configuration's
 IVF-SQ8 at nprobe 16 / 64) it sweeps
   * ivf.pipeline     the PQ list scan's plain or software-pipelined loop,
-  * ivf.split        posting ranges spread over CTAs for small batches
-                     (automatic) or one CTA per query,
+  * ivf.split        the work items of the persistent list scan: each
+                     query's probed postings as one item (0), cut into 2 or
+                     4 equal (query, posting-range) items merged per query
+                     afterwards (2, 4), or the automatic rule (-1: ranges
+                     only for batches of fewer than 4 queries per SM),
   * ivf.tc_coarse    the exact fp32 coarse probe or the tensor-core one
                      (candidates, exact rescore, proof or exact fallback),
 all of which give the same answer (the tests check it), and keeps the
@@ -131,7 +134,7 @@ def tune_ivf_shape(name, spec, runs=3, nsub=100, log=print):
 
     results, answer = [], None
     for pipeline in ((0, 1) if mode == "pq" else (0,)):
-        for split in (-1, 0):
+        for split in (-1, 0, 2, 4):
             for tcc in (0, 1):
                 with scan.tuned(tc_table=0, ivf_pipeline=pipeline, ivf_split=split, ivf_tc_coarse=tcc):
                     for _ in range(2):

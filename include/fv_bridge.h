@@ -342,10 +342,6 @@ int fv_profile_summary(char* buf, size_t len);
  *                       of long rows (more than two K blocks) run on CTA
  *                       pairs (cta_group::2), each SM streaming half of
  *                       every base tile
- *   "tc.a1"             1 (default): scans of one K block per tile (fp8 rows
- *                       of d <= 125) keep a single resident query tile in
- *                       shared memory and use the room for a deeper base-tile
- *                       ring; 0: the ring layout of longer rows
  *   "tc.table"          1 (default): knobs left automatic and a zero
  *                       over-fetch take the committed autotuner results
  *                       for the call's shape (tuning/gb300.json); 0: ignore
