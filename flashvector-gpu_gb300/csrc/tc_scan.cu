@@ -601,6 +601,10 @@ int launch_tc_scan_ext(const TcTables& t, const float* queries, uint32_t nq, uin
   a.status = status_word();
   a.filters = filters;
   a.tile_stride = 1;
+  // "tc.wait_limit_ns" (0: 2 s) bounds the pipeline's waits; a wait that runs
+  // out ends the scan early and is reported through the status word
+  const int64_t wl = tune_value("tc.wait_limit_ns", 0);
+  a.wait_ns = wl > 0 ? (uint64_t)wl : 2000000000ull;
   // use_pair: the CTA-pair variant (not for the re-scan of flagged queries,
   // whose blocks leave independently)
   auto scan = [&](const TcScanArgs& args, int kl_t, uint32_t splits_n, const char* name, bool use_pair) -> cudaError_t {

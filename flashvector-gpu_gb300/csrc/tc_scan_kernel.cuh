@@ -39,6 +39,7 @@ constexpr int TC_N = 256;                  // base rows per tile (MMA N)
 constexpr int KB_BYTES = 128;              // K bytes per stage row (one 128B swizzle atom)
 constexpr int A_STAGE = TC_M * KB_BYTES;   // 16 KB
 constexpr int B_STAGE = TC_N * KB_BYTES;   // 32 KB
+
 // threads of a scan CTA with G epilogue groups: warp 0 TMA, warp 1 MMA,
 // 4 epilogue warps per group
 __host__ __device__ constexpr int scan_threads(int G) { return 64 + 128 * G; }
@@ -60,6 +61,7 @@ struct TcScanArgs {
   const float* qbound;         // per-query admission bound (distance), or null
   const uint32_t* active;      // per-query flags: only flagged queries are scanned (null: all)
   uint32_t tile_stride;        // scan every tile_stride-th 256-row tile (a sample when > 1)
+  uint64_t wait_ns;            // limit of the pipeline's waits (the drains keep their own)
 };
 
 // PAIR: a CTA of a cta_group::2 pair holds half of each 256-row base tile.
@@ -244,7 +246,7 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
       for (uint32_t i = 0; ok && i < my_tiles; ++i) {
         const int32_t row_b = (int32_t)((t_begin + i) * tstride * TC_N);
         for (uint32_t kb = 0; kb < a.kblocks; ++kb) {
-          if (!tc::mbar_wait(&empty[stage], phase ^ 1, abort_flag, a.status)) {
+          if (!tc::mbar_wait(&empty[stage], phase ^ 1, abort_flag, a.status, a.wait_ns)) {
             ok = false;
             break;
           }
@@ -289,11 +291,11 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
       bool ok = true;
       for (uint32_t i = 0; ok && i < my_tiles; ++i) {
         const uint32_t buf = i & 1, use = i >> 1;
-        if (!tc::mbar_wait(&acc_empty[buf], (use & 1) ^ 1, abort_flag, a.status)) break;
+        if (!tc::mbar_wait(&acc_empty[buf], (use & 1) ^ 1, abort_flag, a.status, a.wait_ns)) break;
         tc::tc_fence_after();
         const uint32_t d_tmem = tmem + buf * TC_N;
         for (uint32_t kb = 0; kb < a.kblocks; ++kb) {
-          if (!tc::mbar_wait(&full[stage], phase, abort_flag, a.status)) {
+          if (!tc::mbar_wait(&full[stage], phase, abort_flag, a.status, a.wait_ns)) {
             ok = false;
             break;
           }
@@ -446,7 +448,7 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
           const uint4 w = __ldcg(reinterpret_cast<const uint4*>(slots + s4));
           smax = max(smax, max(max(w.x, w.y), max(w.z, w.w)));
         }
-      if (!tc::mbar_wait(&acc_full[buf], use & 1, abort_flag, a.status)) break;
+      if (!tc::mbar_wait(&acc_full[buf], use & 1, abort_flag, a.status, a.wait_ns)) break;
       tc::tc_fence_after();
       if (slots && smax != 0xFFFFFFFFu) bound = fminf(bound, order_float(smax));
       refresh();

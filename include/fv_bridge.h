@@ -342,6 +342,12 @@ int fv_profile_summary(char* buf, size_t len);
  *                       of long rows (more than two K blocks) run on CTA
  *                       pairs (cta_group::2), each SM streaming half of
  *                       every base tile
+ *   "tc.wait_limit_ns"  0 (default): the tensor-core scan's pipeline waits give
+ *                       up after 2 s; n > 0: after n ns. A wait that runs
+ *                       out ends the scan early (its answer is not valid)
+ *                       and sets the timeout bit that fv_read_device_status
+ *                       reports; the context stays usable (a short limit
+ *                       exercises that path)
  *   "tc.table"          1 (default): knobs left automatic and a zero
  *                       over-fetch take the committed autotuner results
  *                       for the call's shape (tuning/gb300.json); 0: ignore

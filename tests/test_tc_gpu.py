@@ -487,3 +487,33 @@ def test_cta_pair_scan_matches_single_cta(cuda, fp8, n, dim, nq, k):
         got = res_np(search(t, q, k, "l2"))
     assert scan.device_status() == 0
     assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+
+
+def test_scan_wait_timeout_is_reported_and_the_next_call_is_exact(cuda):
+    """A pipeline wait that runs out ends the scan early without faulting: a
+    test-only 1 ns limit on the tensor-core scan's waits (its tile copies
+    cannot land that fast) makes the kernel abort, drain its copies in
+    flight, free its accumulators and return; the device status word reports
+    the timeout, the context stays usable, and the next call on the same
+    stream, with the normal limit, returns exactly the answer of a call
+    before it. One-CTA scans (short rows: no CTA pairs)."""
+    from fvgb300 import scan
+
+    torch = cuda
+    x = unit_mixture(20000, 64, 32, 0.3, 21)
+    q = unit_mixture(256, 64, 32, 0.3, 22)
+    table = scan.Fp16Table(torch.from_numpy(x).cuda())
+    qt = torch.from_numpy(q).cuda()
+    scan.device_status()  # read and clear
+    with scan.tuned(tc_pair=0):
+        ref = scan.fp16_search(table, qt, 10, "ip", dropin=True).clone()
+        torch.cuda.synchronize()
+        assert scan.device_status() == 0
+        with scan.tuned(tc_wait_limit_ns=1):
+            scan.fp16_search(table, qt, 10, "ip", dropin=True)
+            torch.cuda.synchronize()
+        assert scan.device_status() & 1  # the timeout bit
+        again = scan.fp16_search(table, qt, 10, "ip", dropin=True)
+        torch.cuda.synchronize()
+        assert scan.device_status() == 0
+    assert torch.equal(ref, again)
