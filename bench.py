@@ -65,6 +65,8 @@ def parse_args():
     ap.add_argument("--rates", type=str, default="5000,20000,50000,100000,200000",
                     help="serve: offered request rates (requests/s)")
     ap.add_argument("--serve-seconds", type=float, default=0.5, help="serve: trace length per rate")
+    ap.add_argument("--serve-graphs", type=int, default=0, choices=[0, 1],
+                    help="serve: 1 runs each batch's kernels as one CUDA graph (FvServeConfig.graphs)")
     ap.add_argument("--serve-means", default="unit", choices=["unit", "raw"],
                     help="serve: component means normalised (unit, the default reading of the configuration) "
                          "or left N(0, I) (raw, the fp8 configuration's convention)")
@@ -996,7 +998,8 @@ def run_serve(a, world, rank, local, dev, peaks, peak_kind):
     qall = datasets.sample_torch(mix, max(counts), seed=1, stream=1, device=dev).cpu().numpy()
     sweep = {}
     nsub = 100
-    with SearchBatcher.for_index(idx, max_wait_us=200, max_batch_size=1024, inflight=4) as b:
+    with SearchBatcher.for_index(idx, max_wait_us=200, max_batch_size=1024, inflight=4,
+                                 graphs=bool(a.serve_graphs)) as b:
         fid = b.add_filter(sel)
         # warm-up: every launch class once
         wk = [BatchKey(e, k, p, 0) for e in ("fp16", "ivf_sq8") for k in (10, 100) for p in (16, 64)]
@@ -1040,13 +1043,16 @@ def run_serve(a, world, rank, local, dev, peaks, peak_kind):
         st = b.serve_stats()
         scratch_waits, scratch_peak, scratch_pool = st["scratch_waits"], st["scratch_peak_bytes"], \
             st["scratch_pool_bytes"]
+        graph_inst, graph_fb = st["graph_instantiations"], st["graph_fallbacks"]
     top = sweep[rates[-1]]
     cfg = {"workload": "continuous batching: fp16 flat (1M x 768, IP) + IVF-SQ8 (nlist 4096) resident; requests "
                        "k in {10,100}, nprobe in {16,64}, filter in {none, 20%}; Poisson arrivals",
            "N": a.n, "dim": a.dim, "rates": rates, "max_batch": 1024, "max_wait_us": 200, "inflight": 4,
            "build_seconds": build_s, "l2": "inputs larger than L2 (fp16 base 1.54 GB, SQ8 codes 0.77 GB)",
            "component_means": a.serve_means,
-           "scratch_budget": "512 MiB pool per server (FvServeConfig.scratch_budget_kb = 0)"}
+           "scratch_budget": "512 MiB pool per server (FvServeConfig.scratch_budget_kb = 0)",
+           "graphs": ({"on": True, "instantiations": graph_inst, "plain_launch_batches": graph_fb}
+                      if a.serve_graphs else {"on": False})}
     if a.serve_means == "unit":
         cfg["ivf_recall_note"] = ("the mixture is nearly isotropic (unit centres, sigma 0.3 x sqrt(768) noise): true "
                                   "neighbours spread over almost all 4096 lists, so IVF at nprobe 16-64 finds few; "

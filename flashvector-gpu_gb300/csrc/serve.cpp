@@ -50,6 +50,7 @@ namespace {
 
 constexpr uint32_t kMaxTopK = 256;  // reference clamp (streams.rs:14)
 constexpr size_t kDefaultScratchBudget = (size_t)512 << 20;  // FvServeConfig.scratch_budget_kb = 0
+constexpr size_t kGraphsPerSlot = 64;  // executable graphs kept per stream (FvServeConfig.graphs)
 
 uint64_t now_ns() {
   return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
@@ -123,6 +124,9 @@ struct Slot {
   bool pinned_index = false;
   // this batch's part of the server's scratch pool (index-backed servers)
   size_t scratch_off = 0, scratch_bytes = 0;
+  // FvServeConfig.graphs: executable graphs of this stream's batches by
+  // launch shape (engine, nq, k, nprobe, rerank_k, filtered)
+  std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, bool>, cudaGraphExec_t> graphs;
   // executor-backed servers: a worker thread per slot
   std::vector<float> x_q;
   std::vector<FvRequest> x_reqs;
@@ -211,6 +215,7 @@ class Server {
       }
       if (s->stream) {
         cudaStreamSynchronize(s->stream);
+        for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
         fv_release_stream_scratch(s->stream);
         cudaStreamDestroy(s->stream);
       }
@@ -365,6 +370,8 @@ class Server {
     s->completed = completed_;
     s->failed = failed_;
     s->max_inflight = max_inflight_;
+    s->graph_instantiations = graph_instantiations_.load(std::memory_order_relaxed);
+    s->graph_fallbacks = graph_fallbacks_.load(std::memory_order_relaxed);
     if (completed_ && last_done_ > first_arrival_)
       s->qps = (double)completed_ / ((double)(last_done_ - first_arrival_) / 1e9);
     auto pct = [](std::vector<double> v, double* p50, double* p90, double* p99, double* p999, double* mx,
@@ -619,7 +626,7 @@ class Server {
     // launches (the batch before it on this stream has completed)
     int rc = fv_set_stream_scratch(s->stream, pool_ + s->scratch_off, s->scratch_bytes);
     if (!rc) rc = (int)cudaMemcpyAsync(s->d_in, s->h_in, lay.total, cudaMemcpyHostToDevice, s->stream);
-    if (!rc) rc = index_launch_batch(index_, b, s->stream);
+    if (!rc) rc = cfg_.graphs ? launch_graph(s, b, any_filter) : index_launch_batch(index_, b, s->stream);
     if (!rc)
       rc = (int)cudaMemcpyAsync(s->h_out, s->d_out, (size_t)nq * kmax * sizeof(GpuSearchResult),
                                 cudaMemcpyDeviceToHost, s->stream);
@@ -628,6 +635,57 @@ class Server {
       cudaStreamSynchronize(s->stream);  // nothing enqueued may still use the staging
       complete(s, rc);
     }
+  }
+
+  // The batch's kernels as one CUDA graph: captured on the slot's stream
+  // (thread-local capture: the other threads' CUDA calls are unaffected),
+  // then applied to the slot's executable graph of the same launch shape by
+  // cudaGraphExecUpdate (same kernels; new pointers, scratch and sizes), or
+  // instantiated when the shape is new or the update is refused. The slot's
+  // previous batch has completed, so its graphs are idle.
+  int launch_graph(Slot* s, const BatchLaunch& b, bool any_filter) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return (int)e;
+    const int rc = index_launch_batch(index_, b, s->stream);
+    e = cudaStreamEndCapture(s->stream, &g);
+    if (rc || e != cudaSuccess) {
+      // a capture the driver invalidated (the first launch of a kernel in
+      // the process loads its module, which a capture does not allow) runs
+      // as plain launches; later batches of the shape are captured
+      if (g) cudaGraphDestroy(g);
+      (void)cudaGetLastError();
+      graph_fallbacks_.fetch_add(1, std::memory_order_relaxed);
+      return index_launch_batch(index_, b, s->stream);
+    }
+    const auto key = std::make_tuple(b.engine, b.nq, b.top_k, b.nprobe, b.rerank_k, any_filter);
+    auto it = s->graphs.find(key);
+    cudaGraphExec_t ex = nullptr;
+    if (it != s->graphs.end()) {
+      cudaGraphExecUpdateResultInfo info{};
+      if (cudaGraphExecUpdate(it->second, g, &info) == cudaSuccess) {
+        ex = it->second;
+      } else {
+        (void)cudaGetLastError();  // the refused update leaves no sticky error
+        cudaGraphExecDestroy(it->second);
+        s->graphs.erase(it);
+      }
+    }
+    if (!ex) {
+      if (s->graphs.size() >= kGraphsPerSlot) {
+        cudaGraphExecDestroy(s->graphs.begin()->second);
+        s->graphs.erase(s->graphs.begin());
+      }
+      e = cudaGraphInstantiate(&ex, g, 0);
+      if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return (int)e;
+      }
+      s->graphs[key] = ex;
+      graph_instantiations_.fetch_add(1, std::memory_order_relaxed);
+    }
+    cudaGraphDestroy(g);
+    return (int)cudaGraphLaunch(ex, s->stream);
   }
 
   static void CUDART_CB host_fn(void* p) {
@@ -729,6 +787,8 @@ class Server {
 
   uint64_t total_requests_ = 0, total_batches_ = 0, completed_ = 0, failed_ = 0;
   uint32_t max_inflight_ = 0;
+  std::atomic<uint32_t> graph_instantiations_{0};
+  std::atomic<uint64_t> graph_fallbacks_{0};
   uint64_t first_arrival_ = UINT64_MAX, last_done_ = 0;
   std::vector<double> lat_us_, queue_us_;
 

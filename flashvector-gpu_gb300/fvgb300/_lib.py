@@ -82,7 +82,7 @@ class FvIndexInfo(C.Structure):
 
 class FvServeConfig(C.Structure):
     _fields_ = [("max_batch", U32), ("max_wait_us", U32), ("inflight", U32), ("group_by_params", U32),
-                ("queue_capacity", U32), ("scratch_budget_kb", U32), ("reserved", U32 * 2)]
+                ("queue_capacity", U32), ("scratch_budget_kb", U32), ("graphs", U32), ("reserved", U32)]
 
 
 class FvRequest(C.Structure):
@@ -95,8 +95,9 @@ class FvServeStats(C.Structure):
                 ("completed", C.c_uint64), ("failed", C.c_uint64)] + \
                [(n, C.c_double) for n in ("qps", "p50_us", "p90_us", "p99_us", "p999_us", "max_us", "mean_us",
                                           "queue_p50_us", "queue_p99_us")] + \
-               [("max_inflight", U32), ("reserved", U32), ("scratch_waits", C.c_uint64),
-                ("scratch_split", C.c_uint64), ("scratch_peak_bytes", C.c_uint64), ("scratch_pool_bytes", C.c_uint64)]
+               [("max_inflight", U32), ("graph_instantiations", U32), ("scratch_waits", C.c_uint64),
+                ("scratch_split", C.c_uint64), ("scratch_peak_bytes", C.c_uint64), ("scratch_pool_bytes", C.c_uint64),
+                ("graph_fallbacks", C.c_uint64)]
 
 
 # int (*)(void* user, const FvRequest*, const float* queries, uint32_t nq, uint32_t dim, uint32_t k_stride,

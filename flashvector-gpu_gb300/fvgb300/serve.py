@@ -49,9 +49,10 @@ class BatcherStats:
     avg_batch_size: float
 
 
-def _config(max_wait_us, max_batch_size, inflight, group_by_params, queue_capacity, scratch_budget_kb=0):
+def _config(max_wait_us, max_batch_size, inflight, group_by_params, queue_capacity, scratch_budget_kb=0,
+            graphs=False):
     return _lib.FvServeConfig(max_batch_size, max_wait_us, inflight, 1 if group_by_params else 0, queue_capacity,
-                              scratch_budget_kb, (_lib.U32 * 2)())
+                              scratch_budget_kb, 1 if graphs else 0, 0)
 
 
 class SearchBatcher:
@@ -63,12 +64,14 @@ class SearchBatcher:
     @classmethod
     def for_index(cls, index, max_wait_us: int = 350, max_batch_size: int = 64, inflight: int = 4,
                   group_by_params: bool = False, queue_capacity: int = 0,
-                  scratch_budget_kb: int = 0) -> "SearchBatcher":
+                  scratch_budget_kb: int = 0, graphs: bool = False) -> "SearchBatcher":
         """batcher.rs:89-125 (defaults: 350 us window, 64 requests). Batches
         are admitted by scratch memory: together those in flight hold at most
-        scratch_budget_kb KiB (0: 512 MiB) of device scratch."""
+        scratch_budget_kb KiB (0: 512 MiB) of device scratch. graphs: each
+        batch's kernels run as one CUDA graph (FvServeConfig.graphs)."""
         h = C.c_void_p()
-        cfg = _config(max_wait_us, max_batch_size, inflight, group_by_params, queue_capacity, scratch_budget_kb)
+        cfg = _config(max_wait_us, max_batch_size, inflight, group_by_params, queue_capacity, scratch_budget_kb,
+                      graphs)
         call("fv_serve_create", index._h, C.byref(cfg), C.byref(h))
         return cls(h, index.config.dim, keepalive=index)
 

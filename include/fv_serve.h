@@ -58,7 +58,14 @@ typedef struct {
                                  returns FV_ERR_QUEUE_FULL                                  */
     uint32_t scratch_budget_kb; /* device scratch of all batches in flight together, KiB (0:
                                    512 MiB); one pool of this size is allocated at create  */
-    uint32_t reserved[2];
+    uint32_t graphs;          /* 1: each batch's kernels run as one CUDA graph, captured on
+                                 its stream and applied (cudaGraphExecUpdate) to the
+                                 stream's executable graph of the same launch shape
+                                 (engine, batch size, k, nprobe, rerank_k, filtered or not),
+                                 instantiated when the shape is new; a batch whose capture
+                                 the driver invalidates runs as plain launches; 0: launched
+                                 one by one                                                */
+    uint32_t reserved;
 } FvServeConfig;
 
 typedef struct {
@@ -82,12 +89,15 @@ typedef struct {
     double p50_us, p90_us, p99_us, p999_us, max_us, mean_us;  /* arrival -> completion */
     double queue_p50_us, queue_p99_us;                         /* arrival -> launch     */
     uint32_t max_inflight;
-    uint32_t reserved;
+    uint32_t graph_instantiations; /* executable graphs built since create (graphs = 1)   */
     /* admission by scratch memory */
     uint64_t scratch_waits;       /* times a ready batch waited for scratch to free up      */
     uint64_t scratch_split;       /* batches cut smaller to fit the budget                  */
     uint64_t scratch_peak_bytes;  /* most scratch held by the batches in flight at once     */
     uint64_t scratch_pool_bytes;  /* the budget (pool size)                                 */
+    uint64_t graph_fallbacks;     /* graphs = 1: batches whose capture the driver invalidated
+                                     (a kernel's first launch in the process loads its module)
+                                     and that ran as plain launches, since create           */
 } FvServeStats;
 
 /* A batch executor for a server without an index (host-only use and

@@ -169,7 +169,7 @@ def test_queue_capacity():
 
     cb = _lib.FvServeExecutor(lambda u, r, q, nq, d, ks, out: (gate.wait(5), 0)[1])
     h = C.c_void_p()
-    cfg = _lib.FvServeConfig(1, 0, 1, 1, 2, 0, (_lib.U32 * 2)())
+    cfg = _lib.FvServeConfig(1, 0, 1, 1, 2, 0, 0, 0)
     _lib.call("fv_serve_create_with_executor", 2, C.byref(cfg), cb, None, C.byref(h))
     b = SearchBatcher(h, 2, keepalive=cb)
     key = BatchKey("flat", 1)

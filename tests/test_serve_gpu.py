@@ -58,8 +58,11 @@ def alone(idx, key, q, filt):
                                      {3: "pq", 4: "sq8", 5: "rabitq"}[eng], filt)
 
 
+@pytest.mark.parametrize("graphs", [False, True])
 @pytest.mark.parametrize("group", [False, True])
-def test_identical_alone_and_in_the_mix(served, group):
+def test_identical_alone_and_in_the_mix(served, group, graphs):
+    """graphs: every batch runs as one CUDA graph (captured, applied to the
+    stream's executable of its launch shape)."""
     from fvgb300.serve import SearchBatcher
 
     idx, rows = served
@@ -69,7 +72,7 @@ def test_identical_alone_and_in_the_mix(served, group):
     engines = ["flat", "fp16", "fp8", "ivf_pq", "ivf_sq8", "ivf_rabitq"]
     keys, fids, q = make_mix(160, rng, 64, engines)
     with SearchBatcher.for_index(idx, max_wait_us=2000, max_batch_size=64, inflight=3,
-                                 group_by_params=group) as b:
+                                 group_by_params=group, graphs=graphs) as b:
         fid_map = [b.add_filter(f) for f in filters]
         sfids = [fid_map[f] if f >= 0 else -1 for f in fids]
         # a burst: everything arrives at once, so the batches are mixed
@@ -77,6 +80,7 @@ def test_identical_alone_and_in_the_mix(served, group):
         s = b.serve_stats()
     assert np.all(status == 0)
     assert s["completed"] == len(keys) and s["avg_batch_size"] > 1.0
+    assert (s["graph_instantiations"] > 0) == graphs
     for i, key in enumerate(keys):
         filt = filters[fids[i]] if fids[i] >= 0 else None
         a_ids, a_dist = alone(idx, key, q[i], filt)
@@ -106,13 +110,38 @@ def test_poisson_arrivals_report_latency(served):
     assert s["completed"] == n and s["qps"] > 0 and s["p99_us"] >= s["p50_us"] > 0
 
 
-def test_serving_survives_index_updates(served):
+def test_graph_launches_reuse_executables(served):
+    """The same bursts served twice with graphs: batches of a launch shape
+    already seen on the stream update its executable instead of building one
+    (fewer instantiations than batches), and every pass gives the answers of
+    the kernel-by-kernel launch."""
+    from fvgb300.serve import BatchKey, SearchBatcher
+
+    idx, rows = served
+    q = gen_clustered(256, 64, 24, 31)
+    keys = [BatchKey("fp16", 10), BatchKey("ivf_sq8", 10, 16, 64), BatchKey("fp8", 100), BatchKey("flat", 10)]
+    with SearchBatcher.for_index(idx, max_wait_us=0, max_batch_size=64, inflight=1) as b:
+        want = [_burst(b, key, q) for key in keys]
+    with SearchBatcher.for_index(idx, max_wait_us=0, max_batch_size=64, inflight=1, graphs=True) as b:
+        got1 = [_burst(b, key, q) for key in keys]
+        built = b.serve_stats()["graph_instantiations"]
+        got2 = [_burst(b, key, q) for key in keys]
+        s = b.serve_stats()
+    assert built > 0 and s["graph_instantiations"] < s["total_batches"]
+    for w, g1, g2 in zip(want, got1, got2):
+        for a in (g1, g2):
+            assert np.all(a[2] == 0)
+            assert np.array_equal(a[0], w[0]) and np.array_equal(a[1], w[1])
+
+
+@pytest.mark.parametrize("graphs", [False, True])
+def test_serving_survives_index_updates(served, graphs):
     """Writers wait for the batches in flight; requests after an update see it."""
     from fvgb300.serve import BatchKey, SearchBatcher
 
     idx, rows = served
     marker = np.full((1, 64), 40.0, dtype=np.float32)
-    with SearchBatcher.for_index(idx, max_wait_us=0, inflight=2) as b:
+    with SearchBatcher.for_index(idx, max_wait_us=0, inflight=2, graphs=graphs) as b:
         key = BatchKey("flat", 5)
         before = b.search(key, marker[0])[0]
         new_id = int(idx.add_vectors(marker)[0])
