@@ -29,7 +29,7 @@ struct Knob {
 };
 Knob g_knobs[] = {{"tc.prepass", {-1}}, {"tc.prepass_stride", {0}}, {"tc.prepass_margin", {0}}, {"tc.pair", {-1}},
                   {"tc.table", {1}}, {"ivf.pipeline", {-1}}, {"ivf.split", {-1}}, {"ivf.compact", {1}},
-                  {"ivf.tc_coarse", {-1}}, {"tc.wait_limit_ns", {0}}};
+                  {"ivf.tc_coarse", {-1}}, {"tc.wait_limit_ns", {0}}, {"tc.groups", {-1}}};
 }  // namespace
 
 bool tune_set(const char* key, int64_t value) {

@@ -408,7 +408,7 @@ uint32_t fill_waves(uint32_t s_min, uint32_t nqb, uint32_t ntiles, uint32_t sms,
 struct TcPlan {
   bool fp8 = false, pair = false, prepass = false;
   uint32_t elem = 0, kblocks = 0, shortlist = 0, kl = 0, kl_tmpl = 0;
-  int groups = 1;
+  int groups = 1, pgroups = 1;  // epilogue groups of the main scan and of the pre-pass
   uint32_t nqb = 0, nqb_grid = 0, splits = 0, tps = 0;
   uint32_t pstride = 0, pr = 0, pkl_tmpl = 0, psplits = 0, ptps = 0;
   uint32_t nq_rows = 0, slot_stride = 0;
@@ -427,9 +427,14 @@ TcPlan plan_tc_scan(const TcTables& t, uint32_t nq, uint32_t k, MetricType metri
   const uint32_t shortlist = t.vectors ? std::min<uint32_t>(std::max(k, overfetch * k), 4096u) : k;
   // short K (at most two 64-element fp16 / 128-element fp8 blocks per tile):
   // a tile costs the MMA little and the epilogue much, so two epilogue
-  // groups drain the two accumulator buffers in parallel
-  const int groups = kblocks <= 2 ? 2 : 1;
-  const uint32_t kl_cap = groups == 2 ? 48u : 64u;
+  // groups drain the two accumulator buffers in parallel. Fused fp8 with one
+  // K block and a shortlist above 48 keys (where two groups' heaps hold less
+  // than the shortlist too) runs four ("tc.groups": -1 auto, 2 or 4).
+  const bool fused_fp8 = fp8 && t.fp8_table_scale && metric != METRIC_COSINE && kblocks == 1;
+  const int64_t groups_knob = tune_value("tc.groups", -1);
+  const bool four = fused_fp8 && (groups_knob == 4 || (groups_knob < 0 && shortlist > 48u));
+  const int groups = kblocks > 2 ? 1 : (four ? 4 : 2);
+  const uint32_t kl_cap = groups == 4 ? 32u : (groups == 2 ? 48u : 64u);
   const uint32_t kl = std::min<uint32_t>(kl_cap, shortlist);         // heap entries per (query, range, group)
   const uint32_t kl_tmpl = std::min<uint32_t>(kl_cap, (kl + 15) / 16 * 16);  // heap capacity (template)
   const uint32_t nqb = (nq + TC_M - 1) / TC_M;
@@ -478,10 +483,14 @@ TcPlan plan_tc_scan(const TcTables& t, uint32_t nq, uint32_t k, MetricType metri
   // pre-pass bound instead of the cross-CTA shared one); forced on (knob 1):
   // any base
   const bool prepass = psampled > 0 && (pp_knob == 1 || (pp_knob != 0 && psampled >= 64u));
-  const uint32_t pkl_tmpl = std::min<uint32_t>(kl_cap, (pr + 15) / 16 * 16);
+  // the pre-pass keeps two groups where the main scan runs four: its tiles
+  // are far apart, and two groups alternating them (each its own
+  // accumulator buffer) beat four splitting every tile's columns
+  const int pgroups = groups == 4 ? 2 : groups;
+  const uint32_t pkl_tmpl = std::min<uint32_t>(pgroups == 2 ? 48u : 64u, (pr + 15) / 16 * 16);
   uint32_t psplits = std::max<uint32_t>(1u, std::min<uint32_t>((uint32_t)sms / nqb_grid, psampled));
-  psplits = fill_waves(psplits, nqb_grid, psampled, (uint32_t)sms, groups * pr);
-  while (psplits > 1 && next_pow2(psplits * groups * pr) > 16384u) --psplits;
+  psplits = fill_waves(psplits, nqb_grid, psampled, (uint32_t)sms, pgroups * pr);
+  while (psplits > 1 && next_pow2(psplits * pgroups * pr) > 16384u) --psplits;
   const uint32_t ptps = (psampled + psplits - 1) / psplits;
   psplits = (psampled + ptps - 1) / ptps;
 
@@ -495,13 +504,14 @@ TcPlan plan_tc_scan(const TcTables& t, uint32_t nq, uint32_t k, MetricType metri
   const size_t part_bytes = align_up((size_t)nq * splits * groups * kl * 8, 256);
   const uint32_t slot_stride = ((prepass ? std::max(kl, pr) : kl) + 3) / 4 * 4;
   const size_t slot_bytes = align_up((size_t)nq * slot_stride * 4, 256);
-  const size_t ppart_bytes = prepass ? align_up((size_t)nq * psplits * groups * pr * 8, 256) : 0;
+  const size_t ppart_bytes = prepass ? align_up((size_t)nq * psplits * pgroups * pr * 8, 256) : 0;
   const size_t tau_bytes = prepass ? 2 * qn_bytes : 0;
   P.fp8 = fp8;
   P.elem = elem;
   P.kblocks = kblocks;
   P.shortlist = shortlist;
   P.groups = groups;
+  P.pgroups = pgroups;
   P.kl = kl;
   P.kl_tmpl = kl_tmpl;
   P.nqb = nqb;
@@ -544,7 +554,7 @@ int launch_tc_scan_ext(const TcTables& t, const float* queries, uint32_t nq, uin
   const TcPlan P = plan_tc_scan(t, nq, k, metric, opt);
   const bool fp8 = P.fp8;
   const uint32_t elem = P.elem, kblocks = P.kblocks, shortlist = P.shortlist, kl = P.kl, kl_tmpl = P.kl_tmpl;
-  const int groups = P.groups;
+  const int groups = P.groups, pgroups = P.pgroups;
   const uint32_t nqb = P.nqb, nqb_grid = P.nqb_grid, splits = P.splits, tps = P.tps;
   const bool pair = P.pair, prepass = P.prepass;
   const uint32_t pstride = P.pstride, pr = P.pr, pkl_tmpl = P.pkl_tmpl, psplits = P.psplits, ptps = P.ptps;
@@ -607,9 +617,10 @@ int launch_tc_scan_ext(const TcTables& t, const float* queries, uint32_t nq, uin
   a.wait_ns = wl > 0 ? (uint64_t)wl : 2000000000ull;
   // use_pair: the CTA-pair variant (not for the re-scan of flagged queries,
   // whose blocks leave independently)
-  auto scan = [&](const TcScanArgs& args, int kl_t, uint32_t splits_n, const char* name, bool use_pair) -> cudaError_t {
+  auto scan = [&](const TcScanArgs& args, int kl_t, uint32_t splits_n, const char* name, bool use_pair,
+                  int groups_n) -> cudaError_t {
     ProfScope ps(name, stream);
-    const int g = use_pair ? -1 : groups;
+    const int g = use_pair ? -1 : groups_n;
     const uint32_t grid = (use_pair ? nqb_grid : nqb) * splits_n;
     const CUtensorMap& b = use_pair ? tb_half : tb;
     return fp8 ? dispatch_tc_scan_fp8(kl_t, g, (int)metric, t.fp8_table_scale, ta, b, args, grid, stream)
@@ -624,9 +635,9 @@ int launch_tc_scan_ext(const TcTables& t, const float* queries, uint32_t nq, uin
     p.kl = pr;
     p.share = 1;  // the pre-pass heap holds its whole "shortlist" (pr keys)
     p.tile_stride = pstride;
-    e = scan(p, (int)pkl_tmpl, psplits, fp8 ? "tc_prepass_fp8" : "tc_prepass_fp16", pair);
+    e = scan(p, (int)pkl_tmpl, psplits, fp8 ? "tc_prepass_fp8" : "tc_prepass_fp16", pair, pgroups);
     if (e != cudaSuccess) return (int)e;
-    const uint32_t total = psplits * groups * pr, pow2 = next_pow2(total);
+    const uint32_t total = psplits * pgroups * pr, pow2 = next_pow2(total);
     e = cudaFuncSetAttribute(tc_tau_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(pow2 * 8));
     if (e != cudaSuccess) return (int)e;
     {
@@ -643,7 +654,7 @@ int launch_tc_scan_ext(const TcTables& t, const float* queries, uint32_t nq, uin
   a.kl = kl;
   a.share = (kl == shortlist && !prepass) ? 1u : 0u;
   a.qbound = tau;
-  e = scan(a, (int)kl_tmpl, splits, fp8 ? "tc_scan_fp8" : "tc_scan_fp16", pair);
+  e = scan(a, (int)kl_tmpl, splits, fp8 ? "tc_scan_fp8" : "tc_scan_fp16", pair, groups);
   if (e != cudaSuccess) return (int)e;
 
   SelectArgs s{partial, splits * groups, kl, next_pow2(splits * groups * kl), shortlist, k, queries, t.vectors, t.dim,
@@ -665,7 +676,7 @@ int launch_tc_scan_ext(const TcTables& t, const float* queries, uint32_t nq, uin
     f.qbound = nullptr;
     f.active = redo;
     f.share = 0;
-    e = scan(f, (int)kl_tmpl, splits, fp8 ? "tc_rescan_fp8" : "tc_rescan_fp16", false);
+    e = scan(f, (int)kl_tmpl, splits, fp8 ? "tc_rescan_fp8" : "tc_rescan_fp16", false, groups);
     if (e != cudaSuccess) return (int)e;
     SelectArgs r = s;
     r.tau = nullptr;

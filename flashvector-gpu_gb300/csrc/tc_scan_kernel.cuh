@@ -65,19 +65,32 @@ struct TcScanArgs {
 };
 
 // PAIR: a CTA of a cta_group::2 pair holds half of each 256-row base tile.
-template <int KL, int STAGES, int G, bool PAIR = false>
+// COLS: the epilogue stages per-column norms / scales (not the fused fp8
+// forms, whose accumulator is the ranking value). A_STAGES: query-tile
+// buffers (1 where the query tile is always resident).
+template <int KL, int STAGES, int G, bool PAIR = false, bool COLS = true, int A_STAGES = STAGES>
 struct ScanSmem {
   static constexpr size_t b_stage = PAIR ? B_STAGE / 2 : B_STAGE;
   static constexpr size_t a_off = 0;
-  static constexpr size_t b_off = a_off + (size_t)STAGES * A_STAGE;
+  static constexpr size_t b_off = a_off + (size_t)A_STAGES * A_STAGE;
   static constexpr size_t heap_off = b_off + (size_t)STAGES * b_stage;
   static constexpr size_t col_off = heap_off + (size_t)G * KL * TC_M * 8;  // [4G warps][2][TC_N] floats
-  static constexpr size_t cmask_off = col_off + 4 * G * 2 * TC_N * 4;      // [4G warps][8] words
+  static constexpr size_t cmask_off = col_off + (COLS ? 4 * G * 2 * TC_N * 4 : 0);  // [4G warps][8] words
   static constexpr size_t bar_off = cmask_off + 4 * G * 8 * 4;          // barriers
   static constexpr size_t nbars = 2 * STAGES + 5;
   static constexpr size_t misc_off = bar_off + nbars * 8;
   static constexpr size_t bytes = misc_off + 16 + 1024;                 // + alignment slack
 };
+
+// The fused fp8 forms (table scale, L2 / inner product): the accumulator is
+// the ranking value, so no column data is staged.
+template <bool FP8, int METRIC, bool TS>
+constexpr bool kFusedScan = FP8 && TS && METRIC != METRIC_COSINE;
+
+// G = 4 runs only the fused fp8 forms with one K block per tile, whose query
+// tile is resident: one query-tile buffer.
+template <bool FP8, int KL, int STAGES, int METRIC, int G, bool PAIR, bool TS>
+using ScanLayout = ScanSmem<KL, STAGES, G, PAIR, !kFusedScan<FP8, METRIC, TS>, G == 4 ? 1 : STAGES>;
 
 // Sift `key` down from position i of a max-heap of kl keys stored with
 // stride TC_M (one heap per query row of the block).
@@ -141,8 +154,17 @@ static __device__ __forceinline__ float select32(const float* v, int j) {
 // groups drain every tile, group g the columns [128 g, 128 g + 128) of it,
 // so the MMA of tile i + 1 (the other accumulator buffer) runs while tile i
 // is drained. A sampled scan (tile stride > 1, whose tile loads are further
-// apart) alternates tiles instead: group g drains tiles g, g + 2, .., so
-// each group's wait for its next tile overlaps the other group's work.
+// apart) alternates tiles instead: group g drains tiles g, g + 2, .. (each
+// group owns one buffer), so each group's wait for its next tile overlaps
+// the other group's work.
+//
+// G = 4 (fused fp8 with one K block per tile, shortlists above 48 keys; the
+// host runs that call's sampled pre-pass with G = 2): 16 epilogue warps,
+// group g draining the 32-column chunks g and g + 4 of every tile, in any
+// scan (alternating tiles would put two groups on one accumulator buffer,
+// and a parity wait cannot tell its phase from the phase two uses later).
+// Heaps of at most 32 keys fit four groups' heaps in shared memory;
+// interleaved chunks spread runs of consecutive slots over the groups.
 //
 // PAIR: the CTA is one of a cluster of two (a cta_group::2 pair) sharing the
 // same base range: CTA r holds query block 2p + r and rows [128 r, 128 r +
@@ -155,7 +177,7 @@ static __device__ __forceinline__ float select32(const float* v, int j) {
 template <bool FP8, int KL, int STAGES, int METRIC, int G, bool PAIR, bool TS>
 __global__ void __launch_bounds__(scan_threads(G), 1)
     tc_scan_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcScanArgs a) {
-  using L = ScanSmem<KL, STAGES, G, PAIR>;
+  using L = ScanLayout<FP8, KL, STAGES, METRIC, G, PAIR, TS>;
   constexpr uint32_t b_stage = (uint32_t)L::b_stage;
   constexpr int SCAN_THREADS = scan_threads(G);
   extern __shared__ uint8_t smem_raw[];
@@ -195,7 +217,7 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
     if (!__syncthreads_or(any)) return;
   }
   const uint32_t tstride = a.tile_stride ? a.tile_stride : 1u;
-  const bool col_split = G == 2 && tstride == 1;
+  const bool col_split = G == 4 || (G == 2 && tstride == 1);
   const uint32_t ntiles = ((a.n + TC_N - 1) / TC_N + tstride - 1) / tstride;
   const uint32_t t_begin = split * a.tiles_per_split;
   const uint32_t t_end = min(t_begin + a.tiles_per_split, ntiles);
@@ -454,6 +476,55 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
       refresh();
 
       const uint32_t t_row = tmem + ((uint32_t)(quad * 32) << 16) + buf * TC_N;
+      if constexpr (G == 4) {
+        // fused fp8, the group's 32-column chunks at 32 g and 128 + 32 g: the
+        // accumulator is the ranking value (v = sc * acc, sc < 0), so a
+        // larger accumulator is better; a chunk whose largest value cannot
+        // enter is skipped whole
+        auto chunk32 = [&](const uint32_t (&rr)[32], uint32_t col, uint32_t m32) {
+          if (m32 == 0u) return;
+          auto max3 = [](float x, float y, float z) {
+            float d;
+            asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(x), "f"(y), "f"(z));
+            return d;
+          };
+          float v[32];
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(rr[j]);
+          float t1[11];
+#pragma unroll
+          for (int j = 0; j < 10; ++j) t1[j] = max3(v[3 * j], v[3 * j + 1], v[3 * j + 2]);
+          t1[10] = fmaxf(v[30], v[31]);
+          const float top = fmaxf(max3(max3(t1[0], t1[1], t1[2]), max3(t1[3], t1[4], t1[5]), max3(t1[6], t1[7], t1[8])),
+                                  fmaxf(t1[9], t1[10]));
+          if (!(top >= thr)) return;
+          uint32_t pass = 0;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) pass |= (uint32_t)(v[j] >= thr) << j;
+          pass &= m32;
+          while (pass) {
+            const int j = __ffs(pass) - 1;
+            pass &= pass - 1;
+            const float x = select32(v, j) * sc;
+            const float d = METRIC == METRIC_L2 ? fmaxf(0.f, qn + x) : x;
+            if (d < worst && d <= bound) {
+              keep(d, v0 + col + (uint32_t)j);
+              refresh();
+            }
+          }
+        };
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+          const uint32_t col = 128u * (uint32_t)h + 32u * (uint32_t)grp;
+          uint32_t ra[32];
+          __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent insertions
+          tc::tmem_ld32_async(t_row + col, ra);
+          uint32_t m32 = qvalid ? cm[col >> 5] : 0u;
+          if (qf.words) m32 &= filter_word(qf, (v0 + col) >> 5);
+          tc::tmem_wait_ld(ra);
+          chunk32(ra, col, m32);
+        }
+      } else {
 #pragma unroll 1
       for (int c0 = c_lo; c0 < c_hi; c0 += 64) {
         uint32_t ra[32], rb[32];
@@ -562,6 +633,7 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
         };
         chunk(std::integral_constant<bool, fused>{});
       }
+      }
       tc::tc_fence_before();
       __syncwarp();
       if (lane == 0) {
@@ -608,7 +680,7 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
 template <bool FP8, int KL, int STAGES, int METRIC, int G, bool PAIR = false, bool TS = true>
 cudaError_t launch_scan_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a, uint32_t grid,
                                cudaStream_t stream) {
-  using L = ScanSmem<KL, STAGES, G, PAIR>;
+  using L = ScanLayout<FP8, KL, STAGES, METRIC, G, PAIR, TS>;
   static_assert(L::bytes <= 227 * 1024, "scan shared memory above the 227 KB per-CTA limit");
   auto kern = tc_scan_kernel<FP8, KL, STAGES, METRIC, G, PAIR, TS>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes);
@@ -638,8 +710,9 @@ cudaError_t launch_scan_kernel(const CUtensorMap& ta, const CUtensorMap& tb, con
 
 // groups == 2 (short K: one or two K blocks per tile, where the epilogue
 // rather than the MMA bounds a tile) halves the stage ring and caps the heap
-// at 48 entries so that two groups' heaps fit next to it. groups == -1
-// selects the CTA-pair variant (grid = 2 CTAs per cluster).
+// at 48 entries so that two groups' heaps fit next to it; groups == 4 (fused
+// fp8, one K block) caps it at 32. groups == -1 selects the CTA-pair
+// variant (grid = 2 CTAs per cluster).
 template <bool FP8, int METRIC, bool TS>
 cudaError_t dispatch_scan_kl(int kl, int groups, const CUtensorMap& ta, const CUtensorMap& tb, const TcScanArgs& a,
                              uint32_t grid, cudaStream_t stream) {
@@ -652,6 +725,16 @@ cudaError_t dispatch_scan_kl(int kl, int groups, const CUtensorMap& ta, const CU
       case 48: return launch_scan_kernel<FP8, 48, 5, METRIC, 1, true, TS>(ta, tb, a, grid, stream);
       default: return launch_scan_kernel<FP8, 64, 4, METRIC, 1, true, TS>(ta, tb, a, grid, stream);
     }
+  }
+  if (groups == 4) {
+    // fused fp8 with one K block per tile only (the layout keeps one
+    // query-tile buffer); heaps of 16 or 32 keys
+    if constexpr (kFusedScan<FP8, METRIC, TS>) {
+      if (a.kblocks != 1) return cudaErrorInvalidValue;
+      if (kl <= 16) return launch_scan_kernel<FP8, 16, 4, METRIC, 4, false, TS>(ta, tb, a, grid, stream);
+      return launch_scan_kernel<FP8, 32, 2, METRIC, 4, false, TS>(ta, tb, a, grid, stream);
+    }
+    return cudaErrorInvalidValue;
   }
   if (groups == 2) {
     switch (kl) {

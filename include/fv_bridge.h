@@ -342,6 +342,13 @@ int fv_profile_summary(char* buf, size_t len);
  *                       of long rows (more than two K blocks) run on CTA
  *                       pairs (cta_group::2), each SM streaming half of
  *                       every base tile
+ *   "tc.groups"         -1 (default): fp8 scans of a table-scale table (L2,
+ *                       inner product) with one K block per tile and a
+ *                       shortlist above 48 keys drain each tile with four
+ *                       epilogue groups (16 warps, heaps of <= 32 keys),
+ *                       other short-row scans with two (heaps of <= 48);
+ *                       2 or 4: that many wherever the four-group form
+ *                       applies. Same answers
  *   "tc.wait_limit_ns"  0 (default): the tensor-core scan's pipeline waits give
  *                       up after 2 s; n > 0: after n ns. A wait that runs
  *                       out ends the scan early (its answer is not valid)

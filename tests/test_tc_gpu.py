@@ -489,6 +489,34 @@ def test_cta_pair_scan_matches_single_cta(cuda, fp8, n, dim, nq, k):
     assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
 
 
+@pytest.mark.parametrize("metric", ["l2", "ip"])
+@pytest.mark.parametrize(
+    "n,dim,nq,k,prepass,masked",
+    [(100_001, 96, 300, 100, -1, False), (60_000, 96, 257, 100, 1, False), (40_000, 112, 129, 64, 1, True),
+     (70_000, 70, 200, 100, 0, True), (3_000, 96, 1, 16, -1, False)],
+)
+def test_fp8_four_group_epilogue_matches_two_groups(cuda, metric, n, dim, nq, k, prepass, masked):
+    """Table-scale fp8 rows of one K block: four epilogue groups (16 warps,
+    interleaved 32-column chunks, heaps of <= 32 keys, more ranges) give the
+    same answers as two groups bit for bit -- partial last tiles, odd query
+    blocks, the sampled pre-pass on and off, a packed mask, a single query."""
+    from fvgb300 import datasets, scan
+
+    torch = cuda
+    base = unit_mixture(n, dim, 256, 0.4, n + dim)
+    queries = unit_mixture(nq, dim, 256, 0.4, nq + 5)
+    t = scan.Fp8Table(torch.from_numpy(base).cuda())
+    assert t.pd <= 128
+    q = torch.from_numpy(queries).cuda()
+    mask = torch.from_numpy(datasets.bernoulli_mask_words(n, 0.5, 11).view(np.int32)).cuda() if masked else None
+    with scan.tuned(tc_groups=2, tc_prepass=prepass):
+        ref = res_np(scan.fp8_search(t, q, k, metric, mask=mask))
+    with scan.tuned(tc_groups=4, tc_prepass=prepass):
+        got = res_np(scan.fp8_search(t, q, k, metric, mask=mask))
+    assert scan.device_status() == 0
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+
+
 def test_scan_wait_timeout_is_reported_and_the_next_call_is_exact(cuda):
     """A pipeline wait that runs out ends the scan early without faulting: a
     test-only 1 ns limit on the tensor-core scan's waits (its tile copies
