@@ -9,13 +9,14 @@
 //
 // The scan kernel itself (tc_scan_kernel.cuh) is instantiated per precision
 // in tc_scan_fp16.cu / tc_scan_fp8.cu. Machine mapping (one CTA per SM,
-// 192 threads):
+// 64 + 128 G threads for G epilogue groups):
 //   warp 0    TMA producer: per K block, a 128-query tile (A) and a 256-row
 //             base tile (B), 128-byte-swizzled, into a STAGES-deep ring;
 //   warp 1    TMEM owner + single-thread tcgen05.mma issuer (M=128, N=256,
 //             fp32 accumulators, two 256-column buffers so the epilogue of
 //             tile i overlaps the MMAs of tile i+1);
-//   warps 2-5 epilogue: thread r owns query r of the block (TMEM lane r),
+//   warps 2.. epilogue, 4 warps per group: thread r of a group owns query r
+//             of the block (TMEM lane r),
 //             turns dot products into distances, applies the slot mask and
 //             keeps that query's best KL (distance, slot) keys in a shared-
 //             memory max-heap. No distance matrix ever reaches HBM.
