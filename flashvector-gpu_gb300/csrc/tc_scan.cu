@@ -21,7 +21,7 @@
 //             keeps that query's best KL (distance, slot) keys in a shared-
 //             memory max-heap. No distance matrix ever reaches HBM.
 // A CTA scans a contiguous range of base tiles; the per-(query, range)
-// heaps are merged by tc_select_kernel, which also rescoring in fp32.
+// heaps are merged by tc_select_kernel, which also rescores them in fp32.
 #include <cmath>
 #include <cuda_fp16.h>
 #include <cuda_fp8.h>
