@@ -9,14 +9,19 @@ batches from the same mixture, k = 10, a Bernoulli(0.5) slot bitmask.
 Synthetic data of that shape stands in for the benchmark corpus.
 
 A step is one call of the drop-in entry point cuda_fp16_tc_search_batch over
-one batch. `value` times K steps with the queries already in HBM (CUDA
-events on the call's stream), the steady state replayed from CUDA graphs
-captured from that call (one graph per query buffer; --no-graph times the
-eager calls); the per-kernel split and the roofline's kernel time come from
-a second pass of the same K steps with the library's per-kernel event hook,
-so the hook never runs inside the timed region. `e2e` times K steps that
-each copy the batch from pinned host memory, search, and copy the results
-back; `p50_ms` / `p99_ms` time such batches one by one, each waited for.
+one batch. Steps alternate between two streams, each with its own output
+buffer and scratch, so two batches are in flight (one batch's pre-pass and
+select overlap the other's scan). `value` times K steps with the queries
+already in HBM (CUDA events, the second stream joined into the first before
+the end event), the steady state replayed from CUDA graphs captured from
+that call (one graph per query buffer, on its step's stream; --no-graph
+times the eager calls); the per-kernel split and the roofline's kernel time
+come from a second pass of the same K steps on one stream with the
+library's per-kernel event hook, so every kernel is timed alone and the
+hook never runs inside the timed region. `e2e` times K steps that each copy
+the batch from pinned host memory, search, and copy the results back, on
+the same two streams; `p50_ms` / `p99_ms` time such batches one by one on
+one stream, each waited for.
 The base set (1.54 GB fp16 + 3.07 GB fp32) is far larger than L2, so no
 flush is needed.
 
@@ -284,7 +289,9 @@ def run_ours(a, world, rank, local):
     # a created stream (the legacy default stream cannot be captured)
     stream = torch.cuda.Stream(device=dev)
     torch.cuda.set_stream(stream)
-    graph_note = "steady state replayed from CUDA graphs captured from cuda_fp16_tc_search_batch (one per buffer)"
+    graph_note = ("steady state replayed from CUDA graphs captured from cuda_fp16_tc_search_batch (one per query "
+                  "buffer), batches alternating between two streams (two in flight)")
+    streams = [stream, torch.cuda.Stream(device=dev)]
 
     mix = dataclasses.replace(datasets.FP16_IP_UNIT, dim=a.dim)
     base = datasets.sample_torch(mix, a.n, seed=1, stream=0, device=dev)
@@ -295,13 +302,18 @@ def run_ours(a, world, rank, local):
     mask = torch.from_numpy(words.view(np.int32)).to(dev)
     table = scan.Fp16Table(base)
     opts = scan.options(overfetch=a.overfetch, boundary_fp64=1)
-    out = scan.empty_results(a.batch, a.k, dev)
+    outs = [scan.empty_results(a.batch, a.k, dev) for _ in streams]
+    out = outs[0]
 
-    def step(i, q=None):
-        scan.fp16_search(table, batches[i % nbatches] if q is None else q, a.k, "ip", mask=mask, opts=opts, out=out,
-                         dropin=(a.overfetch == 4))
+    def step(i, q=None, s=None):
+        # batch i on stream i % 2 (or stream s) with that stream's output
+        # buffer (and the library's scratch arena of that stream)
+        s = i % len(streams) if s is None else s
+        with torch.cuda.stream(streams[s]):
+            scan.fp16_search(table, batches[i % nbatches] if q is None else q, a.k, "ip", mask=mask, opts=opts,
+                             out=outs[s], dropin=(a.overfetch == 4))
 
-    for i in range(max(a.warmup, 3)):
+    for i in range(max(a.warmup, 4)):
         step(i)
     torch.cuda.synchronize()
 
@@ -314,13 +326,15 @@ def run_ours(a, world, rank, local):
     # ---- steady state as CUDA graphs: one graph per query buffer, each
     # captured from the drop-in call (the arena is already grown by the warm-up)
     graphs = None
-    if not a.no_graph:
+    if a.no_graph:
+        graph_note = "eager launches (--no-graph), batches alternating between two streams (two in flight)"
+    else:
         try:
-            graphs = [scan.Graph.capture(lambda i=i: step(i), stream) for i in range(nbatches)]
+            graphs = [scan.Graph.capture(lambda i=i: step(i), streams[i % len(streams)]) for i in range(nbatches)]
         except Exception as exc:  # capture is refused on some drivers: time the eager calls
             graphs = None
             graph_note = f"eager launches (capture failed: {exc})"
-    run = (lambda i: graphs[i % nbatches].launch(stream)) if graphs else step
+    run = (lambda i: graphs[i % nbatches].launch(streams[i % len(streams)])) if graphs else step
     for i in range(nbatches):
         run(i)
     torch.cuda.synchronize()
@@ -335,8 +349,10 @@ def run_ours(a, world, rank, local):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
+    streams[1].wait_stream(stream)
     for i in range(a.steps):
         run(i)
+    stream.wait_stream(streams[1])
     ev1.record(stream)
     torch.cuda.synchronize()
     launches = scan.launch_count() - l0
@@ -345,33 +361,42 @@ def run_ours(a, world, rank, local):
     dev_ms = ev0.elapsed_time(ev1)
 
     # ---- kernel split: the same steps again with the library's per-kernel
-    # event hook (eager calls, every event on the call's stream)
+    # event hook (eager calls on one stream, so that every kernel's events
+    # time it alone)
     scan.profile_summary()
     scan.profile_enable(True)
     for i in range(a.steps):
-        step(i)
+        step(i, s=0)
     torch.cuda.synchronize()
     scan.profile_enable(False)
     prof = scan.profile_summary()
 
-    # ---- end-to-end through the C ABI with host buffers
+    # ---- end-to-end through the C ABI with host buffers: every step copies
+    # its queries in from pinned memory, searches (the drop-in call, eager)
+    # and copies its results out, on one of two streams in turn, so that one
+    # step's copies and launches overlap the other's kernels
     host_q = [b.cpu().pin_memory() for b in batches]
-    host_out = torch.empty(out.shape, dtype=out.dtype).pin_memory()
-    dq = torch.empty_like(batches[0])
-    for i in range(2):
-        dq.copy_(host_q[i % nbatches], non_blocking=True)
-        step(i, dq)
-        host_out.copy_(out, non_blocking=True)
+    dqs = [torch.empty_like(batches[0]) for _ in streams]
+    host_outs = [torch.empty(out.shape, dtype=out.dtype).pin_memory() for _ in streams]
+
+    def e2e_step(i):
+        j = i % len(streams)
+        with torch.cuda.stream(streams[j]):
+            dqs[j].copy_(host_q[i % nbatches], non_blocking=True)
+            step(i, dqs[j], s=j)
+            host_outs[j].copy_(outs[j], non_blocking=True)
+
+    for i in range(2 * len(streams)):
+        e2e_step(i)
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
     for i in range(a.steps):
-        dq.copy_(host_q[i % nbatches], non_blocking=True)
-        step(i, dq)
-        host_out.copy_(out, non_blocking=True)
+        e2e_step(i)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     barrier()
+    dq, host_out = dqs[0], host_outs[0]  # the latency pass below runs on the first stream
 
     # ---- per-batch latency: each batch copied in, searched, copied out and
     # waited for on its own (a caller that blocks on every batch)
@@ -379,7 +404,7 @@ def run_ours(a, world, rank, local):
     for i in range(max(a.latency_steps, a.steps)):
         t1 = time.perf_counter()
         dq.copy_(host_q[i % nbatches], non_blocking=True)
-        step(i, dq)
+        step(i, dq, s=0)
         host_out.copy_(out, non_blocking=True)
         torch.cuda.synchronize()
         lat.append((time.perf_counter() - t1) * 1e3)
@@ -417,7 +442,7 @@ def run_ours(a, world, rank, local):
     e2e_qps = total_q / e2e_s
 
     # ---- recall@10 and distance error against an fp64 evaluation on device
-    step(0)
+    step(0, s=0)
     torch.cuda.synchronize()
     res = out.cpu().numpy()
     ids = res[..., 0].view(np.uint32).astype(np.int64)
@@ -473,7 +498,9 @@ def run_ours(a, world, rank, local):
             "dtype": "f16", "data": "synthetic", "config": config(a, {"steady_state": graph_note}),
             "recall_at_k": recall, "max_dist_err_vs_fp64": maxerr,
             "e2e": {"value": e2e_qps, "unit": UNIT, "h2d_bytes_per_step": a.batch * a.dim * 4,
-                    "d2h_bytes_per_step": a.batch * a.k * 8, "ms_per_step": e2e_s / a.steps * 1e3},
+                    "d2h_bytes_per_step": a.batch * a.k * 8, "ms_per_step": e2e_s / a.steps * 1e3,
+                    "how": "per step: H2D of the batch from pinned memory, cuda_fp16_tc_search_batch (eager), D2H "
+                           "of the results; steps alternate between two streams"},
             "gpu_launches": launches, "roofline": roof, "kernels": kernels, "clocks": clk, "cpu_baseline": cpu,
             "p50_ms": latency["p50_ms"], "p99_ms": latency["p99_ms"], "latency": latency, "fp8_c2": fp8_block}
     print(json.dumps(line), flush=True)
