@@ -545,14 +545,21 @@ def _recall(ids, truth):
                  / (truth.shape[0] * k))
 
 
-def _dev_time(fn, steps, stream):
+def _dev_time(fn, steps, stream, others=()):
+    """Device time of `steps` calls of fn (CUDA events on `stream`; work on
+    the `others` streams starts after the start event and is joined into
+    `stream` before the end event)."""
     import torch
 
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
+    for o in others:
+        o.wait_stream(stream)
     for i in range(steps):
         fn(i)
+    for o in others:
+        stream.wait_stream(o)
     e1.record(stream)
     torch.cuda.synchronize()
     return e0.elapsed_time(e1) / 1e3
@@ -579,7 +586,8 @@ def fp8_measure(n, dim, batch, k, dev, stream, steps, warmup, peaks, peak_kind, 
     rescore and fp64 boundary, against the project's exact fp32 scan on the
     same data and queries. Both fp8 layouts are measured: the power-of-two
     table scale with norm digits in the MMA (the fast one) and the per-vector
-    max|x| / 448 scales. Returns a dict of the measured numbers."""
+    max|x| / 448 scales. Batches alternate between two streams (two in
+    flight), as the headline's do. Returns a dict of the measured numbers."""
     import numpy as np
     import torch
 
@@ -590,30 +598,40 @@ def fp8_measure(n, dim, batch, k, dev, stream, steps, warmup, peaks, peak_kind, 
     qpool = datasets.sample_torch(mix, batch * 2, seed=2, stream=1, device=dev)
     qb = [qpool[:batch].contiguous(), qpool[batch:].contiguous()]
     table = scan.Fp8Table(base)
-    out = scan.empty_results(batch, k, dev)
+    # batches alternate between two streams, each with its own output buffer
+    # and scratch, so two are in flight (one's pre-pass and select overlap
+    # the other's scan); the kernel split and accuracy passes use one stream
+    streams = [stream, torch.cuda.Stream(device=dev)]
+    outs = [scan.empty_results(batch, k, dev) for _ in streams]
+    out = outs[0]
     # over-fetch 0: the committed autotuner's value for this shape
     fp8_overfetch = 0 if overfetch is None else overfetch
     opts = scan.options(overfetch=fp8_overfetch, boundary_fp64=1)
     tuned_knobs = scan.tune_lookup("fp8", "l2", dim, n, batch, k)
-    step = lambda i, qq=None: scan.fp8_search(table, qb[i % 2] if qq is None else qq, k, "l2",  # noqa: E731
-                                               opts=opts, out=out)
-    for i in range(max(3, warmup)):
+
+    def step(i, qq=None, s=None, tbl=None):
+        s = i % len(streams) if s is None else s
+        with torch.cuda.stream(streams[s]):
+            scan.fp8_search(table if tbl is None else tbl, qb[i % 2] if qq is None else qq, k, "l2", opts=opts,
+                            out=outs[s])
+
+    for i in range(max(4, warmup)):
         step(i)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
     l0 = scan.launch_count()
-    dev_s = _dev_time(step, steps, stream)
+    dev_s = _dev_time(step, steps, stream, streams[1:])
     launches = scan.launch_count() - l0
     clk = clocks.stop()
-    # kernel split: a separate pass with the per-kernel event hook
+    # kernel split: a separate one-stream pass with the per-kernel event hook
     scan.profile_summary()
     scan.profile_enable(True)
-    _dev_time(step, steps, stream)
+    _dev_time(lambda i: step(i, s=0), steps, stream)
     scan.profile_enable(False)
     prof = scan.profile_summary()
-    step(0)
+    step(0, s=0)
     torch.cuda.synchronize()
     res = out.cpu().numpy()
     ids = res[..., 0].view(np.uint32)
@@ -630,14 +648,16 @@ def fp8_measure(n, dim, batch, k, dev, stream, steps, warmup, peaks, peak_kind, 
     e2e_line = None
     if e2e:
         hq = [b.cpu().pin_memory() for b in qb]
-        hout = torch.empty(out.shape, dtype=out.dtype).pin_memory()
-        dq = torch.empty_like(qb[0])
+        houts = [torch.empty(out.shape, dtype=out.dtype).pin_memory() for _ in streams]
+        dqs = [torch.empty_like(qb[0]) for _ in streams]
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for i in range(steps):
-            dq.copy_(hq[i % 2], non_blocking=True)
-            step(i, dq)
-            hout.copy_(out, non_blocking=True)
+            j = i % len(streams)
+            with torch.cuda.stream(streams[j]):
+                dqs[j].copy_(hq[i % 2], non_blocking=True)
+                step(i, dqs[j], s=j)
+                houts[j].copy_(outs[j], non_blocking=True)
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
         e2e_line = {"value": batch * steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": batch * dim * 4,
@@ -645,17 +665,17 @@ def fp8_measure(n, dim, batch, k, dev, stream, steps, warmup, peaks, peak_kind, 
     # the same workload over the per-vector-scale layout (scales max|x| / 448,
     # each row's scale and norm applied per value in the epilogue)
     pv_table = scan.Fp8Table(base, per_vector=True)
-    pv_step = lambda i: scan.fp8_search(pv_table, qb[i % 2], k, "l2", opts=opts, out=out)  # noqa: E731
-    for i in range(max(3, warmup)):
+    pv_step = lambda i, s=None: step(i, s=s, tbl=pv_table)  # noqa: E731
+    for i in range(max(4, warmup)):
         pv_step(i)
     torch.cuda.synchronize()
-    pv_s = _dev_time(pv_step, steps, stream)
+    pv_s = _dev_time(pv_step, steps, stream, streams[1:])
     scan.profile_summary()
     scan.profile_enable(True)
-    _dev_time(pv_step, steps, stream)
+    _dev_time(lambda i: pv_step(i, s=0), steps, stream)
     scan.profile_enable(False)
     pv_prof = scan.profile_summary()
-    pv_step(0)
+    pv_step(0, s=0)
     torch.cuda.synchronize()
     pids = out.cpu().numpy()[..., 0].view(np.uint32)
     kname = "tc_scan_fp8"
