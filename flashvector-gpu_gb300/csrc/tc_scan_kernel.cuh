@@ -528,113 +528,113 @@ __global__ void __launch_bounds__(scan_threads(G), 1)
         }
       } else {
 #pragma unroll 1
-      for (int c0 = c_lo; c0 < c_hi; c0 += 64) {
-        uint32_t ra[32], rb[32];
-        __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent insertions
-        tc::tmem_ld32_async(t_row + c0, ra);
-        tc::tmem_ld32_async(t_row + c0 + 32, rb);
-        uint64_t mw = qvalid ? ((uint64_t)cm[(c0 >> 5) + 1] << 32 | cm[c0 >> 5]) : 0ull;
-        if (qf.words) {
-          const uint32_t w0 = (v0 + (uint32_t)c0) >> 5;
-          mw &= ((uint64_t)filter_word(qf, w0 + 1) << 32) | filter_word(qf, w0);
-        }
-        tc::tmem_wait_ld(ra);
-        tc::reg_fence(rb);
-        if (mw == 0ull) continue;
-        // the chunk's admission test and insertions; FU: the accumulator is
-        // the ranking value (fp8 table-scale tables)
-        auto chunk = [&](auto fu_tag) {
-          constexpr bool FU = decltype(fu_tag)::value;
-          // per-column values v, v[0..32) columns c0.., v[32..64) columns
-          // c0+32..; the distance is D(v): L2  D(v) = max(0, ||q||^2 + v) with
-          // v = ||x||^2 - 2 <q, x> (the query's norm is added after the
-          // minimum, D being monotone), IP  D(v) = v = -<q, x>, cosine the
-          // full expression. FP8 cosine dots carry the query and table scales.
-          float v[64];
-          if constexpr (FU) {
+        for (int c0 = c_lo; c0 < c_hi; c0 += 64) {
+          uint32_t ra[32], rb[32];
+          __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent insertions
+          tc::tmem_ld32_async(t_row + c0, ra);
+          tc::tmem_ld32_async(t_row + c0 + 32, rb);
+          uint64_t mw = qvalid ? ((uint64_t)cm[(c0 >> 5) + 1] << 32 | cm[c0 >> 5]) : 0ull;
+          if (qf.words) {
+            const uint32_t w0 = (v0 + (uint32_t)c0) >> 5;
+            mw &= ((uint64_t)filter_word(qf, w0 + 1) << 32) | filter_word(qf, w0);
+          }
+          tc::tmem_wait_ld(ra);
+          tc::reg_fence(rb);
+          if (mw == 0ull) continue;
+          // the chunk's admission test and insertions; FU: the accumulator is
+          // the ranking value (fp8 table-scale tables)
+          auto chunk = [&](auto fu_tag) {
+            constexpr bool FU = decltype(fu_tag)::value;
+            // per-column values v, v[0..32) columns c0.., v[32..64) columns
+            // c0+32..; the distance is D(v): L2  D(v) = max(0, ||q||^2 + v) with
+            // v = ||x||^2 - 2 <q, x> (the query's norm is added after the
+            // minimum, D being monotone), IP  D(v) = v = -<q, x>, cosine the
+            // full expression. FP8 cosine dots carry the query and table scales.
+            float v[64];
+            if constexpr (FU) {
 #pragma unroll
-            for (int j = 0; j < 64; ++j) v[j] = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
-          } else if (METRIC == METRIC_COSINE) {
+              for (int j = 0; j < 64; ++j) v[j] = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
+            } else if (METRIC == METRIC_COSINE) {
 #pragma unroll
-            for (int j = 0; j < 64; ++j) {
-              float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
-              if (FP8) dot = dot * (qs * cb[TC_N + c0 + j]);
-              v[j] = 1.0f - dot / (sqrtf(qn * cb[c0 + j]) + 1e-8f);
-            }
-          } else {
-            const float4* nb = reinterpret_cast<const float4*>(cb + c0);
-            const float4* sb = reinterpret_cast<const float4*>(cb + TC_N + c0);
+              for (int j = 0; j < 64; ++j) {
+                float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
+                if (FP8) dot = dot * (qs * cb[TC_N + c0 + j]);
+                v[j] = 1.0f - dot / (sqrtf(qn * cb[c0 + j]) + 1e-8f);
+              }
+            } else {
+              const float4* nb = reinterpret_cast<const float4*>(cb + c0);
+              const float4* sb = reinterpret_cast<const float4*>(cb + TC_N + c0);
 #pragma unroll
-            for (int j4 = 0; j4 < 16; ++j4) {
-              const float4 n4 = METRIC == METRIC_L2 ? nb[j4] : make_float4(0.f, 0.f, 0.f, 0.f);
-              const float4 s4 = FP8 ? sb[j4] : make_float4(0.f, 0.f, 0.f, 0.f);
-              const float nv[4] = {n4.x, n4.y, n4.z, n4.w};
-              const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
+              for (int j4 = 0; j4 < 16; ++j4) {
+                const float4 n4 = METRIC == METRIC_L2 ? nb[j4] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 s4 = FP8 ? sb[j4] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float nv[4] = {n4.x, n4.y, n4.z, n4.w};
+                const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
 #pragma unroll
-              for (int e = 0; e < 4; ++e) {
-                const int j = 4 * j4 + e;
-                const float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
-                if (FP8)  // per-row scales: -2 xs (L2) or -xs (IP) in sv
-                  v[j] = METRIC == METRIC_L2 ? fmaf(dot * qs, sv[e], nv[e]) : (dot * qs) * sv[e];
-                else
-                  v[j] = METRIC == METRIC_L2 ? fmaf(-2.0f, dot, nv[e]) : -dot;
+                for (int e = 0; e < 4; ++e) {
+                  const int j = 4 * j4 + e;
+                  const float dot = __uint_as_float(j < 32 ? ra[j] : rb[j - 32]);
+                  if (FP8)  // per-row scales: -2 xs (L2) or -xs (IP) in sv
+                    v[j] = METRIC == METRIC_L2 ? fmaf(dot * qs, sv[e], nv[e]) : (dot * qs) * sv[e];
+                  else
+                    v[j] = METRIC == METRIC_L2 ? fmaf(-2.0f, dot, nv[e]) : -dot;
+                }
               }
             }
-          }
-          // D: distance from v (fused fp8: from the accumulator, v = sc * acc)
-          auto D = [&](float x) {
-            if (FU) x *= sc;
-            return METRIC == METRIC_L2 ? fmaxf(0.f, qn + x) : x;
-          };
-          // better(x, y): the smaller v, i.e. the larger accumulator when fused
-          auto better = [](float x, float y) { return FU ? fmaxf(x, y) : fminf(x, y); };
-          auto may = [&](float x) { return FU ? x >= thr : x <= thr; };
-          // a tree of three-input bests: a 64-column batch whose best cannot
-          // enter is skipped whole (the common case once warm); the pairwise
-          // bests (j, j + 32) are formed only for a batch that passes
-          // best of three in one instruction (three-input min / max)
-          auto best3 = [](float x, float y, float z) {
-            float d;
-            if (FU)
-              asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(x), "f"(y), "f"(z));
-            else
-              asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(x), "f"(y), "f"(z));
-            return d;
-          };
-          float r[22], s8[8];
+            // D: distance from v (fused fp8: from the accumulator, v = sc * acc)
+            auto D = [&](float x) {
+              if (FU) x *= sc;
+              return METRIC == METRIC_L2 ? fmaxf(0.f, qn + x) : x;
+            };
+            // better(x, y): the smaller v, i.e. the larger accumulator when fused
+            auto better = [](float x, float y) { return FU ? fmaxf(x, y) : fminf(x, y); };
+            auto may = [&](float x) { return FU ? x >= thr : x <= thr; };
+            // a tree of three-input bests: a 64-column batch whose best cannot
+            // enter is skipped whole (the common case once warm); the pairwise
+            // bests (j, j + 32) are formed only for a batch that passes
+            // best of three in one instruction (three-input min / max)
+            auto best3 = [](float x, float y, float z) {
+              float d;
+              if (FU)
+                asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(x), "f"(y), "f"(z));
+              else
+                asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(x), "f"(y), "f"(z));
+              return d;
+            };
+            float r[22], s8[8];
 #pragma unroll
-          for (int i = 0; i < 21; ++i) r[i] = best3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
-          r[21] = v[63];
+            for (int i = 0; i < 21; ++i) r[i] = best3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+            r[21] = v[63];
 #pragma unroll
-          for (int i = 0; i < 7; ++i) s8[i] = best3(r[3 * i], r[3 * i + 1], r[3 * i + 2]);
-          s8[7] = r[21];
-          const float top = best3(best3(s8[0], s8[1], s8[2]), best3(s8[3], s8[4], s8[5]), better(s8[6], s8[7]));
-          if (!(mw != 0ull && may(top))) return;
-          float m1[32];
+            for (int i = 0; i < 7; ++i) s8[i] = best3(r[3 * i], r[3 * i + 1], r[3 * i + 2]);
+            s8[7] = r[21];
+            const float top = best3(best3(s8[0], s8[1], s8[2]), best3(s8[3], s8[4], s8[5]), better(s8[6], s8[7]));
+            if (!(mw != 0ull && may(top))) return;
+            float m1[32];
 #pragma unroll
-          for (int j = 0; j < 32; ++j) m1[j] = better(v[j], v[j + 32]);
-          // pairs (j, j+32) that may hold a candidate, walked lane-parallel
-          uint32_t pass = 0;
+            for (int j = 0; j < 32; ++j) m1[j] = better(v[j], v[j + 32]);
+            // pairs (j, j+32) that may hold a candidate, walked lane-parallel
+            uint32_t pass = 0;
 #pragma unroll
-          for (int j = 0; j < 32; ++j) pass |= (uint32_t)may(m1[j]) << j;
-          pass &= (uint32_t)mw | (uint32_t)(mw >> 32);
-          while (pass) {
-            const int j = __ffs(pass) - 1;
-            pass &= pass - 1;
-            const float dlo = D(select32(v, j));
-            const float dhi = D(select32(v + 32, j));
-            if (((mw >> j) & 1ull) && dlo < worst && dlo <= bound) {
-              keep(dlo, v0 + c0 + j);
-              refresh();
+            for (int j = 0; j < 32; ++j) pass |= (uint32_t)may(m1[j]) << j;
+            pass &= (uint32_t)mw | (uint32_t)(mw >> 32);
+            while (pass) {
+              const int j = __ffs(pass) - 1;
+              pass &= pass - 1;
+              const float dlo = D(select32(v, j));
+              const float dhi = D(select32(v + 32, j));
+              if (((mw >> j) & 1ull) && dlo < worst && dlo <= bound) {
+                keep(dlo, v0 + c0 + j);
+                refresh();
+              }
+              if (((mw >> (j + 32)) & 1ull) && dhi < worst && dhi <= bound) {
+                keep(dhi, v0 + c0 + j + 32);
+                refresh();
+              }
             }
-            if (((mw >> (j + 32)) & 1ull) && dhi < worst && dhi <= bound) {
-              keep(dhi, v0 + c0 + j + 32);
-              refresh();
-            }
-          }
-        };
-        chunk(std::integral_constant<bool, fused>{});
-      }
+          };
+          chunk(std::integral_constant<bool, fused>{});
+        }
       }
       tc::tc_fence_before();
       __syncwarp();
