@@ -876,9 +876,11 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind, mode="pq"):
     adm_lens = np.add.reduceat(adm, offs[:-1].astype(np.int64)) if adm.size else np.zeros(nlist, np.int64)
     adm_lens[lens == 0] = 0
 
-    def search(nprobe, qq=q):
+    outs = [out, scan.empty_results(a.batch, a.k, dev)]  # one per stream of the steady state
+
+    def search(nprobe, qq=q, o=0):
         _lib.call(fn_name, C.byref(tab), C.byref(opt), C.c_void_p(qq.data_ptr()), a.batch, a.k, nprobe,
-                  rerank, 0, C.c_void_p(mask.data_ptr()), C.c_void_p(out.data_ptr()),
+                  rerank, 0, C.c_void_p(mask.data_ptr()), C.c_void_p(outs[o].data_ptr()),
                   C.c_void_p(torch.cuda.current_stream().cuda_stream))
 
     nsub = 200
@@ -886,6 +888,9 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind, mode="pq"):
     sweep = {}
     head = None
     cstream = torch.cuda.Stream()
+    # the steady state alternates batches between two streams (each with its
+    # own output buffer, scratch and graph), so two are in flight
+    cstreams = [cstream, torch.cuda.Stream()]
     clocks = ClockSampler(local)  # sampled across the nprobe sweep (graph replays and recall checks)
     clocks.start()
     for nprobe in [int(x) for x in a.nprobe.split(",")]:
@@ -903,21 +908,24 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind, mode="pq"):
         # bytes the scan moves: one list-order mask bit per probed posting; for
         # each admitted one its compacted position, id and row
         moved_step = admitted * (row_bytes + 8) + scanned // 8
-        # graph-captured steady state
-        with torch.cuda.stream(cstream):
-            search(nprobe)
-            torch.cuda.synchronize()
-            graph = scan.Graph.capture(lambda: search(nprobe), cstream)
-            for _ in range(max(3, a.warmup)):
-                graph.launch(cstream)
-            torch.cuda.synchronize()
-            scan.profile_summary()
-            scan.profile_enable(True)  # graph replays record no per-kernel events; timed by the stream events
-            l0 = scan.launch_count()
-            dev_s = _dev_time(lambda i: graph.launch(cstream), a.steps, cstream)
-            launches = scan.launch_count() - l0
-            scan.profile_enable(False)
-            scan.profile_summary()
+        # graph-captured steady state, two batches in flight
+        graphs = []
+        for si, cs in enumerate(cstreams):
+            with torch.cuda.stream(cs):
+                search(nprobe, o=si)
+                torch.cuda.synchronize()
+                graphs.append(scan.Graph.capture(lambda si=si: search(nprobe, o=si), cs))
+        graph = graphs[0]
+        for i in range(2 * max(3, a.warmup)):
+            graphs[i % 2].launch(cstreams[i % 2])
+        torch.cuda.synchronize()
+        scan.profile_summary()
+        scan.profile_enable(True)  # graph replays record no per-kernel events; timed by the stream events
+        l0 = scan.launch_count()
+        dev_s = _dev_time(lambda i: graphs[i % 2].launch(cstreams[i % 2]), a.steps, cstreams[0], cstreams[1:])
+        launches = scan.launch_count() - l0
+        scan.profile_enable(False)
+        scan.profile_summary()
         qps = a.batch * a.steps / dev_s
         sweep[nprobe] = {"qps": qps, "recall_at_10": rec, "ms_per_batch": dev_s / a.steps * 1e3,
                          "scanned_entries_per_batch": scanned, "admitted_entries_per_batch": admitted,
@@ -1000,6 +1008,8 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind, mode="pq"):
             "peak_source": f"{peak_kind} STREAM copy"}
     cfg = {"workload": ("IVF-RaBitQ" if rq else "IVF-PQ") +
                        ", Zipf(1.1) list lengths (min 64), persistent query-queue scan, CUDA graph",
+           "steady_state": "graph replays alternating between two streams (two batches in flight, each stream "
+                           "with its own output buffer and scratch); e2e: the engine's blocking host call",
            "N": a.n, "dim": a.dim, "nlist": nlist, "batch": a.batch, "k": a.k, "rerank": rerank,
            "nprobe": head, "mask_valid_fraction": 0.10, "list_lengths": hist, "build_seconds": build_s,
            "l2": f"inputs larger than L2 ({a.n * row_bytes / 1e6:.0f} MB of codes + {a.n * 4 / 1e6:.0f} MB ids)"}
