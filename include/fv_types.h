@@ -31,10 +31,11 @@ typedef enum {
     METRIC_INNER_PRODUCT = 2
 } MetricType;
 
-/* One (id, distance) hit; 8 bytes, 8-byte aligned (types.h:39-42).
+/* One (id, distance) hit; 8 bytes, 8-byte aligned (types.h:39-42; the
+ * alignment sits on the first member, the form both C11 and C++ accept).
  * Unfilled slots are {0xFFFFFFFF, 1e30f}. */
-typedef struct FV_ALIGN8 {
-    uint32_t id;
+typedef struct {
+    FV_ALIGN8 uint32_t id;
     float distance;
 } GpuSearchResult;
 
