@@ -922,6 +922,10 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind, mode="pq"):
         # bytes the scan moves: one list-order mask bit per probed posting; for
         # each admitted one its compacted position, id and row
         moved_step = admitted * (row_bytes + 8) + scanned // 8
+        # the exact rerank inside the same kernel: per query its shortlist
+        # (min(rerank, admitted postings in its probed lists)) fp32 rows
+        adm_q = torch.from_numpy(adm_lens).to(dev)[probes].sum(dim=1)
+        rerank_step = int(torch.clamp(adm_q, max=rerank).sum()) * a.dim * 4
         # graph-captured steady state, two batches in flight
         graphs = []
         for si, cs in enumerate(cstreams):
@@ -943,7 +947,7 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind, mode="pq"):
         qps = a.batch * a.steps / dev_s
         sweep[nprobe] = {"qps": qps, "recall_at_10": rec, "ms_per_batch": dev_s / a.steps * 1e3,
                          "scanned_entries_per_batch": scanned, "admitted_entries_per_batch": admitted,
-                         "moved_bytes_per_batch": moved_step,
+                         "moved_bytes_per_batch": moved_step, "rerank_bytes_per_batch": rerank_step,
                          "hbm_gbs_algorithmic": bytes_step / (dev_s / a.steps) / 1e9,
                          "graph_kernels": graph.kernels, "launches": launches}
         if head is None or nprobe == 32:
@@ -1007,16 +1011,22 @@ def run_ivf(a, world, rank, local, dev, stream, peaks, peak_kind, mode="pq"):
     h = sweep[head]
     kname = "ivf_rabitq_scan" if rq else "ivf_pq_scan"
     kms = prof[kname]["ms"] / prof[kname]["launches"]
-    achieved = h["moved_bytes_per_batch"] / (kms / 1e3) / 1e9
+    achieved = (h["moved_bytes_per_batch"] + h["rerank_bytes_per_batch"]) / (kms / 1e3) / 1e9
     peak = peaks.get("hbm_gbs", 6800.0)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None, "kernel": kname, "kernel_ms": kms,
             "bytes_counted": "per probed posting one list-order mask bit; per mask-admitted posting its "
                              "4-byte compacted position, 4-byte id and " +
-                             ("16-byte sign bits + 16-byte meta" if rq else "32-byte code row"),
+                             ("16-byte sign bits + 16-byte meta" if rq else "32-byte code row") +
+                             "; per query its rerank shortlist's fp32 rows (dim x 4 bytes each)",
+            "traffic_note": "not scaled from the 2M-row ncu capture: the rerank's bytes grow with the batch, "
+                            "the list bytes with the rows; that capture read 1.08 GB per launch "
+                            "(scan 0.34 GB + rerank gathers at a 49% L2 hit rate)" if rq else None,
             "algorithmic_bytes_all_postings": h["scanned_entries_per_batch"] * (row_bytes + 4),
             "measured_bound": "not HBM: the probed rows are mostly L2-resident (the Zipf head lists are probed "
-                              "by most queries); " + ("the popcount estimate's integer issue" if rq else
+                              "by most queries); " + ("barrier stalls first (block-wide shortlist flushes and "
+                                                      "per-list query setup), then the rerank's dependent row "
+                                                      "gathers (ncu, 2M-row capture)" if rq else
                                                       "shared-memory LUT lookups (ncu: L1/shared 80% of peak, "
                                                       "short-scoreboard stalls first, 2M-row capture)"),
             "peak_source": f"{peak_kind} STREAM copy"}
