@@ -136,69 +136,65 @@ __device__ __forceinline__ float warp_tree_sum(float v) {
   return __shfl_sync(0xffffffffu, v, 0);
 }
 
-__device__ __forceinline__ float warp_metric_distance(const float* __restrict__ q, const float* __restrict__ x,
-                                                      uint32_t dim, int lane, MetricType metric) {
-  // The lane-strided elements are loaded eight steps ahead of the
-  // accumulation, which keeps the per-lane fmaf order (and so the result
-  // bit for bit) while a row's loads are in flight together.
-  constexpr int B = 8;
-  if (metric == METRIC_INNER_PRODUCT) {
-    float dot = 0.f;
-    for (uint32_t d0 = lane; d0 < dim; d0 += 32 * B) {
-      float qa[B], xa[B];
+// R rows against one query at once: every row keeps its own per-lane fmaf
+// chain in dimension order and its own shuffle tree, so each result is the
+// one-row result bit for bit, while the R rows' loads are in flight together.
+// The lane-strided elements of a row are loaded B steps ahead of the
+// accumulation for the same reason.
+template <int R, int B>
+__device__ __forceinline__ void warp_metric_distances(const float* __restrict__ q, const float* const (&x)[R],
+                                                      uint32_t dim, int lane, MetricType metric, float (&out)[R]) {
+  float acc[R], nx[R], nq = 0.f;
 #pragma unroll
-      for (int b = 0; b < B; ++b) {
-        const uint32_t d = d0 + 32 * b;
-        qa[b] = d < dim ? q[d] : 0.f;
-        xa[b] = d < dim ? __ldg(x + d) : 0.f;
-      }
-#pragma unroll
-      for (int b = 0; b < B; ++b)
-        if (d0 + 32 * b < dim) dot = fmaf(qa[b], xa[b], dot);
-    }
-    return -warp_tree_sum(dot);
-  }
-  if (metric == METRIC_COSINE) {
-    float dot = 0.f, nq = 0.f, nx = 0.f;
-    for (uint32_t d0 = lane; d0 < dim; d0 += 32 * B) {
-      float qa[B], xa[B];
-#pragma unroll
-      for (int b = 0; b < B; ++b) {
-        const uint32_t d = d0 + 32 * b;
-        qa[b] = d < dim ? q[d] : 0.f;
-        xa[b] = d < dim ? __ldg(x + d) : 0.f;
-      }
-#pragma unroll
-      for (int b = 0; b < B; ++b)
-        if (d0 + 32 * b < dim) {
-          dot = fmaf(qa[b], xa[b], dot);
-          nq = fmaf(qa[b], qa[b], nq);
-          nx = fmaf(xa[b], xa[b], nx);
-        }
-    }
-    dot = warp_tree_sum(dot);
-    nq = warp_tree_sum(nq);
-    nx = warp_tree_sum(nx);
-    float denom = __fadd_rn(__fmul_rn(sqrtf(nq), sqrtf(nx)), 1e-8f);
-    return __fsub_rn(1.0f, __fdiv_rn(dot, denom));
-  }
-  float acc = 0.f;
+  for (int r = 0; r < R; ++r) acc[r] = nx[r] = 0.f;
   for (uint32_t d0 = lane; d0 < dim; d0 += 32 * B) {
-    float qa[B], xa[B];
+    float qa[B], xa[R][B];
 #pragma unroll
     for (int b = 0; b < B; ++b) {
       const uint32_t d = d0 + 32 * b;
       qa[b] = d < dim ? q[d] : 0.f;
-      xa[b] = d < dim ? __ldg(x + d) : 0.f;
+#pragma unroll
+      for (int r = 0; r < R; ++r) xa[r][b] = d < dim ? __ldg(x[r] + d) : 0.f;
     }
 #pragma unroll
-    for (int b = 0; b < B; ++b)
-      if (d0 + 32 * b < dim) {
-        const float diff = qa[b] - xa[b];
-        acc = fmaf(diff, diff, acc);
+    for (int b = 0; b < B; ++b) {
+      if (d0 + 32 * b >= dim) continue;
+      if (metric == METRIC_COSINE) nq = fmaf(qa[b], qa[b], nq);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (metric == METRIC_INNER_PRODUCT) {
+          acc[r] = fmaf(qa[b], xa[r][b], acc[r]);
+        } else if (metric == METRIC_COSINE) {
+          acc[r] = fmaf(qa[b], xa[r][b], acc[r]);
+          nx[r] = fmaf(xa[r][b], xa[r][b], nx[r]);
+        } else {
+          const float diff = qa[b] - xa[r][b];
+          acc[r] = fmaf(diff, diff, acc[r]);
+        }
       }
+    }
   }
-  return warp_tree_sum(acc);
+  if (metric == METRIC_COSINE) nq = warp_tree_sum(nq);
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const float a = warp_tree_sum(acc[r]);
+    if (metric == METRIC_INNER_PRODUCT) {
+      out[r] = -a;
+    } else if (metric == METRIC_COSINE) {
+      const float denom = __fadd_rn(__fmul_rn(sqrtf(nq), sqrtf(warp_tree_sum(nx[r]))), 1e-8f);
+      out[r] = __fsub_rn(1.0f, __fdiv_rn(a, denom));
+    } else {
+      out[r] = a;
+    }
+  }
+}
+
+__device__ __forceinline__ float warp_metric_distance(const float* __restrict__ q, const float* __restrict__ x,
+                                                      uint32_t dim, int lane, MetricType metric) {
+  const float* const rows[1] = {x};
+  float d[1];
+  warp_metric_distances<1, 8>(q, rows, dim, lane, metric, d);
+  return d[0];
 }
 
 }  // namespace fv

@@ -131,13 +131,24 @@ __device__ void ivf_finish_query(const IvfArgs& a, uint64_t* keys, uint32_t q, u
                                  bool do_rerank, const float* qv) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (do_rerank) {
-    for (uint32_t c = warp; c < S; c += IVF_THREADS / 32) {
-      const uint64_t key = keys[c];
-      if (key == kSentinelKey) continue;
-      const uint32_t vid = key_slot(key);
-      if (vid >= a.num_vectors) continue;
-      const float d = warp_metric_distance(qv, a.vectors + (size_t)vid * a.dim, a.dim, lane, (MetricType)a.metric);
-      if (lane == 0) keys[c] = make_key(d, vid);
+    // Two candidates per warp pass (c and c + NW, both owned by warp c % NW
+    // as with one at a time), so two rows' gathers are in flight per warp.
+    constexpr uint32_t NW = IVF_THREADS / 32;
+    for (uint32_t c0 = warp; c0 < S; c0 += 2 * NW) {
+      const uint32_t c1 = c0 + NW;
+      const uint64_t k0 = keys[c0], k1 = c1 < S ? keys[c1] : kSentinelKey;
+      const bool v0 = k0 != kSentinelKey && key_slot(k0) < a.num_vectors;
+      const bool v1 = k1 != kSentinelKey && key_slot(k1) < a.num_vectors;
+      if (!v0 && !v1) continue;
+      // an unused slot re-reads the other (valid) row and its result is dropped
+      const uint32_t s0 = key_slot(v0 ? k0 : k1), s1 = key_slot(v1 ? k1 : k0);
+      const float* const rows[2] = {a.vectors + (size_t)s0 * a.dim, a.vectors + (size_t)s1 * a.dim};
+      float d[2];
+      warp_metric_distances<2, 4>(qv, rows, a.dim, lane, (MetricType)a.metric, d);
+      if (lane == 0) {
+        if (v0) keys[c0] = make_key(d[0], s0);
+        if (v1) keys[c1] = make_key(d[1], s1);
+      }
     }
     const uint32_t p2 = next_pow2_dev(S);
     for (uint32_t i = S + tid; i < p2; i += IVF_THREADS) keys[i] = kSentinelKey;
